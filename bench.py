@@ -1,0 +1,349 @@
+"""Benchmark of the lattice-gas hot path on GB300.
+
+Workload (one "step" of this benchmark): the FHP-III Karman vortex street on
+an 8192 x 2048 lattice -- pipe walls on the first and last row, a no-slip disc
+of radius 128 centred at (1024, 1024), a forcing column at x = 16 with flip
+probability 0.02, Bernoulli(0.3) occupation of all seven channels from seed 2
+-- advanced by 100 lattice steps followed by the 32 x 32 integer block sums of
+the coarse-graining.  `--steps 100` is the whole 10000-step run.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is site updates per second of the
+whole job with the lattice resident in HBM; `e2e` is the same metric through
+the C ABI with the state uploaded from / downloaded to pinned host memory
+every step; `roofline` is the step kernel against the measured HBM copy
+bandwidth; `cpu_baseline` is the CPU oracle (the reference algorithm in C,
+OpenMP) on this host's cores.  Multi-GPU (torchrun) runs one independent
+lattice per rank (weak scaling; no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W_K, H_K = 8192, 2048
+STEPS_PER_CHUNK = 100
+BLOCK = 32
+MODEL = 3  # FHP-III
+METRIC = "GSite-updates/s & %HBM roofline; batched/served vs plain jobs/s, p50/p99 lat"
+UNIT = "GSite-updates/s"
+WORKLOAD = ("FHP-III Karman vortex street 8192x2048: walls on rows 0 and 2047, no-slip disc r=128 "
+            "at (1024,1024), forcing column x=16 p=0.02, Bernoulli p=0.3 (moving and rest) seed 2; "
+            "bench step = 100 lattice steps + 32x32 integer block sums")
+SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(name):
+    """Per-launch DRAM bytes from a committed ncu summary (line
+    `traffic_bytes_per_launch: N`), or None."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={SMI_FIELDS}", "--format=csv",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9 or not parts[1].split()[0].isdigit():
+                    continue
+                sm.append(int(parts[1].split()[0]))
+                smax = int(parts[2].split()[0])
+                for n, v in zip(names[1:], parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": 0}
+        loaded = [s for s in sm if s > 0.5 * (smax or max(sm))] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def karman_types():
+    from lgca_gb300 import geometry as G
+    return G.disc(W_K, H_K, 1024, 1024, 128)
+
+
+def cpu_baseline(budget_s=12.0):
+    """The oracle (reference algorithm in C, OpenMP on all host threads) on a
+    bounded sample of the same workload: lattice steps of the 8192x2048
+    Karman lattice until ~budget_s seconds have been spent."""
+    from oracle import oracle as O
+    O.build(ref=False)
+    types = karman_types()
+    st = O.init_bernoulli(MODEL, W_K, H_K, types, seed=2, p_move=0.3, p_rest=0.3)
+    O.run(MODEL, st, 1, types=types, seed=2, force_x=16, force_p=0.02)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    cur = st
+    while time.perf_counter() - t0 < budget_s and steps < 400:
+        cur = O.run(MODEL, cur, 2, types=types, seed=2, t0=steps, force_x=16, force_p=0.02)
+        steps += 2
+    dt = time.perf_counter() - t0
+    return {"value": W_K * H_K * steps / dt / 1e9, "unit": UNIT, "cores": O.lib().oracle_threads(),
+            "kind": "port",
+            "sample": f"{steps} lattice steps of the 8192x2048 FHP-III Karman lattice (incl. forcing)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build(ref=False)
+    types = karman_types()
+    st = O.init_bernoulli(MODEL, W_K, H_K, types, seed=2, p_move=0.3, p_rest=0.3)
+    per_step = 2  # lattice steps per benchmark step: a bounded sample of the 100-step chunk
+    t = 0
+    for _ in range(args.warmup):
+        st = O.run(MODEL, st, per_step, types=types, seed=2, t0=t, force_x=16, force_p=0.02)
+        t += per_step
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = O.run(MODEL, st, per_step, types=types, seed=2, t0=t, force_x=16, force_p=0.02)
+        t += per_step
+    dt = time.perf_counter() - t0
+    value = W_K * H_K * per_step * args.steps / dt / 1e9
+    cores = O.lib().oracle_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "reference_step": f"{per_step} lattice steps (bounded sample)",
+                   "parallelism": f"cpu x{cores} threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{per_step * args.steps} lattice steps of the 8192x2048 FHP-III "
+                                   "Karman lattice"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def gate_measurement(gpu, torch, hbm_peak):
+    """Plain single-lattice kernel on the 32768x16384 FHP-III periodic lattice
+    (the roofline gate): HBM bytes per step = 2 * 7/8 B per site."""
+    W, H = 32768, 16384
+    with gpu.GpuLattice(MODEL, W, H, seed=3) as L:
+        L.init_random(0.5, 0.5)
+        s = torch.cuda.ExternalStream(L.stream_ptr())
+        L.collide_and_propagate(3)
+        n = 30
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        L.sync()
+        e0.record(s)
+        L.collide_and_propagate(n)
+        e1.record(s)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / n
+    bytes_step = W * H * 2 * 7 / 8
+    gbs = bytes_step / (ms * 1e-3) / 1e9
+    return {"workload": "FHP-III periodic 32768x16384, plain kernel, 1 step per pass",
+            "ms_per_launch": ms, "gsite_updates_s": W * H / (ms * 1e-3) / 1e9,
+            "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+            "bytes_per_launch": bytes_step, "traffic": profiled_traffic("step_fhp3_32768x16384.md")}
+
+
+def run_ours(args):
+    import torch
+    import lgca_gb300 as gpu
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    gpu.build()
+    hbm_peak, peak_kind = peaks()
+    seed = 2 + 1000 * rank
+    types = karman_types()
+    L = gpu.GpuLattice(MODEL, W_K, H_K, seed=seed)
+    L.set_cell_types(types)
+    L.init_random(0.3, 0.3)
+    L.set_forcing_column(16, 0.02)
+    stream = torch.cuda.ExternalStream(L.stream_ptr())
+    Hb, Wb = H_K // BLOCK, W_K // BLOCK
+    sums = torch.empty((3, Hb, Wb), dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def chunk():
+        L.collide_and_propagate(STEPS_PER_CHUNK)
+        L.block_sums_device(BLOCK, sums[0].data_ptr(), sums[1].data_ptr(), sums[2].data_ptr())
+
+    for _ in range(args.warmup):
+        chunk()
+    L.sync()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    with ClockSampler(dev) as clk:
+        t_wall = time.perf_counter()
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xff)  # L2 flush between timed steps (outside the events)
+            ev[i][0].record(stream)
+            L.collide_and_propagate(STEPS_PER_CHUNK)
+            ev[i][1].record(stream)
+            L.block_sums_device(BLOCK, sums[0].data_ptr(), sums[1].data_ptr(), sums[2].data_ptr())
+            ev[i][2].record(stream)
+        barrier()
+        t_wall = time.perf_counter() - t_wall
+    step_ms = [e[0].elapsed_time(e[2]) for e in ev]
+    kern_ms = [e[0].elapsed_time(e[1]) for e in ev]
+    t_dev = sum(step_ms) / 1e3
+    if ws > 1:
+        tt = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    sites = W_K * H_K * STEPS_PER_CHUNK * args.steps
+    value = sites * ws / t_dev / 1e9
+
+    # roofline of the step kernel: algorithmic bytes per launch / launch time
+    bytes_launch = W_K * H_K * (2 * 7 / 8 + 1 / 8)  # 7 planes read + written, solid plane read
+    launch_s = sum(kern_ms) / 1e3 / (STEPS_PER_CHUNK * args.steps)
+    achieved = bytes_launch / launch_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": profiled_traffic("step_fhp3_karman_8192x2048.md"),
+                "peak_kind": peak_kind, "kernel": "k_step<FHP_II/III, GEOM_NOSLIP>",
+                "bytes_per_launch": bytes_launch,
+                "note": "state (2 x 14.7 MB) + solid plane stay L2-resident within a step chunk"}
+
+    # end to end through the C ABI with host buffers
+    aos = torch.empty((H_K, W_K), dtype=torch.uint8, pin_memory=True)
+    hs = torch.empty((3, Hb, Wb), dtype=torch.int32, pin_memory=True)
+    aos_np, hs_np = aos.numpy(), hs.numpy()
+    L.download(aos_np)
+    e2e_steps = max(1, min(args.steps, 50))
+    barrier()
+    t_e2e = time.perf_counter()
+    for i in range(e2e_steps):
+        L.upload(aos_np)
+        L.collide_and_propagate(STEPS_PER_CHUNK)
+        gpu.lib().lgca_block_sums(L.handle, BLOCK, hs_np[0].ctypes.data, hs_np[1].ctypes.data,
+                                  hs_np[2].ctypes.data)
+        L.download(aos_np)
+    barrier()
+    t_e2e = time.perf_counter() - t_e2e
+    if ws > 1:
+        tt = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e = {"value": W_K * H_K * STEPS_PER_CHUNK * e2e_steps * ws / t_e2e / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": W_K * H_K, "d2h_bytes_per_step": W_K * H_K + 3 * 4 * Hb * Wb,
+           "steps": e2e_steps}
+
+    gate = gate_measurement(gpu, torch, hbm_peak) if rank == 0 else None
+    L.close()
+    if rank == 0:
+        cpu = cpu_baseline() if ws == 1 else None
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "global_batch": ws, "lattice": [W_K, H_K],
+                       "lattice_steps_per_step": STEPS_PER_CHUNK, "block": BLOCK,
+                       "l2": "flushed between timed steps (256 MiB write, outside the events)",
+                       "parallelism": f"replicas x{ws}"},
+            "wall_s": t_wall, "e2e": e2e, "roofline": roofline, "roofline_gate": gate,
+            "cpu_baseline": cpu, "clocks": clk.summary(),
+            "gpu_launches": (STEPS_PER_CHUNK + 1) * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

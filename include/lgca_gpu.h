@@ -1,0 +1,174 @@
+/*
+ * lgca_gpu.h -- C ABI of the GB300 lattice-gas engine (liblgca_gpu.so).
+ *
+ * One handle = one lattice resident in GPU memory as multi-spin-coded
+ * bit-planes (one bit per site and channel, 64 sites per uint64 word), plus
+ * its geometry planes, its step counter and the CUDA stream it runs on.
+ * Plain C types only; every call returns an lgca_status (0 = success) and
+ * records a message retrievable with lgca_last_error().  Calls on one handle
+ * must not overlap from several host threads.  Host buffers are owned by the
+ * caller and may be freed when the call returns.
+ *
+ * The entry points replace the backend half of the reference's Lattice<Model>
+ * interface (keva92/lgca src/lattice.h:32-238, implemented by OMP_Lattice in
+ * src/omp_lattice.{h,cpp}); each declaration names the reference member it
+ * stands in for.  The reference state format -- one byte per cell, bit d =
+ * channel d (src/lgca_bitset.h:31-245, bit dir + 8*cell) -- is the exchange
+ * format of lgca_upload_state / lgca_download_state.
+ *
+ * Randomness: collision chirality and forcing draws come from the
+ * counter-based generator in include/lgca/rng.h, keyed by the lattice seed
+ * and the global step number, so a run is reproducible bit for bit.
+ */
+#ifndef LGCA_GPU_H_
+#define LGCA_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LGCA_GPU_ABI_VERSION 1
+
+typedef enum {
+    LGCA_OK = 0,
+    LGCA_ERR_INVALID = 1,  /* bad argument; nothing was changed             */
+    LGCA_ERR_NOMEM = 2,    /* device allocation failed or over the budget   */
+    LGCA_ERR_CUDA = 3,     /* CUDA runtime error (message has the details)  */
+    LGCA_ERR_TIMEOUT = 4,  /* a bounded device-side wait gave up            */
+    LGCA_ERR_BUSY = 5      /* resource in use                                */
+} lgca_status;
+
+/* Model and cell-type values are those of src/lgca_common.h:49-60. */
+typedef enum { LGCA_HPP = 0, LGCA_FHP_I = 1, LGCA_FHP_II = 2, LGCA_FHP_III = 3 } lgca_model;
+typedef enum { LGCA_FLUID = 0, LGCA_SOLID_NO_SLIP = 1, LGCA_SOLID_SLIP = 2 } lgca_cell_type;
+
+typedef struct lgca_lattice *lgca_handle;
+
+/* ABI version and the device the library was built for. */
+int lgca_abi_version(void);
+const char *lgca_status_string(int status);
+const char *lgca_last_error(lgca_handle h); /* h may be NULL: last global error */
+
+/* Allocate a dim_x x dim_y lattice of `model` on the current CUDA device,
+ * all cells FLUID and empty, step counter 0.  FHP models need an even dim_y
+ * (src/lattice.cpp:141, src/omp_lattice.cpp:103-111).
+ * Replaces: OMP_Lattice<M>::OMP_Lattice + allocate_memory
+ *           (src/omp_lattice.cpp:75-88,457-471). */
+int lgca_create(int model, int dim_x, int dim_y, uint64_t seed, lgca_handle *out);
+
+/* Replaces: OMP_Lattice<M>::~OMP_Lattice + free_memory (src/omp_lattice.cpp:91-97,474-489). */
+int lgca_destroy(lgca_handle h);
+
+/* Dimensions, model, seed and step counter of a handle. */
+int lgca_info(lgca_handle h, int *model, int *dim_x, int *dim_y, uint64_t *seed,
+              uint64_t *step);
+
+/* Set / read the global step number t that keys the step's random draws. */
+int lgca_set_step(lgca_handle h, uint64_t t);
+
+/* Cell-type map, dim_x*dim_y int32 values of lgca_cell_type in row-major
+ * order (x fastest), the layout of the reference's m_cell_type_cpu
+ * (src/lattice.h:80).  Any other value is rejected.
+ * Replaces the effect of apply_cell_type_all / apply_boundary_cell_type_* /
+ * apply_bc_* (src/lattice.cpp:221-395), which build that map on the host. */
+int lgca_set_cell_types(lgca_handle h, const int32_t *types);
+int lgca_get_cell_types(lgca_handle h, int32_t *types);
+
+/* Whole state in the reference byte format: dim_x*dim_y bytes, bit d =
+ * channel d.  Bits >= NUM_DIR are ignored on upload and zero on download.
+ * Replaces: copy_data_to_device / copy_data_from_device
+ * (src/lattice.h:206-211, src/lattice.cpp:422-435). */
+int lgca_upload_state(lgca_handle h, const uint8_t *cells);
+int lgca_download_state(lgca_handle h, uint8_t *cells);
+
+/* Occupy each channel of each FLUID cell independently with probability
+ * p_move (moving channels) or p_rest (rest channel of FHP-II/III), drawn from
+ * the INIT stream; other cells are emptied.
+ * Replaces: Lattice::init_random (src/lattice.cpp:198-217, p = 1/NUM_DIR). */
+int lgca_init_random(lgca_handle h, double p_move, double p_rest);
+
+/* Empty lattice.  Replaces: Lattice::init_zero (src/lattice.cpp:166-170). */
+int lgca_init_zero(lgca_handle h);
+
+/* Forcing column: before each step, every FLUID cell (x, y) with a
+ * west-moving particle and an empty east-moving channel reverses it with
+ * probability p (FORCE stream); x < 0 or p <= 0 disables.  The reversal rule
+ * is the reference's x body force (src/omp_lattice.cpp:295-300, :313-318). */
+int lgca_set_forcing_column(lgca_handle h, int x, double p);
+
+/* Chirality source.  field == NULL: counter-based draw per site and step
+ * (default).  Otherwise dim_x*dim_y bytes (0/1) frozen for all later steps,
+ * which is the reference's own model: a per-cell bit field drawn once
+ * (m_rnd_cpu, src/omp_lattice.cpp:84,198). */
+int lgca_set_chirality(lgca_handle h, const uint8_t *field);
+
+/* Temporal blocking depth: steps advanced per pass over the state in global
+ * memory (1..8).  Results do not depend on it. */
+int lgca_set_temporal_depth(lgca_handle h, int depth);
+
+/* Advance nsteps steps (forcing column, then pull-stream + collide by cell
+ * type), enqueued on the handle's stream; the step counter advances by
+ * nsteps.  Replaces: OMP_Lattice<M>::collide_and_propagate
+ * (src/omp_lattice.cpp:100-249), called nsteps times; its `p` argument is
+ * ignored there and has no counterpart. */
+int lgca_collide_and_propagate(lgca_handle h, int nsteps);
+
+/* Random-cell body force with the reference's semantics: candidate cells
+ * are drawn (FSEQ stream, call counter of the handle) until `forcing`
+ * particles were reverted or 2*num_cells draws were made; bf_dir is 'x', 'y'
+ * or 0.  *reverted (may be NULL) receives the number of reversals.
+ * Replaces: OMP_Lattice<M>::apply_body_force (src/omp_lattice.cpp:254-346). */
+int lgca_apply_body_force(lgca_handle h, int forcing, int bf_dir, uint64_t *reverted);
+
+/* Replaces: Lattice::get_n_particles (src/lattice.cpp:180-195). */
+int lgca_count_particles(lgca_handle h, uint64_t *n);
+
+/* Mean over FLUID cells of cell momentum / cell density (cells with density
+ * 0 add nothing).  Replaces: OMP_Lattice<M>::get_mean_velocity
+ * (src/omp_lattice.cpp:508-557). */
+int lgca_mean_velocity(lgca_handle h, float *ux, float *uy);
+
+/* Exact integer sums over non-overlapping B x B blocks (B >= 1; blocks at
+ * the top/right edge are clipped): N = particles, Jx2 = x momentum in units
+ * of 1/2, Jy = y momentum in units of sin(60 deg) (FHP) or 1 (HPP).  Each
+ * output holds ceil(dim_y/B) rows of ceil(dim_x/B) int32 values.  Host
+ * pointers; the _device variant takes device pointers and does not wait.
+ * No reference counterpart: the integer form of the coarse-graining of
+ * src/omp_lattice.cpp:397-454. */
+int lgca_block_sums(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32_t *Jy);
+int lgca_block_sums_device(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32_t *Jy);
+
+/* Post-processing with the reference's arithmetic: per-cell density and FP32
+ * momentum (dim_x*dim_y and 2*dim_x*dim_y floats, momentum interleaved x,y)
+ * and the coarse means over radius r (coarse grid (dim_x/2r) x (dim_y/2r)).
+ * Any output pointer may be NULL.  Host pointers.
+ * Replaces: OMP_Lattice<M>::post_process = cell_post_process +
+ * mean_post_process (src/omp_lattice.cpp:349-454). */
+int lgca_post_process(lgca_handle h, int r, float *cell_density, float *cell_momentum,
+                      float *mean_density, float *mean_momentum);
+
+/* Wait for all work of the handle. */
+int lgca_sync(lgca_handle h);
+
+/* The cudaStream_t the handle enqueues on (as void*), and a way to replace
+ * it by a caller-owned stream (NULL restores the handle's own stream). */
+void *lgca_stream(lgca_handle h);
+int lgca_set_stream(lgca_handle h, void *stream);
+
+/* Device view of the current state: base pointer of plane 0, words between
+ * consecutive planes, words between consecutive rows.  Valid until the next
+ * call that steps or replaces the state. */
+int lgca_state_device(lgca_handle h, const uint64_t **planes, size_t *plane_stride,
+                      int *row_pitch);
+
+/* Bytes of device memory the handle holds. */
+int lgca_device_bytes(lgca_handle h, size_t *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LGCA_GPU_H_ */

@@ -1,0 +1,254 @@
+"""GB300-native lattice-gas cellular automaton engine.
+
+The compute path is liblgca_gpu.so (CUDA kernels for sm_103a behind the C ABI
+declared in include/lgca_gpu.h).  This module binds that library with ctypes
+and offers `GpuLattice`, a thin handle wrapper with numpy in/out used by the
+tests, the benchmark and Python callers.  There is no CPU fallback: without
+the library (or without a GPU) every call raises.
+
+States exchanged with the host use the reference's format (keva92/lgca
+src/lgca_bitset.h): a uint8 array of shape (dim_y, dim_x), bit d = channel d.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+HPP, FHP_I, FHP_II, FHP_III = 0, 1, 2, 3
+FLUID, SOLID_NO_SLIP, SOLID_SLIP = 0, 1, 2
+NUM_DIR = {HPP: 4, FHP_I: 6, FHP_II: 7, FHP_III: 7}
+MODEL_NAMES = {"HPP": HPP, "FHP_I": FHP_I, "FHP_II": FHP_II, "FHP_III": FHP_III}
+
+LIB_PATH = _build.LIB
+
+_lib = None
+
+
+class LgcaError(RuntimeError):
+    """A C-ABI call returned a non-zero lgca_status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[status {status}] {message}")
+        self.status = status
+
+
+def build(force: bool = False) -> str:
+    return _build.build(force=force)
+
+
+def lib() -> C.CDLL:
+    """The loaded liblgca_gpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: run lgca_gb300.build() (nvcc, sm_103a) first")
+        L = C.CDLL(LIB_PATH)
+        vp, u64, i32p = C.c_void_p, C.c_uint64, C.POINTER(C.c_int32)
+        sig = {
+            "lgca_abi_version": (C.c_int, []),
+            "lgca_status_string": (C.c_char_p, [C.c_int]),
+            "lgca_last_error": (C.c_char_p, [vp]),
+            "lgca_create": (C.c_int, [C.c_int, C.c_int, C.c_int, u64, C.POINTER(vp)]),
+            "lgca_destroy": (C.c_int, [vp]),
+            "lgca_info": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(u64), C.POINTER(u64)]),
+            "lgca_set_step": (C.c_int, [vp, u64]),
+            "lgca_set_cell_types": (C.c_int, [vp, vp]),
+            "lgca_get_cell_types": (C.c_int, [vp, vp]),
+            "lgca_upload_state": (C.c_int, [vp, vp]),
+            "lgca_download_state": (C.c_int, [vp, vp]),
+            "lgca_init_random": (C.c_int, [vp, C.c_double, C.c_double]),
+            "lgca_init_zero": (C.c_int, [vp]),
+            "lgca_set_forcing_column": (C.c_int, [vp, C.c_int, C.c_double]),
+            "lgca_set_chirality": (C.c_int, [vp, vp]),
+            "lgca_set_temporal_depth": (C.c_int, [vp, C.c_int]),
+            "lgca_collide_and_propagate": (C.c_int, [vp, C.c_int]),
+            "lgca_apply_body_force": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(u64)]),
+            "lgca_count_particles": (C.c_int, [vp, C.POINTER(u64)]),
+            "lgca_mean_velocity": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            "lgca_block_sums": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+            "lgca_block_sums_device": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+            "lgca_post_process": (C.c_int, [vp, C.c_int, vp, vp, vp, vp]),
+            "lgca_sync": (C.c_int, [vp]),
+            "lgca_stream": (vp, [vp]),
+            "lgca_set_stream": (C.c_int, [vp, vp]),
+            "lgca_state_device": (C.c_int, [vp, C.POINTER(vp), C.POINTER(C.c_size_t),
+                                            C.POINTER(C.c_int)]),
+            "lgca_device_bytes": (C.c_int, [vp, C.POINTER(C.c_size_t)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a) -> C.c_void_p | None:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(C.c_void_p)
+    return C.c_void_p(int(a))
+
+
+def _check(h, status: int) -> None:
+    if status != 0:
+        msg = lib().lgca_last_error(h).decode(errors="replace")
+        raise LgcaError(status, msg)
+
+
+class GpuLattice:
+    """One lattice resident on the GPU, driven through the C ABI."""
+
+    def __init__(self, model: int, dim_x: int, dim_y: int, seed: int = 0):
+        h = C.c_void_p()
+        st = lib().lgca_create(int(model), int(dim_x), int(dim_y), int(seed), C.byref(h))
+        if st != 0:
+            raise LgcaError(st, lib().lgca_last_error(None).decode(errors="replace"))
+        self._h = h
+        self.model, self.dim_x, self.dim_y, self.seed = int(model), int(dim_x), int(dim_y), int(seed)
+
+    # lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().lgca_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def shape(self):
+        return (self.dim_y, self.dim_x)
+
+    # configuration
+    def set_cell_types(self, types: np.ndarray) -> None:
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        assert t.shape == self.shape, (t.shape, self.shape)
+        _check(self._h, lib().lgca_set_cell_types(self._h, _ptr(t)))
+
+    def get_cell_types(self) -> np.ndarray:
+        t = np.empty(self.shape, np.int32)
+        _check(self._h, lib().lgca_get_cell_types(self._h, _ptr(t)))
+        return t
+
+    def upload(self, state: np.ndarray) -> None:
+        s = np.ascontiguousarray(state, dtype=np.uint8)
+        assert s.shape == self.shape
+        _check(self._h, lib().lgca_upload_state(self._h, _ptr(s)))
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        s = np.empty(self.shape, np.uint8) if out is None else out
+        _check(self._h, lib().lgca_download_state(self._h, _ptr(s)))
+        return s
+
+    def init_random(self, p_move: float, p_rest: float | None = None) -> None:
+        p_rest = p_move if p_rest is None else p_rest
+        _check(self._h, lib().lgca_init_random(self._h, float(p_move), float(p_rest)))
+
+    def init_zero(self) -> None:
+        _check(self._h, lib().lgca_init_zero(self._h))
+
+    def set_forcing_column(self, x: int, p: float) -> None:
+        _check(self._h, lib().lgca_set_forcing_column(self._h, int(x), float(p)))
+
+    def set_chirality(self, field: np.ndarray | None) -> None:
+        f = None if field is None else np.ascontiguousarray(field, dtype=np.uint8)
+        _check(self._h, lib().lgca_set_chirality(self._h, _ptr(f)))
+
+    def set_temporal_depth(self, depth: int) -> None:
+        _check(self._h, lib().lgca_set_temporal_depth(self._h, int(depth)))
+
+    def set_step(self, t: int) -> None:
+        _check(self._h, lib().lgca_set_step(self._h, int(t)))
+
+    @property
+    def step_count(self) -> int:
+        t = C.c_uint64()
+        _check(self._h, lib().lgca_info(self._h, None, None, None, None, C.byref(t)))
+        return t.value
+
+    # work
+    def collide_and_propagate(self, nsteps: int = 1) -> None:
+        _check(self._h, lib().lgca_collide_and_propagate(self._h, int(nsteps)))
+
+    def apply_body_force(self, forcing: int, bf_dir: str | None = "x") -> int:
+        n = C.c_uint64()
+        d = ord(bf_dir) if bf_dir else 0
+        _check(self._h, lib().lgca_apply_body_force(self._h, int(forcing), d, C.byref(n)))
+        return n.value
+
+    def count_particles(self) -> int:
+        n = C.c_uint64()
+        _check(self._h, lib().lgca_count_particles(self._h, C.byref(n)))
+        return n.value
+
+    def mean_velocity(self):
+        ux, uy = C.c_float(), C.c_float()
+        _check(self._h, lib().lgca_mean_velocity(self._h, C.byref(ux), C.byref(uy)))
+        return ux.value, uy.value
+
+    def block_sums(self, B: int):
+        Hb, Wb = -(-self.dim_y // B), -(-self.dim_x // B)
+        N = np.empty((Hb, Wb), np.int32)
+        Jx2 = np.empty_like(N)
+        Jy = np.empty_like(N)
+        _check(self._h, lib().lgca_block_sums(self._h, int(B), _ptr(N), _ptr(Jx2), _ptr(Jy)))
+        return N, Jx2, Jy
+
+    def block_sums_device(self, B: int, N_ptr: int, Jx2_ptr: int, Jy_ptr: int) -> None:
+        _check(self._h, lib().lgca_block_sums_device(self._h, int(B), _ptr(N_ptr), _ptr(Jx2_ptr),
+                                                     _ptr(Jy_ptr)))
+
+    def post_process(self, r: int, cells: bool = True, means: bool = True):
+        H, W = self.shape
+        Hc, Wc = H // (2 * r), W // (2 * r)
+        cd = np.empty((H, W), np.float32) if cells else None
+        cm = np.empty((H, W, 2), np.float32) if cells else None
+        md = np.empty((Hc, Wc), np.float32) if means else None
+        mm = np.empty((Hc, Wc, 2), np.float32) if means else None
+        _check(self._h, lib().lgca_post_process(self._h, int(r), _ptr(cd), _ptr(cm), _ptr(md),
+                                                _ptr(mm)))
+        return cd, cm, md, mm
+
+    def sync(self) -> None:
+        _check(self._h, lib().lgca_sync(self._h))
+
+    def stream_ptr(self) -> int:
+        return lib().lgca_stream(self._h) or 0
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        _check(self._h, lib().lgca_set_stream(self._h, _ptr(stream_ptr) if stream_ptr else None))
+
+    def device_bytes(self) -> int:
+        n = C.c_size_t()
+        _check(self._h, lib().lgca_device_bytes(self._h, C.byref(n)))
+        return n.value
+
+    def state_device(self):
+        p, ps, pitch = C.c_void_p(), C.c_size_t(), C.c_int()
+        _check(self._h, lib().lgca_state_device(self._h, C.byref(p), C.byref(ps), C.byref(pitch)))
+        return p.value, ps.value, pitch.value
+
+
+__all__ = ["GpuLattice", "LgcaError", "build", "lib", "HPP", "FHP_I", "FHP_II", "FHP_III",
+           "FLUID", "SOLID_NO_SLIP", "SOLID_SLIP", "NUM_DIR"]

@@ -1,0 +1,105 @@
+// Internal declarations shared by the CUDA translation units of
+// liblgca_gpu.so.  Not part of the public interface (include/lgca_gpu.h).
+//
+// Device layout of one lattice (W x H sites, D channels):
+//   state   D bit-planes, each H rows of `pitch` uint64 words; word w of row y
+//           of plane d holds channel d of sites x = 64w .. 64w+63, bit i =
+//           site 64w+i.  Bits at x >= W (the tail of the last word) are 0.
+//           Plane d starts at base + d * plane_stride (words).
+//   solid   one plane of the same shape, bit = SOLID_NO_SLIP (optional)
+//   slip    one plane, bit = SOLID_SLIP (optional)
+//   chir    one plane of frozen chirality bits (optional)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "collide.cuh"
+
+namespace lgca_gpu {
+
+// Geometry modes of the step kernels: which cell-type planes exist.
+enum : int { GEOM_NONE = 0, GEOM_NOSLIP = 1, GEOM_FULL = 2 };
+
+struct PlaneGeom {
+    int W, H;          // sites
+    int nw;            // words per row = ceil(W / 64)
+    int pitch;         // words between rows (>= nw, even)
+    size_t ps;         // words between planes (= H * pitch)
+    int L;             // bit index of site W-1 inside the last word
+    uint64_t lastmask; // valid bits of the last word of a row
+};
+
+struct StepArgs {
+    const uint64_t *__restrict__ src;
+    uint64_t *__restrict__ dst;
+    const uint64_t *__restrict__ solid;  // GEOM_NOSLIP / GEOM_FULL
+    const uint64_t *__restrict__ slip;   // GEOM_FULL
+    const uint64_t *__restrict__ chir;   // frozen chirality plane or nullptr
+    PlaneGeom g;
+    int chunks;         // 32-word chunks per row
+    uint64_t chir_key;  // lgca_rng_key(seed, CHIR, t)
+    uint64_t force_key; // lgca_rng_key(seed, FORCE, t)
+    uint64_t force_thr; // 0 disables forcing
+    int fx;             // forcing column (valid when force_thr > 0)
+};
+
+// One lattice step of `a` (k = 1), launched on `stream`.
+cudaError_t launch_step(int model, int geom_mode, const StepArgs &a, cudaStream_t stream);
+
+// Multi-step pass: advances `depth` steps per pass over global memory.
+// keys[i] / fkeys[i] are the chirality / forcing keys of step i of the pass.
+struct MultiStepArgs {
+    StepArgs base;  // src / dst of the whole pass; keys unused
+    int depth;
+    uint64_t chir_keys[8];
+    uint64_t force_keys[8];
+};
+cudaError_t launch_multistep(int model, int geom_mode, const MultiStepArgs &a,
+                             cudaStream_t stream);
+bool multistep_supported(int model, const PlaneGeom &g, int depth);
+
+// Layout conversion between the reference byte-per-cell format and planes.
+cudaError_t launch_aos_to_planes(int D, const PlaneGeom &g, const uint8_t *aos, uint64_t *planes,
+                                 cudaStream_t s);
+cudaError_t launch_planes_to_aos(int D, const PlaneGeom &g, const uint64_t *planes, uint8_t *aos,
+                                 cudaStream_t s);
+// Cell types (int32) -> solid / slip planes; *bad set to 1 on invalid values.
+cudaError_t launch_types_to_planes(const PlaneGeom &g, const int32_t *types, uint64_t *solid,
+                                   uint64_t *slip, int *bad, cudaStream_t s);
+cudaError_t launch_planes_to_types(const PlaneGeom &g, const uint64_t *solid, const uint64_t *slip,
+                                   int32_t *types, cudaStream_t s);
+// Bernoulli initial occupation (fluid cells only).
+cudaError_t launch_init_random(int D, const PlaneGeom &g, const uint64_t *solid,
+                               const uint64_t *slip, uint64_t *planes, uint64_t seed,
+                               uint64_t thr_move, uint64_t thr_rest, cudaStream_t s);
+// Bytes (0/1) -> one plane.
+cudaError_t launch_bytes_to_plane(const PlaneGeom &g, const uint8_t *bytes, uint64_t *plane,
+                                  cudaStream_t s);
+// Integer block sums.
+cudaError_t launch_block_sums(int model, const PlaneGeom &g, const uint64_t *planes, int B,
+                              int32_t *N, int32_t *Jx2, int32_t *Jy, cudaStream_t s);
+// Reference-arithmetic post-processing.
+cudaError_t launch_cell_post(int model, const PlaneGeom &g, const uint64_t *planes,
+                             float *cell_density, float *cell_momentum, cudaStream_t s);
+cudaError_t launch_mean_post(int model, const PlaneGeom &g, const uint64_t *planes, int r,
+                             float *mean_density, float *mean_momentum, cudaStream_t s);
+// Reductions: out[0] = particles; mean velocity sums into dsum[0..1] (double)
+// and the fluid-cell count into out[1].
+cudaError_t launch_count(int D, const PlaneGeom &g, const uint64_t *planes,
+                         unsigned long long *out, cudaStream_t s);
+cudaError_t launch_mean_velocity(int model, const PlaneGeom &g, const uint64_t *planes,
+                                 const uint64_t *solid, const uint64_t *slip, double *dsum,
+                                 unsigned long long *nfluid, cudaStream_t s);
+
+// Random-cell body force (reference semantics).  scratch must hold
+// body_force_scratch_bytes(num_cells) bytes.
+size_t body_force_scratch_bytes(size_t num_cells);
+cudaError_t launch_body_force(int model, const PlaneGeom &g, uint64_t *planes,
+                              const uint64_t *solid, const uint64_t *slip, uint64_t key,
+                              long long forcing, int bf_dir, void *scratch,
+                              unsigned long long *reverted_dev, cudaStream_t s);
+
+static inline int num_dir(int model) { return model == M_HPP ? 4 : (model == M_FHP_I ? 6 : 7); }
+
+}  // namespace lgca_gpu

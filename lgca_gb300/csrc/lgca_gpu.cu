@@ -1,0 +1,571 @@
+// C ABI of the GB300 lattice-gas engine: handle management, host <-> device
+// transfers and dispatch to the kernels.  Declarations and the reference
+// interface each entry point replaces: include/lgca_gpu.h.
+#include "internal.cuh"
+#include "../../include/lgca_gpu.h"
+#include "../../include/lgca/rng.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+using namespace lgca_gpu;
+
+struct lgca_lattice {
+    int model = 0, D = 0;
+    PlaneGeom g{};
+    uint64_t seed = 0, t = 0, fcall = 0;
+    uint64_t *buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    uint64_t *solid = nullptr, *slip = nullptr, *chir = nullptr;
+    bool has_noslip = false, has_slip = false, frozen = false;
+    int force_x = -1;
+    uint64_t force_thr = 0;
+    int depth = 1;
+    int device = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    size_t bytes = 0;
+    std::string err;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(lgca_lattice *h, int status, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    if (h) h->err = buf;
+    return status;
+}
+
+int cuda_fail(lgca_lattice *h, cudaError_t e, const char *what)
+{
+    return fail(h, e == cudaErrorMemoryAllocation ? LGCA_ERR_NOMEM : LGCA_ERR_CUDA, "%s: %s", what,
+                cudaGetErrorString(e));
+}
+
+#define CK(h, expr)                                                   \
+    do {                                                              \
+        cudaError_t e_ = (expr);                                      \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #expr);      \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int scratch_reserve(lgca_lattice *h, size_t bytes)
+{
+    if (h->scratch_bytes >= bytes) return LGCA_OK;
+    if (h->scratch) {
+        cudaStreamSynchronize(h->stream);
+        cudaFree(h->scratch);
+        h->bytes -= h->scratch_bytes;
+        h->scratch = nullptr;
+        h->scratch_bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&h->scratch, bytes);
+    if (e != cudaSuccess) {
+        h->scratch = nullptr;
+        return cuda_fail(h, e, "cudaMalloc(scratch)");
+    }
+    h->scratch_bytes = bytes;
+    h->bytes += bytes;
+    return LGCA_OK;
+}
+
+int geom_mode(const lgca_lattice *h)
+{
+    if (h->has_slip) return GEOM_FULL;
+    if (h->has_noslip) return GEOM_NOSLIP;
+    return GEOM_NONE;
+}
+
+bool valid(lgca_handle h) { return h != nullptr && h->buf[0] != nullptr; }
+
+#define CHECK_HANDLE(h)                                                          \
+    do {                                                                         \
+        if (!valid(h)) return fail(nullptr, LGCA_ERR_INVALID, "invalid handle"); \
+    } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int lgca_abi_version(void) { return LGCA_GPU_ABI_VERSION; }
+
+const char *lgca_status_string(int status)
+{
+    switch (status) {
+    case LGCA_OK: return "ok";
+    case LGCA_ERR_INVALID: return "invalid argument";
+    case LGCA_ERR_NOMEM: return "out of device memory";
+    case LGCA_ERR_CUDA: return "CUDA error";
+    case LGCA_ERR_TIMEOUT: return "device wait timed out";
+    case LGCA_ERR_BUSY: return "busy";
+    default: return "unknown status";
+    }
+}
+
+const char *lgca_last_error(lgca_handle h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+int lgca_create(int model, int W, int H, uint64_t seed, lgca_handle *out)
+{
+    if (!out) return fail(nullptr, LGCA_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (model < LGCA_HPP || model > LGCA_FHP_III)
+        return fail(nullptr, LGCA_ERR_INVALID, "unknown model %d", model);
+    if (W < 1 || H < 1) return fail(nullptr, LGCA_ERR_INVALID, "invalid dimensions %d x %d", W, H);
+    if (model != LGCA_HPP && (H % 2) != 0)
+        return fail(nullptr, LGCA_ERR_INVALID,
+                    "FHP lattices need an even number of rows (dim_y = %d)", H);
+    if ((unsigned long long)W * (unsigned long long)H > 0x7fffffffULL)
+        return fail(nullptr, LGCA_ERR_INVALID, "lattice of %d x %d exceeds 2^31-1 cells", W, H);
+
+    lgca_lattice *h = new (std::nothrow) lgca_lattice();
+    if (!h) return fail(nullptr, LGCA_ERR_NOMEM, "host allocation failed");
+    h->model = model;
+    h->D = num_dir(model);
+    h->seed = seed;
+    PlaneGeom &g = h->g;
+    g.W = W;
+    g.H = H;
+    g.nw = (W + 63) / 64;
+    g.pitch = (g.nw + 1) & ~1;
+    g.ps = (size_t)H * g.pitch;
+    g.L = (W - 1) & 63;
+    g.lastmask = (g.L == 63) ? ~0ull : ((1ull << (g.L + 1)) - 1ull);
+    cudaGetDevice(&h->device);
+
+    cudaError_t e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        int st = cuda_fail(nullptr, e, "cudaStreamCreate");
+        delete h;
+        return st;
+    }
+    h->stream = h->own_stream;
+    const size_t state_bytes = (size_t)h->D * g.ps * sizeof(uint64_t);
+    for (int i = 0; i < 2; ++i) {
+        e = cudaMalloc(&h->buf[i], state_bytes);
+        if (e == cudaSuccess) e = cudaMemsetAsync(h->buf[i], 0, state_bytes, h->stream);
+        if (e != cudaSuccess) {
+            int st = cuda_fail(nullptr, e, "cudaMalloc(state)");
+            cudaFree(h->buf[0]);
+            cudaFree(h->buf[1]);
+            cudaStreamDestroy(h->own_stream);
+            delete h;
+            return st;
+        }
+        h->bytes += state_bytes;
+    }
+    *out = h;
+    return LGCA_OK;
+}
+
+int lgca_destroy(lgca_handle h)
+{
+    if (!h) return LGCA_OK;
+    DeviceGuard dg(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->buf[0]);
+    cudaFree(h->buf[1]);
+    cudaFree(h->solid);
+    cudaFree(h->slip);
+    cudaFree(h->chir);
+    cudaFree(h->scratch);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+    return LGCA_OK;
+}
+
+int lgca_info(lgca_handle h, int *model, int *W, int *H, uint64_t *seed, uint64_t *step)
+{
+    CHECK_HANDLE(h);
+    if (model) *model = h->model;
+    if (W) *W = h->g.W;
+    if (H) *H = h->g.H;
+    if (seed) *seed = h->seed;
+    if (step) *step = h->t;
+    return LGCA_OK;
+}
+
+int lgca_set_step(lgca_handle h, uint64_t t)
+{
+    CHECK_HANDLE(h);
+    h->t = t;
+    return LGCA_OK;
+}
+
+int lgca_set_cell_types(lgca_handle h, const int32_t *types)
+{
+    CHECK_HANDLE(h);
+    if (!types) return fail(h, LGCA_ERR_INVALID, "types is NULL");
+    DeviceGuard dg(h->device);
+    const PlaneGeom &g = h->g;
+    const size_t n = (size_t)g.W * g.H;
+    // scan on the host first: it decides which planes exist, and rejects
+    // invalid values before anything changes
+    bool any_noslip = false, any_slip = false;
+    for (size_t i = 0; i < n; ++i) {
+        const int32_t t = types[i];
+        if (t < 0 || t > 2) return fail(h, LGCA_ERR_INVALID, "invalid cell type %d at cell %zu", t, i);
+        any_noslip |= (t == 1);
+        any_slip |= (t == 2);
+    }
+    const size_t plane_bytes = g.ps * sizeof(uint64_t);
+    if (!h->solid) {
+        CK(h, cudaMalloc(&h->solid, plane_bytes));
+        CK(h, cudaMalloc(&h->slip, plane_bytes));
+        CK(h, cudaMemsetAsync(h->solid, 0, plane_bytes, h->stream));
+        CK(h, cudaMemsetAsync(h->slip, 0, plane_bytes, h->stream));
+        h->bytes += 2 * plane_bytes;
+    }
+    int st = scratch_reserve(h, n * sizeof(int32_t) + 256);
+    if (st) return st;
+    int *bad = reinterpret_cast<int *>(static_cast<char *>(h->scratch) + n * sizeof(int32_t));
+    CK(h, cudaMemcpyAsync(h->scratch, types, n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemsetAsync(bad, 0, sizeof(int), h->stream));
+    CK(h, launch_types_to_planes(g, static_cast<const int32_t *>(h->scratch), h->solid, h->slip, bad,
+                                 h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->has_noslip = any_noslip;
+    h->has_slip = any_slip;
+    return LGCA_OK;
+}
+
+int lgca_get_cell_types(lgca_handle h, int32_t *types)
+{
+    CHECK_HANDLE(h);
+    if (!types) return fail(h, LGCA_ERR_INVALID, "types is NULL");
+    DeviceGuard dg(h->device);
+    const size_t n = (size_t)h->g.W * h->g.H;
+    if (!h->solid) {
+        memset(types, 0, n * sizeof(int32_t));
+        return LGCA_OK;
+    }
+    int st = scratch_reserve(h, n * sizeof(int32_t));
+    if (st) return st;
+    CK(h, launch_planes_to_types(h->g, h->solid, h->slip, static_cast<int32_t *>(h->scratch), h->stream));
+    CK(h, cudaMemcpyAsync(types, h->scratch, n * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LGCA_OK;
+}
+
+int lgca_upload_state(lgca_handle h, const uint8_t *cells)
+{
+    CHECK_HANDLE(h);
+    if (!cells) return fail(h, LGCA_ERR_INVALID, "cells is NULL");
+    DeviceGuard dg(h->device);
+    const size_t n = (size_t)h->g.W * h->g.H;
+    int st = scratch_reserve(h, n + 64);
+    if (st) return st;
+    CK(h, cudaMemcpyAsync(h->scratch, cells, n, cudaMemcpyHostToDevice, h->stream));
+    CK(h, launch_aos_to_planes(h->D, h->g, static_cast<const uint8_t *>(h->scratch), h->buf[h->cur],
+                               h->stream));
+    return LGCA_OK;
+}
+
+int lgca_download_state(lgca_handle h, uint8_t *cells)
+{
+    CHECK_HANDLE(h);
+    if (!cells) return fail(h, LGCA_ERR_INVALID, "cells is NULL");
+    DeviceGuard dg(h->device);
+    const size_t n = (size_t)h->g.W * h->g.H;
+    int st = scratch_reserve(h, n + 64);
+    if (st) return st;
+    CK(h, launch_planes_to_aos(h->D, h->g, h->buf[h->cur], static_cast<uint8_t *>(h->scratch),
+                               h->stream));
+    CK(h, cudaMemcpyAsync(cells, h->scratch, n, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LGCA_OK;
+}
+
+int lgca_init_random(lgca_handle h, double p_move, double p_rest)
+{
+    CHECK_HANDLE(h);
+    if (!(p_move >= 0.0 && p_move <= 1.0) || !(p_rest >= 0.0 && p_rest <= 1.0))
+        return fail(h, LGCA_ERR_INVALID, "probabilities must lie in [0, 1]");
+    DeviceGuard dg(h->device);
+    CK(h, launch_init_random(h->D, h->g, h->has_noslip ? h->solid : nullptr,
+                             h->has_slip ? h->slip : nullptr, h->buf[h->cur], h->seed,
+                             lgca_prob_threshold(p_move), lgca_prob_threshold(p_rest), h->stream));
+    return LGCA_OK;
+}
+
+int lgca_init_zero(lgca_handle h)
+{
+    CHECK_HANDLE(h);
+    DeviceGuard dg(h->device);
+    CK(h, cudaMemsetAsync(h->buf[h->cur], 0, (size_t)h->D * h->g.ps * sizeof(uint64_t), h->stream));
+    return LGCA_OK;
+}
+
+int lgca_set_forcing_column(lgca_handle h, int x, double p)
+{
+    CHECK_HANDLE(h);
+    if (x >= h->g.W) return fail(h, LGCA_ERR_INVALID, "forcing column %d outside 0..%d", x, h->g.W - 1);
+    if (!(p >= 0.0 && p <= 1.0)) return fail(h, LGCA_ERR_INVALID, "probability must lie in [0, 1]");
+    if (x < 0 || p <= 0.0) {
+        h->force_x = -1;
+        h->force_thr = 0;
+    } else {
+        h->force_x = x;
+        h->force_thr = lgca_prob_threshold(p);
+    }
+    return LGCA_OK;
+}
+
+int lgca_set_chirality(lgca_handle h, const uint8_t *field)
+{
+    CHECK_HANDLE(h);
+    DeviceGuard dg(h->device);
+    if (!field) {
+        h->frozen = false;
+        return LGCA_OK;
+    }
+    const size_t n = (size_t)h->g.W * h->g.H;
+    if (!h->chir) {
+        CK(h, cudaMalloc(&h->chir, h->g.ps * sizeof(uint64_t)));
+        CK(h, cudaMemsetAsync(h->chir, 0, h->g.ps * sizeof(uint64_t), h->stream));
+        h->bytes += h->g.ps * sizeof(uint64_t);
+    }
+    int st = scratch_reserve(h, n + 64);
+    if (st) return st;
+    CK(h, cudaMemcpyAsync(h->scratch, field, n, cudaMemcpyHostToDevice, h->stream));
+    CK(h, launch_bytes_to_plane(h->g, static_cast<const uint8_t *>(h->scratch), h->chir, h->stream));
+    h->frozen = true;
+    return LGCA_OK;
+}
+
+int lgca_set_temporal_depth(lgca_handle h, int depth)
+{
+    CHECK_HANDLE(h);
+    if (depth < 1 || depth > 8) return fail(h, LGCA_ERR_INVALID, "depth %d outside 1..8", depth);
+    h->depth = depth;
+    return LGCA_OK;
+}
+
+int lgca_collide_and_propagate(lgca_handle h, int nsteps)
+{
+    CHECK_HANDLE(h);
+    if (nsteps < 0) return fail(h, LGCA_ERR_INVALID, "nsteps < 0");
+    DeviceGuard dg(h->device);
+    StepArgs a;
+    a.solid = h->solid;
+    a.slip = h->slip;
+    a.chir = h->frozen ? h->chir : nullptr;
+    a.g = h->g;
+    a.chunks = (h->g.nw + 31) / 32;
+    a.force_thr = h->force_thr;
+    a.fx = h->force_x;
+    const int gm = geom_mode(h);
+    int done = 0;
+    while (done < nsteps) {
+        const int k = std::min(h->depth, nsteps - done);
+        if (k > 1 && multistep_supported(h->model, h->g, k)) {
+            MultiStepArgs m;
+            m.base = a;
+            m.base.src = h->buf[h->cur];
+            m.base.dst = h->buf[h->cur ^ 1];
+            m.depth = k;
+            for (int i = 0; i < k; ++i) {
+                m.chir_keys[i] = lgca_rng_key(h->seed, LGCA_STREAM_CHIR, h->t + (uint64_t)i);
+                m.force_keys[i] = lgca_rng_key(h->seed, LGCA_STREAM_FORCE, h->t + (uint64_t)i);
+            }
+            CK(h, launch_multistep(h->model, gm, m, h->stream));
+            h->cur ^= 1;
+            h->t += (uint64_t)k;
+            done += k;
+            continue;
+        }
+        a.src = h->buf[h->cur];
+        a.dst = h->buf[h->cur ^ 1];
+        a.chir_key = lgca_rng_key(h->seed, LGCA_STREAM_CHIR, h->t);
+        a.force_key = lgca_rng_key(h->seed, LGCA_STREAM_FORCE, h->t);
+        CK(h, launch_step(h->model, gm, a, h->stream));
+        h->cur ^= 1;
+        h->t += 1;
+        done += 1;
+    }
+    return LGCA_OK;
+}
+
+int lgca_apply_body_force(lgca_handle h, int forcing, int bf_dir, uint64_t *reverted)
+{
+    CHECK_HANDLE(h);
+    if (!(bf_dir == 'x' || bf_dir == 'y' || bf_dir == 0))
+        return fail(h, LGCA_ERR_INVALID, "bf_dir must be 'x', 'y' or 0");
+    DeviceGuard dg(h->device);
+    const size_t n = (size_t)h->g.W * h->g.H;
+    const size_t need = body_force_scratch_bytes(n) + 64;
+    int st = scratch_reserve(h, need);
+    if (st) return st;
+    unsigned long long *rev = reinterpret_cast<unsigned long long *>(
+        static_cast<char *>(h->scratch) + need - 64);
+    const uint64_t key = lgca_rng_key(h->seed, LGCA_STREAM_FSEQ, h->fcall);
+    CK(h, launch_body_force(h->model, h->g, h->buf[h->cur], h->has_noslip ? h->solid : nullptr,
+                            h->has_slip ? h->slip : nullptr, key, forcing, bf_dir, h->scratch, rev,
+                            h->stream));
+    h->fcall += 1;
+    if (reverted) {
+        unsigned long long v = 0;
+        CK(h, cudaMemcpyAsync(&v, rev, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        *reverted = v;
+    }
+    return LGCA_OK;
+}
+
+int lgca_count_particles(lgca_handle h, uint64_t *n)
+{
+    CHECK_HANDLE(h);
+    if (!n) return fail(h, LGCA_ERR_INVALID, "n is NULL");
+    DeviceGuard dg(h->device);
+    int st = scratch_reserve(h, 64);
+    if (st) return st;
+    unsigned long long *d = static_cast<unsigned long long *>(h->scratch);
+    CK(h, cudaMemsetAsync(d, 0, sizeof(*d), h->stream));
+    CK(h, launch_count(h->D, h->g, h->buf[h->cur], d, h->stream));
+    unsigned long long v = 0;
+    CK(h, cudaMemcpyAsync(&v, d, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    *n = v;
+    return LGCA_OK;
+}
+
+int lgca_mean_velocity(lgca_handle h, float *ux, float *uy)
+{
+    CHECK_HANDLE(h);
+    if (!ux || !uy) return fail(h, LGCA_ERR_INVALID, "output is NULL");
+    DeviceGuard dg(h->device);
+    int st = scratch_reserve(h, 64);
+    if (st) return st;
+    double *ds = static_cast<double *>(h->scratch);
+    unsigned long long *nf = reinterpret_cast<unsigned long long *>(ds + 2);
+    CK(h, cudaMemsetAsync(ds, 0, 3 * sizeof(double), h->stream));
+    CK(h, launch_mean_velocity(h->model, h->g, h->buf[h->cur], h->has_noslip ? h->solid : nullptr,
+                               h->has_slip ? h->slip : nullptr, ds, nf, h->stream));
+    struct { double s[2]; unsigned long long n; } v;
+    CK(h, cudaMemcpyAsync(&v, ds, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    *ux = (float)(v.s[0] / (double)v.n);
+    *uy = (float)(v.s[1] / (double)v.n);
+    return LGCA_OK;
+}
+
+int lgca_block_sums_device(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32_t *Jy)
+{
+    CHECK_HANDLE(h);
+    if (B < 1 || !N || !Jx2 || !Jy) return fail(h, LGCA_ERR_INVALID, "invalid block-sum arguments");
+    DeviceGuard dg(h->device);
+    CK(h, launch_block_sums(h->model, h->g, h->buf[h->cur], B, N, Jx2, Jy, h->stream));
+    return LGCA_OK;
+}
+
+int lgca_block_sums(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32_t *Jy)
+{
+    CHECK_HANDLE(h);
+    if (B < 1 || !N || !Jx2 || !Jy) return fail(h, LGCA_ERR_INVALID, "invalid block-sum arguments");
+    DeviceGuard dg(h->device);
+    const size_t nb = (size_t)((h->g.W + B - 1) / B) * ((h->g.H + B - 1) / B);
+    int st = scratch_reserve(h, 3 * nb * sizeof(int32_t));
+    if (st) return st;
+    int32_t *d = static_cast<int32_t *>(h->scratch);
+    CK(h, launch_block_sums(h->model, h->g, h->buf[h->cur], B, d, d + nb, d + 2 * nb, h->stream));
+    CK(h, cudaMemcpyAsync(N, d, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(Jx2, d + nb, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(Jy, d + 2 * nb, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LGCA_OK;
+}
+
+int lgca_post_process(lgca_handle h, int r, float *cell_density, float *cell_momentum,
+                      float *mean_density, float *mean_momentum)
+{
+    CHECK_HANDLE(h);
+    if (r < 1) return fail(h, LGCA_ERR_INVALID, "coarse-graining radius must be >= 1");
+    DeviceGuard dg(h->device);
+    const size_t n = (size_t)h->g.W * h->g.H;
+    const int Wc = h->g.W / (2 * r), Hc = h->g.H / (2 * r);
+    const size_t nc = (size_t)std::max(Wc, 0) * (size_t)std::max(Hc, 0);
+    const size_t cell_bytes = (cell_density ? n : 0) * 4 + (cell_momentum ? 2 * n : 0) * 4;
+    const size_t mean_bytes = (mean_density ? nc : 0) * 4 + (mean_momentum ? 2 * nc : 0) * 4;
+    int st = scratch_reserve(h, cell_bytes + mean_bytes + 512);
+    if (st) return st;
+    char *p = static_cast<char *>(h->scratch);
+    float *dcd = cell_density ? reinterpret_cast<float *>(p) : nullptr;
+    p += cell_density ? ((n * 4 + 127) & ~(size_t)127) : 0;
+    float *dcm = cell_momentum ? reinterpret_cast<float *>(p) : nullptr;
+    p += cell_momentum ? ((2 * n * 4 + 127) & ~(size_t)127) : 0;
+    float *dmd = mean_density ? reinterpret_cast<float *>(p) : nullptr;
+    p += mean_density ? ((nc * 4 + 127) & ~(size_t)127) : 0;
+    float *dmm = mean_momentum ? reinterpret_cast<float *>(p) : nullptr;
+    if (dcd || dcm) CK(h, launch_cell_post(h->model, h->g, h->buf[h->cur], dcd, dcm, h->stream));
+    if ((dmd || dmm) && nc > 0)
+        CK(h, launch_mean_post(h->model, h->g, h->buf[h->cur], r, dmd, dmm, h->stream));
+    if (dcd) CK(h, cudaMemcpyAsync(cell_density, dcd, n * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (dcm) CK(h, cudaMemcpyAsync(cell_momentum, dcm, 2 * n * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (dmd && nc) CK(h, cudaMemcpyAsync(mean_density, dmd, nc * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (dmm && nc) CK(h, cudaMemcpyAsync(mean_momentum, dmm, 2 * nc * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LGCA_OK;
+}
+
+int lgca_sync(lgca_handle h)
+{
+    CHECK_HANDLE(h);
+    DeviceGuard dg(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LGCA_OK;
+}
+
+void *lgca_stream(lgca_handle h) { return valid(h) ? (void *)h->stream : nullptr; }
+
+int lgca_set_stream(lgca_handle h, void *stream)
+{
+    CHECK_HANDLE(h);
+    DeviceGuard dg(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+    return LGCA_OK;
+}
+
+int lgca_state_device(lgca_handle h, const uint64_t **planes, size_t *plane_stride, int *row_pitch)
+{
+    CHECK_HANDLE(h);
+    if (planes) *planes = h->buf[h->cur];
+    if (plane_stride) *plane_stride = h->g.ps;
+    if (row_pitch) *row_pitch = h->g.pitch;
+    return LGCA_OK;
+}
+
+int lgca_device_bytes(lgca_handle h, size_t *bytes)
+{
+    CHECK_HANDLE(h);
+    if (bytes) *bytes = h->bytes;
+    return LGCA_OK;
+}
+
+}  // extern "C"

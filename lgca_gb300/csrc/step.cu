@@ -1,0 +1,226 @@
+// Plain lattice step (one step per pass over global memory).
+//
+// Reference: OMP_Lattice<M>::collide_and_propagate, keva92/lgca
+// src/omp_lattice.cpp:100-249.  The reference pulls, for every cell and
+// channel d, the bit of channel d of the cell at offset_to_neighbor[INV_DIR[d]]
+// plus the periodic edge corrections (src/lgca_models.h:79-132 HPP,
+// :292-365 / :483-566 / :701-784 FHP).  With an even number of rows those
+// tables describe a torus; the source cell of channel d of site (x, y) is
+//
+//   d   FHP, y even   FHP, y odd    HPP
+//   0   (x-1, y)      (x-1, y)      (x-1, y)
+//   1   (x-1, y-1)    (x,   y-1)    (x,   y-1)
+//   2   (x,   y-1)    (x+1, y-1)    (x+1, y)
+//   3   (x+1, y)      (x+1, y)      (x,   y+1)
+//   4   (x,   y+1)    (x+1, y+1)
+//   5   (x-1, y+1)    (x,   y+1)
+//   6   (x,   y)      (x,   y)
+//
+// all coordinates modulo (W, H).  On bit-planes every channel is read from a
+// single row, and an x offset of +-1 is a one-bit shift of the word with the
+// missing bit taken from the neighbouring word (a warp shuffle, or a load at
+// a warp edge / the periodic x seam).
+//
+// Mapping: one warp per (row, chunk of 32 words), one word (64 sites) per
+// lane.  Each lane loads D words and stores D words; the only other traffic
+// is one word per shifted plane at the two warp edges.
+#include "internal.cuh"
+#include "../../include/lgca/rng.h"
+
+namespace lgca_gpu {
+
+static constexpr unsigned FULL = 0xffffffffu;
+
+// Forcing decision at site (fx, y): a FLUID cell with channel 0 empty and the
+// west-moving channel (3 for FHP, 2 for HPP) occupied reverses with
+// probability thr / 2^32.  Used by the lanes that fetch the forced word from
+// another chunk.
+template <int MODEL, int GM>
+__device__ __forceinline__ uint64_t force_flip_at(const StepArgs &a, int y)
+{
+    constexpr int WEST = (MODEL == M_HPP) ? 2 : 3;
+    const int fw = a.fx >> 6, fb = a.fx & 63;
+    const size_t r0 = (size_t)y * a.g.pitch + fw;
+    uint64_t n0 = a.src[r0], nw = a.src[(size_t)WEST * a.g.ps + r0];
+    uint64_t fluid = ~0ull;
+    if (GM >= GEOM_NOSLIP) fluid &= ~a.solid[r0];
+    if (GM == GEOM_FULL) fluid &= ~a.slip[r0];
+    const uint64_t u = lgca_rng_draw(a.force_key, lgca_rng_index((uint32_t)y, (uint32_t)a.fx)) >> 32;
+    const uint64_t cand = (~n0 & nw & fluid) >> fb & 1ull;
+    return (u < a.force_thr) ? cand : 0ull;
+}
+
+template <int MODEL, int GM>
+__device__ __forceinline__ void step_word(const StepArgs &a, const int y, const int w,
+                                          const int lane)
+{
+    constexpr int D = ModelTraits<MODEL>::D;
+    const PlaneGeom &g = a.g;
+    const bool active = w < g.nw;
+    const int ym = (y == 0) ? g.H - 1 : y - 1;
+    const int yp = (y == g.H - 1) ? 0 : y + 1;
+    const size_t rowm = (size_t)ym * g.pitch, row0 = (size_t)y * g.pitch,
+                 rowp = (size_t)yp * g.pitch;
+    const uint64_t *__restrict__ s = a.src;
+    const size_t ps = g.ps;
+    const bool even = (y & 1) == 0;
+
+    // which plane comes from which row (see the table above)
+    // HPP: 0 -> row y, 1 -> row y-1, 2 -> row y, 3 -> row y+1
+    // FHP: 0,3,6 -> row y, 1,2 -> row y-1, 4,5 -> row y+1
+    auto row_of = [&](int d) -> size_t {
+        if (MODEL == M_HPP) return d == 1 ? rowm : (d == 3 ? rowp : row0);
+        return (d == 1 || d == 2) ? rowm : ((d == 4 || d == 5) ? rowp : row0);
+    };
+
+    uint64_t n[7];
+#pragma unroll
+    for (int d = 0; d < D; ++d) n[d] = active ? __ldg(s + (size_t)d * ps + row_of(d) + w) : 0ull;
+
+    uint64_t solid = 0, slip = 0;
+    if (GM >= GEOM_NOSLIP && active) solid = __ldg(a.solid + row0 + w);
+    if (GM == GEOM_FULL && active) slip = __ldg(a.slip + row0 + w);
+
+    // forcing column: applied to the source words before the pull
+    constexpr int WEST = (MODEL == M_HPP) ? 2 : 3;
+    const bool forcing = a.force_thr != 0;
+    if (forcing && active && w == (a.fx >> 6)) {
+        const int fb = a.fx & 63;
+        const uint64_t u =
+            lgca_rng_draw(a.force_key, lgca_rng_index((uint32_t)y, (uint32_t)a.fx)) >> 32;
+        const uint64_t fl = (u < a.force_thr) ? ((~n[0] & n[WEST] & ~solid & ~slip) >> fb & 1ull) : 0ull;
+        n[0] |= fl << fb;
+        n[WEST] &= ~(fl << fb);
+    }
+
+    // neighbour words at the warp edges and the periodic x seam
+    const bool need_w = active && (lane == 0 || w == 0);
+    const bool need_e = active && (lane == 31 || w == g.nw - 1);
+    const int widx = (w == 0) ? g.nw - 1 : w - 1;
+    const int wbit = (w == 0) ? g.L : 63;
+    const int eidx = (w == g.nw - 1) ? 0 : w + 1;
+    const int epos = (w == g.nw - 1) ? g.L : 63;
+    const int wx = (w == 0) ? g.W - 1 : 64 * w - 1;  // site of the fetched west bit
+    const int ex = (w == g.nw - 1) ? 0 : 64 * w + 64; // site of the fetched east bit
+
+    // x-1 pull: (v << 1) | bit of site x-1
+    auto shl = [&](uint64_t v, int d, size_t row) -> uint64_t {
+        const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v >> 32), 1);
+        uint64_t in = hi >> 31;
+        if (need_w) {
+            in = (__ldg(s + (size_t)d * ps + row + widx) >> wbit) & 1ull;
+            if (d == 0 && row == row0 && forcing && wx == a.fx) in |= force_flip_at<MODEL, GM>(a, y);
+        }
+        return (v << 1) | in;
+    };
+    // x+1 pull: (v >> 1) | bit of site x+1 placed at the last valid bit
+    auto shr = [&](uint64_t v, int d, size_t row) -> uint64_t {
+        const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v, 1);
+        uint64_t in = lo & 1u;
+        if (need_e) {
+            in = __ldg(s + (size_t)d * ps + row + eidx) & 1ull;
+            if (d == WEST && row == row0 && forcing && ex == a.fx)
+                in &= ~force_flip_at<MODEL, GM>(a, y);
+        }
+        return (v >> 1) | (in << epos);
+    };
+
+    uint64_t p[7];
+    if (MODEL == M_HPP) {
+        p[0] = shl(n[0], 0, row0);
+        p[1] = n[1];
+        p[2] = shr(n[2], 2, row0);
+        p[3] = n[3];
+    } else {
+        p[0] = shl(n[0], 0, row0);
+        p[3] = shr(n[3], 3, row0);
+        if (even) {
+            p[1] = shl(n[1], 1, rowm);
+            p[5] = shl(n[5], 5, rowp);
+            p[2] = n[2];
+            p[4] = n[4];
+        } else {
+            p[2] = shr(n[2], 2, rowm);
+            p[4] = shr(n[4], 4, rowp);
+            p[1] = n[1];
+            p[5] = n[5];
+        }
+        if (D == 7) p[6] = n[6];
+    }
+    if (!active) return;
+
+    uint64_t c[7];
+#pragma unroll
+    for (int d = 0; d < D; ++d) c[d] = p[d];
+    if (MODEL != M_HPP) {
+        const uint64_t chir =
+            a.chir ? __ldg(a.chir + row0 + w)
+                   : lgca_rng_draw(a.chir_key, lgca_rng_index((uint32_t)y, (uint32_t)w));
+        collide<MODEL>(c, chir);
+    } else {
+        collide<MODEL>(c, 0ull);
+    }
+
+    uint64_t out[7];
+    if (GM == GEOM_NONE) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) out[d] = c[d];
+    } else {
+        const uint64_t fluid = ~(solid | slip);
+        // slip cells: mirror in x on the first/last row, in y on the first/last
+        // column (the latter wins at corners), unchanged elsewhere
+        const bool nsrow = (y == 0) || (y == g.H - 1);
+        const uint64_t ew = (w == 0 ? 1ull : 0ull) | (w == g.nw - 1 ? (1ull << g.L) : 0ull);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            uint64_t o = (fluid & c[d]) | (solid & p[Dirs<MODEL>::inv(d)]);
+            if (GM == GEOM_FULL) {
+                const uint64_t sx = nsrow ? p[Dirs<MODEL>::mirx(d)] : p[d];
+                const uint64_t sl = (ew & p[Dirs<MODEL>::miry(d)]) | (~ew & sx);
+                o |= slip & sl;
+            }
+            out[d] = o;
+        }
+    }
+    const uint64_t m = (w == g.nw - 1) ? g.lastmask : ~0ull;
+    uint64_t *__restrict__ dp = a.dst + row0 + w;
+#pragma unroll
+    for (int d = 0; d < D; ++d) dp[(size_t)d * ps] = out[d] & m;
+}
+
+template <int MODEL, int GM>
+__global__ void __launch_bounds__(256) k_step(const StepArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const long long task = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (task >= (long long)a.g.H * a.chunks) return;
+    const int y = (int)(task / a.chunks);
+    const int chunk = (int)(task - (long long)y * a.chunks);
+    step_word<MODEL, GM>(a, y, chunk * 32 + lane, lane);
+}
+
+template <int MODEL>
+static cudaError_t launch_model(int gm, const StepArgs &a, cudaStream_t st)
+{
+    const long long tasks = (long long)a.g.H * a.chunks;
+    const int threads = 256;
+    const long long blocks = (tasks + (threads / 32) - 1) / (threads / 32);
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    switch (gm) {
+    case GEOM_NONE: k_step<MODEL, GEOM_NONE><<<(unsigned)blocks, threads, 0, st>>>(a); break;
+    case GEOM_NOSLIP: k_step<MODEL, GEOM_NOSLIP><<<(unsigned)blocks, threads, 0, st>>>(a); break;
+    default: k_step<MODEL, GEOM_FULL><<<(unsigned)blocks, threads, 0, st>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step(int model, int gm, const StepArgs &a, cudaStream_t st)
+{
+    switch (model) {
+    case M_HPP: return launch_model<M_HPP>(gm, a, st);
+    case M_FHP_I: return launch_model<M_FHP_I>(gm, a, st);
+    default: return launch_model<M_FHP_II>(gm, a, st);  // FHP-II and FHP-III share one rule set
+    }
+}
+
+}  // namespace lgca_gpu

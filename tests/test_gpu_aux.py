@@ -1,0 +1,143 @@
+"""GPU parity of the kernels around the step: layout conversion, init,
+geometry, block sums, reference post-processing, reductions and the
+random-cell body force.  Bit-exact except the mean velocity, whose reference
+is an FP32 sum in thread-dependent order (tolerance stated below)."""
+import numpy as np
+import pytest
+
+from conftest import load_json, load_npz
+from lgca_gb300 import geometry as G
+
+pytestmark = pytest.mark.gpu
+MODELS = [0, 1, 2, 3]
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("W,H", [(1, 2), (5, 4), (64, 2), (100, 6), (1024, 8), (777, 10)])
+def test_upload_download_roundtrip(gpu, model, W, H):
+    rng = np.random.default_rng(W * H)
+    D = gpu.NUM_DIR[model]
+    st = rng.integers(0, 256, (H, W), dtype=np.uint8)
+    with gpu.GpuLattice(model, W, H) as L:
+        L.upload(st)
+        assert np.array_equal(L.download(), st & np.uint8((1 << D) - 1))
+        assert L.count_particles() == int(np.unpackbits(st & np.uint8((1 << D) - 1)).sum())
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_init_random_matches_oracle(gpu, oracle, model):
+    for W, H, geom in [(130, 20, G.pipe), (64, 64, G.periodic), (333, 12, G.karman_reference)]:
+        types = geom(W, H)
+        with gpu.GpuLattice(model, W, H, seed=99) as L:
+            L.set_cell_types(types)
+            L.init_random(0.37, 0.61)
+            got = L.download()
+        want = oracle.init_bernoulli(model, W, H, types, seed=99, p_move=0.37, p_rest=0.61)
+        assert np.array_equal(got, want)
+
+
+def test_cell_types_roundtrip_and_validation(gpu):
+    W, H = 150, 30
+    t = G.reflecting(W, H, "forward")
+    t[10:20, 40:60] = G.SOLID_NO_SLIP
+    with gpu.GpuLattice(2, W, H) as L:
+        L.set_cell_types(t)
+        assert np.array_equal(L.get_cell_types(), t)
+        bad = t.copy()
+        bad[3, 7] = 5
+        with pytest.raises(gpu.LgcaError):
+            L.set_cell_types(bad)
+        assert np.array_equal(L.get_cell_types(), t)  # unchanged by the rejected call
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("B", [1, 2, 3, 5, 8, 16, 20, 32, 64, 100, 128, 256])
+def test_block_sums_match_oracle(gpu, oracle, model, B):
+    W, H = 520, 90
+    st = oracle.init_bernoulli(model, W, H, None, seed=B, p_move=0.45, p_rest=0.3)
+    with gpu.GpuLattice(model, W, H) as L:
+        L.upload(st)
+        got = L.block_sums(B)
+    want = oracle.block_sums(model, st, B)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_post_process_matches_golden_bitwise(gpu, model):
+    npz = load_npz("postprocess.npz")
+    keys = sorted({k.rsplit("_", 1)[0] for k in npz.files if k.startswith(f"m{model}_")})
+    for k in keys:
+        r = int(k.rsplit("_r", 1)[1])
+        st = npz[k + "_state"]
+        H, W = st.shape
+        with gpu.GpuLattice(model, W, H) as L:
+            L.upload(st)
+            got = L.post_process(r)
+        for name, g in zip(("cd", "cm", "md", "mm"), got):
+            want = npz[f"{k}_{name}"]
+            assert np.array_equal(g.view(np.uint32), want.view(np.uint32)), (k, name)
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_post_process_matches_oracle_bitwise(gpu, oracle, model):
+    for W, H, r in [(200, 60, 10), (1024, 128, 8), (96, 32, 16), (10, 8, 4)]:
+        st = oracle.init_bernoulli(model, W, H, None, seed=W, p_move=0.5, p_rest=0.5)
+        with gpu.GpuLattice(model, W, H) as L:
+            L.upload(st)
+            got = L.post_process(r)
+        for g, w in zip(got, oracle.post_process(model, st, r)):
+            assert np.array_equal(g.view(np.uint32), w.view(np.uint32)), (W, H, r)
+
+
+def test_mean_velocity(gpu, oracle):
+    """Reference: FP32 sum of per-cell u over fluid cells (thread-order
+    dependent); here summed in double.  Tolerance: 1e-5 relative + 1e-7."""
+    for c in load_json("params.json")["mean_velocity"]:
+        m, W, H = c["model"], c["W"], c["H"]
+        types = G.pipe(W, H)
+        st = oracle.init_bernoulli(m, W, H, types, seed=c["seed"], p_move=0.3, p_rest=0.3)
+        st = oracle.run(m, st, c["steps"], types=types, seed=c["seed"], force_x=c["force_x"],
+                        force_p=c["force_p"])
+        with gpu.GpuLattice(m, W, H) as L:
+            L.set_cell_types(types)
+            L.upload(st)
+            ux, uy = L.mean_velocity()
+        assert ux == pytest.approx(c["ux"], rel=1e-5, abs=1e-7)
+        assert uy == pytest.approx(c["uy"], rel=1e-5, abs=1e-7)
+
+
+def test_body_force_matches_golden(gpu):
+    meta = load_json("bodyforce.json")
+    npz = load_npz("bodyforce.npz")
+    geoms = {"pipe": G.pipe, "periodic": G.periodic, "karman": G.karman_reference}
+    for i, c in enumerate(meta):
+        types = geoms[c["geometry"]](c["W"], c["H"])
+        with gpu.GpuLattice(c["model"], c["W"], c["H"], seed=c["seed"]) as L:
+            L.set_cell_types(types)
+            L.upload(npz[f"b{i}_init"])
+            for _ in range(c["call"]):  # advance the handle's call counter
+                L.apply_body_force(0, None)
+            L.apply_body_force(c["forcing"], c["dir"])
+            assert np.array_equal(L.download(), npz[f"b{i}_final"]), c
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_body_force_matches_oracle_large(gpu, oracle, model):
+    """Several chunks of candidates, targets reached mid-chunk and never."""
+    W, H = 1000, 700
+    types = G.karman_reference(W, H)
+    st = oracle.init_bernoulli(model, W, H, types, seed=6, p_move=0.3, p_rest=0.3)
+    for call, (forcing, d) in enumerate([(7000, "x"), (150000, "x"), (50000, "y"), (10 ** 9, "x"),
+                                         (1, "y")]):
+        want, nrev = oracle.apply_body_force(model, st, forcing, types=types, seed=6, call=call,
+                                             bf_dir=d)
+        with gpu.GpuLattice(model, W, H, seed=6) as L:
+            L.set_cell_types(types)
+            L.upload(st)
+            for _ in range(call):
+                L.apply_body_force(0, None)
+            n = L.apply_body_force(forcing, d)
+            got = L.download()
+        assert n == nrev
+        assert np.array_equal(got, want), (forcing, d)

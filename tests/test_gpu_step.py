@@ -1,0 +1,173 @@
+"""GPU parity of the step kernels (liblgca_gpu.so through the C ABI) against
+the golden fixtures made by the reference and against the oracle.  Integer /
+bit work: every comparison is bit-exact."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import load_json, load_npz
+from lgca_gb300 import geometry as G
+
+pytestmark = pytest.mark.gpu
+MODELS = [0, 1, 2, 3]
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def run_gpu(gpu, model, init, steps, types=None, seed=0, chir=None, force_x=-1, force_p=0.0, t0=0,
+            depth=1, chunks=None):
+    H, W = init.shape
+    with gpu.GpuLattice(model, W, H, seed) as L:
+        if types is not None:
+            L.set_cell_types(types)
+        L.upload(init)
+        L.set_step(t0)
+        if chir is not None:
+            L.set_chirality(chir)
+        L.set_forcing_column(force_x, force_p)
+        L.set_temporal_depth(depth)
+        if chunks is None:
+            L.collide_and_propagate(steps)
+        else:
+            done = 0
+            for c in chunks:
+                L.collide_and_propagate(c)
+                done += c
+            assert done == steps
+        assert L.step_count == t0 + steps
+        return L.download()
+
+
+def test_golden_trajectories(gpu):
+    meta = load_json("trajectories.json")
+    npz = load_npz("trajectories.npz")
+    for i, c in enumerate(meta):
+        types = npz[f"c{i}_types"].astype(np.int32)
+        chir = npz[f"c{i}_chir"] if f"c{i}_chir" in npz.files else None
+        out = run_gpu(gpu, c["model"], npz[f"c{i}_init"], c["steps"], types=types, seed=c["seed"],
+                      chir=chir, force_x=c["force_x"], force_p=c["force_p"])
+        assert np.array_equal(out, npz[f"c{i}_final"]), c
+
+
+WIDTHS = [1, 2, 3, 31, 63, 64, 65, 127, 128, 129, 200, 2047, 2048, 2049, 4160]
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("W", WIDTHS)
+def test_ragged_widths_periodic_vs_oracle(gpu, oracle, model, W):
+    H = 6
+    st = oracle.init_bernoulli(model, W, H, None, seed=W, p_move=0.4, p_rest=0.3)
+    want = oracle.run(model, st, 9, seed=W + 1)
+    got = run_gpu(gpu, model, st, 9, seed=W + 1)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("geom", ["pipe", "karman", "reflecting_back", "reflecting_forward", "disc"])
+def test_geometries_and_forcing_vs_oracle(gpu, oracle, model, geom):
+    rng = np.random.default_rng(17 * model + len(geom))
+    for W, H in [(64, 32), (130, 40), (1000, 24), (2112, 10)]:
+        types = {"pipe": G.pipe, "karman": G.karman_reference,
+                 "reflecting_back": lambda w, h: G.reflecting(w, h, "back"),
+                 "reflecting_forward": lambda w, h: G.reflecting(w, h, "forward"),
+                 "disc": lambda w, h: G.disc(w, h, w // 3, h // 2, h // 3)}[geom](W, H)
+        seed = int(rng.integers(1 << 40))
+        st = oracle.init_bernoulli(model, W, H, types, seed=seed, p_move=0.3, p_rest=0.4)
+        # forcing columns on word edges, the seam and inside words
+        for fx in (0, 1, 63, 64, W - 1, int(rng.integers(0, W))):
+            if fx >= W:
+                continue
+            kw = dict(types=types, seed=seed, force_x=fx, force_p=0.6, t0=int(rng.integers(100)))
+            want = oracle.run(model, st, 13, **kw)
+            got = run_gpu(gpu, model, st, 13, **kw)
+            assert np.array_equal(got, want), (W, H, fx)
+
+
+@pytest.mark.parametrize("model", [1, 2, 3])
+def test_frozen_chirality_vs_oracle(gpu, oracle, model):
+    rng = np.random.default_rng(model)
+    W, H = 300, 20
+    st = oracle.init_bernoulli(model, W, H, None, seed=4, p_move=0.4)
+    chir = rng.integers(0, 2, (H, W), dtype=np.uint8)
+    want = oracle.run(model, st, 17, chir=chir, seed=4)
+    got = run_gpu(gpu, model, st, 17, chir=chir, seed=4)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_step_splitting_is_invisible(gpu, oracle, model):
+    W, H = 256, 64
+    types = G.pipe(W, H)
+    st = oracle.init_bernoulli(model, W, H, types, seed=8, p_move=0.3)
+    kw = dict(types=types, seed=8, force_x=10, force_p=0.3)
+    a = run_gpu(gpu, model, st, 24, **kw)
+    b = run_gpu(gpu, model, st, 24, chunks=[1, 5, 7, 11], **kw)
+    assert np.array_equal(a, b)
+    assert np.array_equal(a, oracle.run(model, st, 24, **kw))
+
+
+def test_config_pipe_fhp1_1024x512_1000_steps(gpu):
+    """BASELINE workload 1 at full size: bit-exact with the reference run."""
+    pins = load_json("config_pins.json")["pipe_fhp1_1024x512"]
+    W, H = 1024, 512
+    with gpu.GpuLattice(1, W, H, seed=1) as L:
+        L.set_cell_types(G.pipe(W, H))
+        L.init_random(0.2, 0.2)
+        assert sha(L.download()) == pins["init_sha"]
+        L.set_forcing_column(8, 0.01)
+        L.collide_and_propagate(1000)
+        fin = L.download()
+        assert sha(fin) == pins["final_sha"]
+        assert L.count_particles() == pins["particles"]
+        N, Jx2, Jy = L.block_sums(16)
+    g = load_npz("config_pipe_blocksums.npz")
+    assert np.array_equal(N, g["N"]) and np.array_equal(Jx2, g["Jx2"]) and np.array_equal(Jy, g["Jy"])
+
+
+def test_config_karman_fhp3_8192x2048(gpu):
+    """BASELINE workload 2 at full size: the first 200 steps bit-exact with the
+    reference (its CPU run is pinned at 100 and 200 steps)."""
+    pins = load_json("config_pins.json")["karman_fhp3_8192x2048"]
+    g = load_npz("config_karman_blocksums.npz")
+    W, H = 8192, 2048
+    types = G.disc(W, H, 1024, 1024, 128)
+    assert sha(types) == pins["types_sha"]
+    with gpu.GpuLattice(3, W, H, seed=2) as L:
+        L.set_cell_types(types)
+        L.init_random(0.3, 0.3)
+        assert sha(L.download()) == pins["init_sha"]
+        L.set_forcing_column(16, 0.02)
+        n0 = L.count_particles()
+        for tag in ("t100", "t200"):
+            L.collide_and_propagate(100)
+            assert sha(L.download()) == pins[f"{tag}_sha"], tag
+            N, Jx2, Jy = L.block_sums(32)
+            assert np.array_equal(N, g[f"{tag}_N"]) and np.array_equal(Jx2, g[f"{tag}_Jx2"])
+            assert np.array_equal(Jy, g[f"{tag}_Jy"])
+        # the remaining steps of the 10000-step run: forcing only turns
+        # particles around, walls and the disc reflect them, so mass is conserved
+        L.collide_and_propagate(9800)
+        assert L.count_particles() == n0
+        N, _, _ = L.block_sums(32)
+        assert int(N.sum()) == n0
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_large_periodic_mass_and_block_totals(gpu, model):
+    """Full-width roofline lattice (32768 x 16384): mass is conserved and the
+    block sums add up to the particle count (size-independent properties)."""
+    W, H = 32768, 16384
+    with gpu.GpuLattice(model, W, H, seed=3) as L:
+        L.init_random(0.5, 0.5)
+        n0 = L.count_particles()
+        _, jx0, jy0 = L.block_sums(64)
+        L.collide_and_propagate(20)
+        assert L.count_particles() == n0
+        N, Jx2, Jy = L.block_sums(64)
+        assert int(N.astype(np.int64).sum()) == n0
+        # a periodic lattice without obstacles or forcing conserves momentum
+        assert int(Jx2.astype(np.int64).sum()) == int(jx0.astype(np.int64).sum())
+        assert int(Jy.astype(np.int64).sum()) == int(jy0.astype(np.int64).sum())
