@@ -109,6 +109,12 @@ int lgca_set_chirality(lgca_handle h, const uint8_t *field);
  * memory (1..8).  Results do not depend on it. */
 int lgca_set_temporal_depth(lgca_handle h, int depth);
 
+/* Kernel family for the steps: 0 = automatic (default), 1 = one step per
+ * pass only, 2 = register wavefront (several steps per pass), 3 = shared-
+ * memory tiles (several steps per pass).  Results do not depend on it.
+ * No reference counterpart (a scheduling choice of this engine). */
+int lgca_set_kernel_variant(lgca_handle h, int variant);
+
 /* Advance nsteps steps (forcing column, then pull-stream + collide by cell
  * type), enqueued on the handle's stream; the step counter advances by
  * nsteps.  Replaces: OMP_Lattice<M>::collide_and_propagate

@@ -52,57 +52,66 @@ LGCA_HDI void collide_hpp(uint64_t n[4])
 
 // FHP-I (REST = false) and FHP-II/III (REST = true).  `p` is the chirality
 // word: 1 rotates a two-body collision one way, 0 the other.
+//
+// The reference writes every collision pattern as "these channels occupied
+// and all other moving channels empty" (e.g. db1 = a&d&~(b|c|e|f),
+// src/lgca_models.h:376) and flips channel x when any pattern that moves x
+// matches.  The same boolean function, regrouped for few operations, indexing
+// the moving channels n0..n5 around the hexagon (the reference's a..f are
+// n1..n5, n0):
+//   * count the occupied moving channels once with a bit-sliced adder
+//     (c0 + 2 c1 + 4 c2) and form "exactly 1 / 2 / 3 moving" masks;
+//   * head-on pair k = {n_k, n_k+3}: P_k = n_k & n_k+3 & is2; the pair turns by
+//     -60 deg (p = 1) or +60 deg (p = 0), so channel pair k flips when P_k or
+//     (p ? P_k+1 : P_k-1) holds (the reference's db1|(p&db2)|(~p&db3));
+//   * three-body: T = is3 & (n0&n2&n4 | n1&n3&n5) flips all six;
+//   * rest rules (FHP-II): a rest particle plus a single moving particle at x
+//     (R1 = r & is1) and two moving particles at x-1, x+1 without rest
+//     (R2 = ~r & is2) both have their "centre" at x:
+//       K_x = (R1 & n_x) | (R2 & n_x-1 & n_x+1),
+//     and flip exactly channels x-1, x, x+1 and the rest channel.
+// Checked exhaustively against the reference rules in the tests.
 template <bool REST>
 LGCA_HDI void collide_fhp(uint64_t n[7], uint64_t p)
 {
-    const uint64_t a = n[1], b = n[2], c = n[3], d = n[4], e = n[5], f = n[0];
-    const uint64_t np = ~p;
+    const uint64_t n0 = n[0], n1 = n[1], n2 = n[2], n3 = n[3], n4 = n[4], n5 = n[5];
 
-    // head-on pairs with all other moving channels empty
-    const uint64_t db1 = a & d & ~(b | c | e | f);
-    const uint64_t db2 = b & e & ~(a | c | d | f);
-    const uint64_t db3 = c & f & ~(a | b | d | e);
-    // symmetric three-body a,c,e <-> b,d,f (alternating occupation)
-    const uint64_t triple = (a ^ b) & (b ^ c) & (c ^ d) & (d ^ e) & (e ^ f);
+    // moving-particle count: two full adders and a 2-bit combine
+    const uint64_t s1 = n0 ^ n1 ^ n2, k1 = (n0 & n1) | (n2 & (n0 ^ n1));
+    const uint64_t s2 = n3 ^ n4 ^ n5, k2 = (n3 & n4) | (n5 & (n3 ^ n4));
+    const uint64_t c0 = s1 ^ s2, t = s1 & s2;
+    const uint64_t c1 = k1 ^ k2 ^ t, c2 = (k1 & k2) | (t & (k1 ^ k2));
+    const uint64_t is2 = ~c0 & c1 & ~c2;
+    const uint64_t is3 = c0 & c1 & ~c2;
 
-    uint64_t cha = triple | db1 | (p & db2) | (np & db3);
-    uint64_t chb = triple | db2 | (p & db3) | (np & db1);
-    uint64_t chc = triple | db3 | (p & db1) | (np & db2);
-    uint64_t chd = cha, che = chb, chf = chc;
+    const uint64_t P0 = n0 & n3 & is2, P1 = n1 & n4 & is2, P2 = n2 & n5 & is2;
+    const uint64_t T = is3 & ((n0 & n2 & n4) | (n1 & n3 & n5));
+    const uint64_t X0 = T | P0 | ((p & P1) | (~p & P2));
+    const uint64_t X1 = T | P1 | ((p & P2) | (~p & P0));
+    const uint64_t X2 = T | P2 | ((p & P0) | (~p & P1));
 
     if (REST) {
         const uint64_t r = n[6];
-        // exactly one moving particle x: x & ~(the other five)
-        const uint64_t bcdef = b | c | d | e | f;
-        const uint64_t oa = a & ~bcdef;
-        const uint64_t ob = b & ~(a | c | d | e | f);
-        const uint64_t oc = c & ~(a | b | d | e | f);
-        const uint64_t od = d & ~(a | b | c | e | f);
-        const uint64_t oe = e & ~(a | b | c | d | f);
-        const uint64_t of = f & ~(a | b | c | d | e);
-        // rest + one moving -> two moving at +-60 degrees
-        const uint64_t ra = r & oa, rb = r & ob, rc = r & oc;
-        const uint64_t rd = r & od, re = r & oe, rf = r & of;
-        // two moving at 120 degrees apart, no rest -> rest + one moving
-        const uint64_t nr = ~r;
-        const uint64_t ra2 = f & b & nr & ~(a | c | d | e);
-        const uint64_t rb2 = a & c & nr & ~(b | d | e | f);
-        const uint64_t rc2 = b & d & nr & ~(a | c | e | f);
-        const uint64_t rd2 = c & e & nr & ~(a | b | d | f);
-        const uint64_t re2 = d & f & nr & ~(a | b | c | e);
-        const uint64_t rf2 = e & a & nr & ~(b | c | d | f);
-
-        cha |= ra | rb | rf | ra2 | rb2 | rf2;
-        chd |= rd | rc | re | rd2 | rc2 | re2;
-        chb |= rb | ra | rc | rb2 | ra2 | rc2;
-        che |= re | rd | rf | re2 | rd2 | rf2;
-        chc |= rc | rb | rd | rc2 | rb2 | rd2;
-        chf |= rf | ra | re | rf2 | ra2 | re2;
-        const uint64_t chr = ra | rb | rc | rd | re | rf | ra2 | rb2 | rc2 | rd2 | re2 | rf2;
-        n[6] = r ^ chr;
+        const uint64_t is1 = c0 & ~c1 & ~c2;
+        const uint64_t R1 = r & is1, R2 = ~r & is2;
+        const uint64_t K0 = (R1 & n0) | (R2 & n5 & n1);
+        const uint64_t K1 = (R1 & n1) | (R2 & n0 & n2);
+        const uint64_t K2 = (R1 & n2) | (R2 & n1 & n3);
+        const uint64_t K3 = (R1 & n3) | (R2 & n2 & n4);
+        const uint64_t K4 = (R1 & n4) | (R2 & n3 & n5);
+        const uint64_t K5 = (R1 & n5) | (R2 & n4 & n0);
+        n[0] = n0 ^ (X0 | K5 | K0 | K1);
+        n[1] = n1 ^ (X1 | K0 | K1 | K2);
+        n[2] = n2 ^ (X2 | K1 | K2 | K3);
+        n[3] = n3 ^ (X0 | K2 | K3 | K4);
+        n[4] = n4 ^ (X1 | K3 | K4 | K5);
+        n[5] = n5 ^ (X2 | K4 | K5 | K0);
+        n[6] = r ^ ((K0 | K1 | K2) | (K3 | K4 | K5));
+    } else {
+        n[0] = n0 ^ X0; n[3] = n3 ^ X0;
+        n[1] = n1 ^ X1; n[4] = n4 ^ X1;
+        n[2] = n2 ^ X2; n[5] = n5 ^ X2;
     }
-    n[1] = a ^ cha; n[2] = b ^ chb; n[3] = c ^ chc;
-    n[4] = d ^ chd; n[5] = e ^ che; n[0] = f ^ chf;
 }
 
 template <int MODEL>

@@ -55,9 +55,15 @@ struct MultiStepArgs {
     uint64_t chir_keys[8];
     uint64_t force_keys[8];
 };
+// Shared-memory tile form (multistep.cu) and register wavefront form (wave.cu).
 cudaError_t launch_multistep(int model, int geom_mode, const MultiStepArgs &a,
                              cudaStream_t stream);
 bool multistep_supported(int model, const PlaneGeom &g, int depth);
+cudaError_t launch_wave(int model, int geom_mode, const MultiStepArgs &a, cudaStream_t stream);
+bool wave_supported(int model, const PlaneGeom &g, int depth);
+
+// Kernel families selectable per handle.
+enum : int { VARIANT_AUTO = 0, VARIANT_PLAIN = 1, VARIANT_WAVE = 2, VARIANT_TILE = 3 };
 
 // Layout conversion between the reference byte-per-cell format and planes.
 cudaError_t launch_aos_to_planes(int D, const PlaneGeom &g, const uint8_t *aos, uint64_t *planes,

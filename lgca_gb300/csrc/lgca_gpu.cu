@@ -27,6 +27,7 @@ struct lgca_lattice {
     int force_x = -1;
     uint64_t force_thr = 0;
     int depth = 1;
+    int variant = VARIANT_AUTO;
     int device = 0;
     cudaStream_t own_stream = nullptr, stream = nullptr;
     void *scratch = nullptr;
@@ -367,6 +368,15 @@ int lgca_set_temporal_depth(lgca_handle h, int depth)
     return LGCA_OK;
 }
 
+int lgca_set_kernel_variant(lgca_handle h, int variant)
+{
+    CHECK_HANDLE(h);
+    if (variant < VARIANT_AUTO || variant > VARIANT_TILE)
+        return fail(h, LGCA_ERR_INVALID, "unknown kernel variant %d", variant);
+    h->variant = variant;
+    return LGCA_OK;
+}
+
 int lgca_collide_and_propagate(lgca_handle h, int nsteps)
 {
     CHECK_HANDLE(h);
@@ -383,8 +393,14 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     const int gm = geom_mode(h);
     int done = 0;
     while (done < nsteps) {
-        const int k = std::min(h->depth, nsteps - done);
-        if (k > 1 && multistep_supported(h->model, h->g, k)) {
+        // largest supported depth that fits, else one step per pass
+        int k = std::min(h->depth, nsteps - done);
+        const bool tile = h->variant == VARIANT_TILE;
+        if (h->variant == VARIANT_PLAIN) k = 1;
+        while (k > 1 && !(tile ? multistep_supported(h->model, h->g, k)
+                               : wave_supported(h->model, h->g, k)))
+            --k;
+        if (k > 1) {
             MultiStepArgs m;
             m.base = a;
             m.base.src = h->buf[h->cur];
@@ -394,7 +410,8 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
                 m.chir_keys[i] = lgca_rng_key(h->seed, LGCA_STREAM_CHIR, h->t + (uint64_t)i);
                 m.force_keys[i] = lgca_rng_key(h->seed, LGCA_STREAM_FORCE, h->t + (uint64_t)i);
             }
-            CK(h, launch_multistep(h->model, gm, m, h->stream));
+            if (tile) CK(h, launch_multistep(h->model, gm, m, h->stream));
+            else CK(h, launch_wave(h->model, gm, m, h->stream));
             h->cur ^= 1;
             h->t += (uint64_t)k;
             done += k;

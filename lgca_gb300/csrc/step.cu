@@ -40,8 +40,8 @@ __device__ __forceinline__ uint64_t force_flip_at(const StepArgs &a, int y)
 {
     constexpr int WEST = (MODEL == M_HPP) ? 2 : 3;
     const int fw = a.fx >> 6, fb = a.fx & 63;
-    const size_t r0 = (size_t)y * a.g.pitch + fw;
-    uint64_t n0 = a.src[r0], nw = a.src[(size_t)WEST * a.g.ps + r0];
+    const unsigned r0 = (unsigned)y * a.g.pitch + fw;
+    uint64_t n0 = a.src[r0], nw = a.src[WEST * (unsigned)a.g.ps + r0];
     uint64_t fluid = ~0ull;
     if (GM >= GEOM_NOSLIP) fluid &= ~a.solid[r0];
     if (GM == GEOM_FULL) fluid &= ~a.slip[r0];
@@ -59,23 +59,24 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const int y, const 
     const bool active = w < g.nw;
     const int ym = (y == 0) ? g.H - 1 : y - 1;
     const int yp = (y == g.H - 1) ? 0 : y + 1;
-    const size_t rowm = (size_t)ym * g.pitch, row0 = (size_t)y * g.pitch,
-                 rowp = (size_t)yp * g.pitch;
+    // 32-bit offsets: a lattice has at most 2^31 sites, so D * H * pitch < 2^29 words
+    const unsigned rowm = (unsigned)ym * g.pitch, row0 = (unsigned)y * g.pitch,
+                   rowp = (unsigned)yp * g.pitch;
     const uint64_t *__restrict__ s = a.src;
-    const size_t ps = g.ps;
+    const unsigned ps = (unsigned)g.ps;
     const bool even = (y & 1) == 0;
 
     // which plane comes from which row (see the table above)
     // HPP: 0 -> row y, 1 -> row y-1, 2 -> row y, 3 -> row y+1
     // FHP: 0,3,6 -> row y, 1,2 -> row y-1, 4,5 -> row y+1
-    auto row_of = [&](int d) -> size_t {
+    auto row_of = [&](int d) -> unsigned {
         if (MODEL == M_HPP) return d == 1 ? rowm : (d == 3 ? rowp : row0);
         return (d == 1 || d == 2) ? rowm : ((d == 4 || d == 5) ? rowp : row0);
     };
 
     uint64_t n[7];
 #pragma unroll
-    for (int d = 0; d < D; ++d) n[d] = active ? __ldg(s + (size_t)d * ps + row_of(d) + w) : 0ull;
+    for (int d = 0; d < D; ++d) n[d] = active ? __ldg(s + (d * ps + row_of(d) + w)) : 0ull;
 
     uint64_t solid = 0, slip = 0;
     if (GM >= GEOM_NOSLIP && active) solid = __ldg(a.solid + row0 + w);
@@ -104,21 +105,21 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const int y, const 
     const int ex = (w == g.nw - 1) ? 0 : 64 * w + 64; // site of the fetched east bit
 
     // x-1 pull: (v << 1) | bit of site x-1
-    auto shl = [&](uint64_t v, int d, size_t row) -> uint64_t {
+    auto shl = [&](uint64_t v, int d, unsigned row) -> uint64_t {
         const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v >> 32), 1);
         uint64_t in = hi >> 31;
         if (need_w) {
-            in = (__ldg(s + (size_t)d * ps + row + widx) >> wbit) & 1ull;
+            in = (__ldg(s + (d * ps + row + widx)) >> wbit) & 1ull;
             if (d == 0 && row == row0 && forcing && wx == a.fx) in |= force_flip_at<MODEL, GM>(a, y);
         }
         return (v << 1) | in;
     };
     // x+1 pull: (v >> 1) | bit of site x+1 placed at the last valid bit
-    auto shr = [&](uint64_t v, int d, size_t row) -> uint64_t {
+    auto shr = [&](uint64_t v, int d, unsigned row) -> uint64_t {
         const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v, 1);
         uint64_t in = lo & 1u;
         if (need_e) {
-            in = __ldg(s + (size_t)d * ps + row + eidx) & 1ull;
+            in = __ldg(s + (d * ps + row + eidx)) & 1ull;
             if (d == WEST && row == row0 && forcing && ex == a.fx)
                 in &= ~force_flip_at<MODEL, GM>(a, y);
         }
@@ -182,34 +183,37 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const int y, const 
             out[d] = o;
         }
     }
-    const uint64_t m = (w == g.nw - 1) ? g.lastmask : ~0ull;
+    if (w == g.nw - 1) {  // clear the tail bits past site W-1
+#pragma unroll
+        for (int d = 0; d < D; ++d) out[d] &= g.lastmask;
+    }
     uint64_t *__restrict__ dp = a.dst + row0 + w;
 #pragma unroll
-    for (int d = 0; d < D; ++d) dp[(size_t)d * ps] = out[d] & m;
+    for (int d = 0; d < D; ++d) dp[d * ps] = out[d];
 }
 
+// Grid: x = 32-word chunk of a row, y = group of STEP_WARPS rows; one warp
+// per (row, chunk).
+static constexpr int STEP_WARPS = 8;
+
 template <int MODEL, int GM>
-__global__ void __launch_bounds__(256) k_step(const StepArgs a)
+__global__ void __launch_bounds__(32 * STEP_WARPS) k_step(const StepArgs a)
 {
-    const int lane = threadIdx.x & 31;
-    const long long task = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (task >= (long long)a.g.H * a.chunks) return;
-    const int y = (int)(task / a.chunks);
-    const int chunk = (int)(task - (long long)y * a.chunks);
-    step_word<MODEL, GM>(a, y, chunk * 32 + lane, lane);
+    const int y = blockIdx.y * STEP_WARPS + threadIdx.y;
+    if (y >= a.g.H) return;  // whole warp
+    step_word<MODEL, GM>(a, y, blockIdx.x * 32 + threadIdx.x, threadIdx.x);
 }
 
 template <int MODEL>
 static cudaError_t launch_model(int gm, const StepArgs &a, cudaStream_t st)
 {
-    const long long tasks = (long long)a.g.H * a.chunks;
-    const int threads = 256;
-    const long long blocks = (tasks + (threads / 32) - 1) / (threads / 32);
-    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    const dim3 block(32, STEP_WARPS);
+    const dim3 grid((unsigned)a.chunks, (unsigned)((a.g.H + STEP_WARPS - 1) / STEP_WARPS));
+    if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
     switch (gm) {
-    case GEOM_NONE: k_step<MODEL, GEOM_NONE><<<(unsigned)blocks, threads, 0, st>>>(a); break;
-    case GEOM_NOSLIP: k_step<MODEL, GEOM_NOSLIP><<<(unsigned)blocks, threads, 0, st>>>(a); break;
-    default: k_step<MODEL, GEOM_FULL><<<(unsigned)blocks, threads, 0, st>>>(a); break;
+    case GEOM_NONE: k_step<MODEL, GEOM_NONE><<<grid, block, 0, st>>>(a); break;
+    case GEOM_NOSLIP: k_step<MODEL, GEOM_NOSLIP><<<grid, block, 0, st>>>(a); break;
+    default: k_step<MODEL, GEOM_FULL><<<grid, block, 0, st>>>(a); break;
     }
     return cudaGetLastError();
 }

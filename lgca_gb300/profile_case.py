@@ -1,0 +1,61 @@
+"""Run one lattice workload on the GPU for a fixed number of steps: a small,
+self-contained driver for profilers (ncu) and for quick timings.
+
+    python -m lgca_gb300.profile_case --model 3 --W 32768 --H 16384 --steps 3
+    python -m lgca_gb300.profile_case --geometry karman --W 8192 --H 2048 --force-x 16 --force-p 0.02
+
+Prints the average time per step measured with CUDA events.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+import lgca_gb300 as gpu
+from lgca_gb300 import geometry as G
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--model", type=int, default=3)
+    ap.add_argument("--W", type=int, default=32768)
+    ap.add_argument("--H", type=int, default=16384)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--depth", type=int, default=1)
+    ap.add_argument("--variant", type=int, default=0,
+                    help="0 auto, 1 one step per pass, 2 register wavefront, 3 shared-memory tiles")
+    ap.add_argument("--geometry", default="periodic", choices=["periodic", "pipe", "karman"])
+    ap.add_argument("--force-x", type=int, default=-1)
+    ap.add_argument("--force-p", type=float, default=0.0)
+    ap.add_argument("--p", type=float, default=0.5)
+    ap.add_argument("--block", type=int, default=0, help="also compute BxB block sums per step")
+    args = ap.parse_args(argv)
+
+    gpu.build()
+    L = gpu.GpuLattice(args.model, args.W, args.H, seed=3)
+    if args.geometry == "pipe":
+        L.set_cell_types(G.pipe(args.W, args.H))
+    elif args.geometry == "karman":
+        L.set_cell_types(G.disc(args.W, args.H, args.W // 8, args.H // 2, args.H // 16))
+    L.init_random(args.p, args.p)
+    L.set_forcing_column(args.force_x, args.force_p)
+    L.set_temporal_depth(args.depth)
+    L.set_kernel_variant(args.variant)
+    L.collide_and_propagate(args.warmup)
+    L.sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.collide_and_propagate(1 if args.depth == 1 else args.depth)
+        if args.block:
+            L.block_sums(args.block)
+    L.sync()
+    dt = time.perf_counter() - t0
+    n = args.steps * (1 if args.depth == 1 else args.depth)
+    print(f"{args.W}x{args.H} model {args.model} depth {args.depth} variant {args.variant}: {n} steps, {dt / n * 1e3:.4f} ms/step (host clock), "
+          f"{args.W * args.H * n / dt / 1e9:.1f} GSite-updates/s")
+    L.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -18,7 +18,7 @@ def sha(a):
 
 
 def run_gpu(gpu, model, init, steps, types=None, seed=0, chir=None, force_x=-1, force_p=0.0, t0=0,
-            depth=1, chunks=None):
+            depth=1, chunks=None, variant=0):
     H, W = init.shape
     with gpu.GpuLattice(model, W, H, seed) as L:
         if types is not None:
@@ -29,6 +29,7 @@ def run_gpu(gpu, model, init, steps, types=None, seed=0, chir=None, force_x=-1, 
             L.set_chirality(chir)
         L.set_forcing_column(force_x, force_p)
         L.set_temporal_depth(depth)
+        L.set_kernel_variant(variant)
         if chunks is None:
             L.collide_and_propagate(steps)
         else:
@@ -171,3 +172,58 @@ def test_large_periodic_mass_and_block_totals(gpu, model):
         # a periodic lattice without obstacles or forcing conserves momentum
         assert int(Jx2.astype(np.int64).sum()) == int(jx0.astype(np.int64).sum())
         assert int(Jy.astype(np.int64).sum()) == int(jy0.astype(np.int64).sum())
+
+
+# ------------------------------------------------ temporally blocked kernel
+GEOMS = {"periodic": G.periodic, "pipe": G.pipe, "karman": G.karman_reference,
+         "reflecting_back": lambda w, h: G.reflecting(w, h, "back"),
+         "reflecting_forward": lambda w, h: G.reflecting(w, h, "forward"),
+         "disc": lambda w, h: G.disc(w, h, w // 3, h // 2, max(1, h // 3))}
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("depth", [2, 3, 4, 5, 8])
+@pytest.mark.parametrize("geom", sorted(GEOMS))
+@pytest.mark.parametrize("variant", [2, 3])
+def test_temporal_blocking_vs_oracle(gpu, oracle, model, depth, geom, variant):
+    """k steps per pass give the same bits as one step per pass."""
+    rng = np.random.default_rng(depth * 31 + model)
+    for W, H in [(64, 2), (128, 10), (2048, 18), (4160, 40), (256, 64)]:
+        types = GEOMS[geom](W, H)
+        seed = int(rng.integers(1 << 40))
+        st = oracle.init_bernoulli(model, W, H, types, seed=seed, p_move=0.35, p_rest=0.3)
+        fx = int(rng.choice([x for x in (0, 63, 64, W - 1, int(rng.integers(W))) if x < W]))
+        kw = dict(types=types, seed=seed, force_x=fx, force_p=0.5, t0=int(rng.integers(50)))
+        want = oracle.run(model, st, 19, **kw)
+        got = run_gpu(gpu, model, st, 19, depth=depth, variant=variant, **kw)
+        assert np.array_equal(got, want), (W, H, fx)
+
+
+@pytest.mark.parametrize("model", [1, 3])
+@pytest.mark.parametrize("variant", [2, 3])
+def test_temporal_blocking_frozen_chirality(gpu, oracle, model, variant):
+    rng = np.random.default_rng(5)
+    W, H = 640, 36
+    st = oracle.init_bernoulli(model, W, H, None, seed=9, p_move=0.4)
+    chir = rng.integers(0, 2, (H, W), dtype=np.uint8)
+    want = oracle.run(model, st, 16, chir=chir, seed=9)
+    got = run_gpu(gpu, model, st, 16, chir=chir, seed=9, depth=8, variant=variant)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("depth", [2, 4, 8])
+@pytest.mark.parametrize("variant", [2, 3])
+def test_temporal_blocking_karman_config(gpu, depth, variant):
+    """Full-size Karman workload with k steps per pass: pinned reference states."""
+    pins = load_json("config_pins.json")["karman_fhp3_8192x2048"]
+    W, H = 8192, 2048
+    with gpu.GpuLattice(3, W, H, seed=2) as L:
+        L.set_cell_types(G.disc(W, H, 1024, 1024, 128))
+        L.init_random(0.3, 0.3)
+        L.set_forcing_column(16, 0.02)
+        L.set_temporal_depth(depth)
+        L.set_kernel_variant(variant)
+        L.collide_and_propagate(100)
+        assert sha(L.download()) == pins["t100_sha"]
+        L.collide_and_propagate(100)
+        assert sha(L.download()) == pins["t200_sha"]
