@@ -156,6 +156,29 @@ int lgca_block_sums_device(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32
 int lgca_post_process(lgca_handle h, int r, float *cell_density, float *cell_momentum,
                       float *mean_density, float *mean_momentum);
 
+/* Allocation-free random-cell body force.  No counterpart in the reference:
+ * an extra entry point of this library for callers that must not allocate
+ * device memory during a run -- a host that has handed its whole device
+ * budget to resident lattices, or one that cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree between queued steps.  Same rule
+ * and draws as lgca_apply_body_force (its FSEQ call index is `call`), on
+ * caller-owned device buffers in the layout of lgca_state_device: `planes`
+ * (NUM_DIR planes, `plane_stride` words apart, rows `row_pitch` words apart),
+ * optional `solid` / `slip` planes of the same shape (NULL = none), and an
+ * optional device counter `reverted`.  Enqueued on `stream` (NULL = default
+ * stream); nothing is allocated or freed.  Its work arrays live in one fixed
+ * device array of LGCA_NOALLOC_MAX_CELLS * 4 bytes + 4 KiB that every GPU
+ * loading the library holds until exit; lattices above LGCA_NOALLOC_MAX_CELLS
+ * cells are rejected with LGCA_ERR_INVALID.  The first call on a device looks
+ * the array up (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls share the array: calls whose work overlaps on the GPU
+ * race and must be ordered by the caller. */
+#define LGCA_NOALLOC_MAX_CELLS 2097152ULL
+int lgca_apply_body_force_noalloc(int model, int dim_x, int dim_y, uint64_t *planes,
+                                  size_t plane_stride, int row_pitch, const uint64_t *solid,
+                                  const uint64_t *slip, uint64_t seed, uint64_t call, int forcing,
+                                  int bf_dir, unsigned long long *reverted, void *stream);
+
 /* Wait for all work of the handle. */
 int lgca_sync(lgca_handle h);
 

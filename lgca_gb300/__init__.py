@@ -81,6 +81,9 @@ def lib() -> C.CDLL:
             "lgca_state_device": (C.c_int, [vp, C.POINTER(vp), C.POINTER(C.c_size_t),
                                             C.POINTER(C.c_int)]),
             "lgca_device_bytes": (C.c_int, [vp, C.POINTER(C.c_size_t)]),
+            "lgca_apply_body_force_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, C.c_size_t,
+                                                        C.c_int, vp, vp, u64, u64, C.c_int,
+                                                        C.c_int, vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

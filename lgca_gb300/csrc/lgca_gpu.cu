@@ -113,6 +113,11 @@ bool valid(lgca_handle h) { return h != nullptr && h->buf[0] != nullptr; }
 
 }  // namespace
 
+namespace lgca_gpu {
+// Error message for lgca_last_error(NULL) from entry points without a handle.
+void record_error(const char *msg) { g_err = msg; }
+}  // namespace lgca_gpu
+
 extern "C" {
 
 int lgca_abi_version(void) { return LGCA_GPU_ABI_VERSION; }
