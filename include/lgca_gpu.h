@@ -111,7 +111,10 @@ int lgca_set_temporal_depth(lgca_handle h, int depth);
 
 /* Kernel family for the steps: 0 = automatic (default), 1 = one step per
  * pass only, 2 = register wavefront (several steps per pass), 3 = shared-
- * memory tiles (several steps per pass).  Results do not depend on it.
+ * memory tiles (several steps per pass), 4 = persistent (all steps of a call
+ * in one cooperative launch with a bounded grid barrier between steps; a
+ * barrier wait that times out makes lgca_sync return LGCA_ERR_TIMEOUT).
+ * Results do not depend on it.
  * No reference counterpart (a scheduling choice of this engine). */
 int lgca_set_kernel_variant(lgca_handle h, int variant);
 

@@ -62,8 +62,26 @@ bool multistep_supported(int model, const PlaneGeom &g, int depth);
 cudaError_t launch_wave(int model, int geom_mode, const MultiStepArgs &a, cudaStream_t stream);
 bool wave_supported(int model, const PlaneGeom &g, int depth);
 
+// Persistent form (step.cu): nsteps steps in one cooperative launch, buf0
+// holding the input; the result is in buf0 if nsteps is even, else in buf1.
+// `sy` must be zeroed before the launch; sy->err != 0 afterwards means a
+// bounded grid-barrier wait gave up.
+struct PersistSync {
+    unsigned count, gen;
+    int err, pad;
+};
+cudaError_t launch_persistent(int model, int geom_mode, const StepArgs &a, uint64_t *buf0,
+                              uint64_t *buf1, uint64_t seed, uint64_t t0, int nsteps,
+                              PersistSync *sy, cudaStream_t stream);
+
 // Kernel families selectable per handle.
-enum : int { VARIANT_AUTO = 0, VARIANT_PLAIN = 1, VARIANT_WAVE = 2, VARIANT_TILE = 3 };
+enum : int {
+    VARIANT_AUTO = 0,
+    VARIANT_PLAIN = 1,
+    VARIANT_WAVE = 2,
+    VARIANT_TILE = 3,
+    VARIANT_PERSIST = 4
+};
 
 // Layout conversion between the reference byte-per-cell format and planes.
 cudaError_t launch_aos_to_planes(int D, const PlaneGeom &g, const uint8_t *aos, uint64_t *planes,

@@ -32,6 +32,8 @@ struct lgca_lattice {
     cudaStream_t own_stream = nullptr, stream = nullptr;
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    PersistSync *sync = nullptr;  // grid-barrier state of the persistent kernel
+    int *sync_err_host = nullptr; // pinned copy of sync->err, checked at sync points
     size_t bytes = 0;
     std::string err;
 };
@@ -201,6 +203,8 @@ int lgca_destroy(lgca_handle h)
     cudaFree(h->slip);
     cudaFree(h->chir);
     cudaFree(h->scratch);
+    cudaFree(h->sync);
+    if (h->sync_err_host) cudaFreeHost(h->sync_err_host);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return LGCA_OK;
@@ -376,7 +380,7 @@ int lgca_set_temporal_depth(lgca_handle h, int depth)
 int lgca_set_kernel_variant(lgca_handle h, int variant)
 {
     CHECK_HANDLE(h);
-    if (variant < VARIANT_AUTO || variant > VARIANT_TILE)
+    if (variant < VARIANT_AUTO || variant > VARIANT_PERSIST)
         return fail(h, LGCA_ERR_INVALID, "unknown kernel variant %d", variant);
     h->variant = variant;
     return LGCA_OK;
@@ -396,6 +400,22 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     a.force_thr = h->force_thr;
     a.fx = h->force_x;
     const int gm = geom_mode(h);
+    if (h->variant == VARIANT_PERSIST && nsteps > 1) {
+        if (!h->sync) {
+            CK(h, cudaMalloc(&h->sync, sizeof(PersistSync)));
+            CK(h, cudaHostAlloc(&h->sync_err_host, sizeof(int), cudaHostAllocDefault));
+            *h->sync_err_host = 0;
+            h->bytes += sizeof(PersistSync);
+        }
+        CK(h, cudaMemsetAsync(h->sync, 0, sizeof(PersistSync), h->stream));
+        CK(h, launch_persistent(h->model, gm, a, h->buf[h->cur], h->buf[h->cur ^ 1], h->seed, h->t,
+                                nsteps, h->sync, h->stream));
+        CK(h, cudaMemcpyAsync(h->sync_err_host, &h->sync->err, sizeof(int), cudaMemcpyDeviceToHost,
+                              h->stream));
+        if (nsteps & 1) h->cur ^= 1;
+        h->t += (uint64_t)nsteps;
+        return LGCA_OK;
+    }
     int done = 0;
     while (done < nsteps) {
         // largest supported depth that fits, else one step per pass
@@ -560,6 +580,10 @@ int lgca_sync(lgca_handle h)
     CHECK_HANDLE(h);
     DeviceGuard dg(h->device);
     CK(h, cudaStreamSynchronize(h->stream));
+    if (h->sync_err_host && *h->sync_err_host) {
+        *h->sync_err_host = 0;
+        return fail(h, LGCA_ERR_TIMEOUT, "a grid-barrier wait of the persistent kernel timed out");
+    }
     return LGCA_OK;
 }
 

@@ -40,7 +40,8 @@ def main(argv=None):
         L.set_cell_types(G.disc(args.W, args.H, args.W // 8, args.H // 2, args.H // 16))
     L.init_random(args.p, args.p)
     L.set_forcing_column(args.force_x, args.force_p)
-    L.set_temporal_depth(args.depth)
+    if args.variant != 4:
+        L.set_temporal_depth(args.depth)
     L.set_kernel_variant(args.variant)
     L.collide_and_propagate(args.warmup)
     L.sync()

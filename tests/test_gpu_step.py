@@ -184,7 +184,7 @@ GEOMS = {"periodic": G.periodic, "pipe": G.pipe, "karman": G.karman_reference,
 @pytest.mark.parametrize("model", MODELS)
 @pytest.mark.parametrize("depth", [2, 3, 4, 5, 8])
 @pytest.mark.parametrize("geom", sorted(GEOMS))
-@pytest.mark.parametrize("variant", [2, 3])
+@pytest.mark.parametrize("variant", [2, 3, 4])
 def test_temporal_blocking_vs_oracle(gpu, oracle, model, depth, geom, variant):
     """k steps per pass give the same bits as one step per pass."""
     rng = np.random.default_rng(depth * 31 + model)
@@ -200,7 +200,7 @@ def test_temporal_blocking_vs_oracle(gpu, oracle, model, depth, geom, variant):
 
 
 @pytest.mark.parametrize("model", [1, 3])
-@pytest.mark.parametrize("variant", [2, 3])
+@pytest.mark.parametrize("variant", [2, 3, 4])
 def test_temporal_blocking_frozen_chirality(gpu, oracle, model, variant):
     rng = np.random.default_rng(5)
     W, H = 640, 36
@@ -212,7 +212,7 @@ def test_temporal_blocking_frozen_chirality(gpu, oracle, model, variant):
 
 
 @pytest.mark.parametrize("depth", [2, 4, 8])
-@pytest.mark.parametrize("variant", [2, 3])
+@pytest.mark.parametrize("variant", [2, 3, 4])
 def test_temporal_blocking_karman_config(gpu, depth, variant):
     """Full-size Karman workload with k steps per pass: pinned reference states."""
     pins = load_json("config_pins.json")["karman_fhp3_8192x2048"]
