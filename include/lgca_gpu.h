@@ -112,9 +112,11 @@ int lgca_set_temporal_depth(lgca_handle h, int depth);
 /* Kernel family for the steps: 0 = automatic (default), 1 = one step per
  * pass only, 2 = register wavefront (several steps per pass), 3 = shared-
  * memory tiles (several steps per pass), 4 = persistent (all steps of a call
- * in one cooperative launch with a bounded grid barrier between steps; a
- * barrier wait that times out makes lgca_sync return LGCA_ERR_TIMEOUT).
- * Results do not depend on it.
+ * in one cooperative launch; each block owns a band of rows and waits, with a
+ * bounded wait, only for its two neighbour bands between steps; a wait that
+ * times out makes lgca_sync return LGCA_ERR_TIMEOUT),
+ * 5 = one step per pass with two words per lane where dim_x is a multiple of
+ * 128 (variant 1 keeps one word per lane).  Results do not depend on it.
  * No reference counterpart (a scheduling choice of this engine). */
 int lgca_set_kernel_variant(lgca_handle h, int variant);
 

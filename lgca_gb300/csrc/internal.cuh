@@ -42,6 +42,7 @@ struct StepArgs {
     uint64_t force_key; // lgca_rng_key(seed, FORCE, t)
     uint64_t force_thr; // 0 disables forcing
     int fx;             // forcing column (valid when force_thr > 0)
+    int wpt;            // words per lane of the one-step kernel (1 or 2)
 };
 
 // One lattice step of `a` (k = 1), launched on `stream`.
@@ -62,17 +63,15 @@ bool multistep_supported(int model, const PlaneGeom &g, int depth);
 cudaError_t launch_wave(int model, int geom_mode, const MultiStepArgs &a, cudaStream_t stream);
 bool wave_supported(int model, const PlaneGeom &g, int depth);
 
-// Persistent form (step.cu): nsteps steps in one cooperative launch, buf0
-// holding the input; the result is in buf0 if nsteps is even, else in buf1.
-// `sy` must be zeroed before the launch; sy->err != 0 afterwards means a
-// bounded grid-barrier wait gave up.
-struct PersistSync {
-    unsigned count, gen;
-    int err, pad;
-};
+// Persistent band form (step.cu): nsteps steps in one cooperative launch,
+// buf0 holding the input; the result is in buf0 if nsteps is even, else in
+// buf1.  `flags` holds one int per block (at most max_blocks) and, like
+// *err, must be zero before the launch; *err != 0 afterwards means a bounded
+// neighbour wait gave up.
+static constexpr int PERSIST_MAX_BLOCKS = 1024;
 cudaError_t launch_persistent(int model, int geom_mode, const StepArgs &a, uint64_t *buf0,
-                              uint64_t *buf1, uint64_t seed, uint64_t t0, int nsteps,
-                              PersistSync *sy, cudaStream_t stream);
+                              uint64_t *buf1, uint64_t seed, uint64_t t0, int nsteps, int *flags,
+                              int *err, int max_blocks, cudaStream_t stream);
 
 // Kernel families selectable per handle.
 enum : int {
@@ -80,7 +79,8 @@ enum : int {
     VARIANT_PLAIN = 1,
     VARIANT_WAVE = 2,
     VARIANT_TILE = 3,
-    VARIANT_PERSIST = 4
+    VARIANT_PERSIST = 4,
+    VARIANT_PLAIN2 = 5  // one step per pass, two words per lane
 };
 
 // Layout conversion between the reference byte-per-cell format and planes.

@@ -28,12 +28,13 @@ struct lgca_lattice {
     uint64_t force_thr = 0;
     int depth = 1;
     int variant = VARIANT_AUTO;
+    int wpt = 2;  // words per lane of the one-step kernel where the width allows
     int device = 0;
     cudaStream_t own_stream = nullptr, stream = nullptr;
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
-    PersistSync *sync = nullptr;  // grid-barrier state of the persistent kernel
-    int *sync_err_host = nullptr; // pinned copy of sync->err, checked at sync points
+    int *sync = nullptr;          // persistent kernel: error flag + one step flag per block
+    int *sync_err_host = nullptr; // pinned copy of the error flag, checked at sync points
     size_t bytes = 0;
     std::string err;
 };
@@ -380,7 +381,7 @@ int lgca_set_temporal_depth(lgca_handle h, int depth)
 int lgca_set_kernel_variant(lgca_handle h, int variant)
 {
     CHECK_HANDLE(h);
-    if (variant < VARIANT_AUTO || variant > VARIANT_PERSIST)
+    if (variant < VARIANT_AUTO || variant > VARIANT_PLAIN2)
         return fail(h, LGCA_ERR_INVALID, "unknown kernel variant %d", variant);
     h->variant = variant;
     return LGCA_OK;
@@ -399,18 +400,20 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     a.chunks = (h->g.nw + 31) / 32;
     a.force_thr = h->force_thr;
     a.fx = h->force_x;
+    a.wpt = (h->variant == VARIANT_PLAIN) ? 1 : h->wpt;
     const int gm = geom_mode(h);
     if (h->variant == VARIANT_PERSIST && nsteps > 1) {
+        const size_t sync_bytes = (size_t)(PERSIST_MAX_BLOCKS + 1) * sizeof(int);
         if (!h->sync) {
-            CK(h, cudaMalloc(&h->sync, sizeof(PersistSync)));
+            CK(h, cudaMalloc(&h->sync, sync_bytes));
             CK(h, cudaHostAlloc(&h->sync_err_host, sizeof(int), cudaHostAllocDefault));
             *h->sync_err_host = 0;
-            h->bytes += sizeof(PersistSync);
+            h->bytes += sync_bytes;
         }
-        CK(h, cudaMemsetAsync(h->sync, 0, sizeof(PersistSync), h->stream));
+        CK(h, cudaMemsetAsync(h->sync, 0, sync_bytes, h->stream));
         CK(h, launch_persistent(h->model, gm, a, h->buf[h->cur], h->buf[h->cur ^ 1], h->seed, h->t,
-                                nsteps, h->sync, h->stream));
-        CK(h, cudaMemcpyAsync(h->sync_err_host, &h->sync->err, sizeof(int), cudaMemcpyDeviceToHost,
+                                nsteps, h->sync + 1, h->sync, PERSIST_MAX_BLOCKS, h->stream));
+        CK(h, cudaMemcpyAsync(h->sync_err_host, h->sync, sizeof(int), cudaMemcpyDeviceToHost,
                               h->stream));
         if (nsteps & 1) h->cur ^= 1;
         h->t += (uint64_t)nsteps;
@@ -421,7 +424,7 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
         // largest supported depth that fits, else one step per pass
         int k = std::min(h->depth, nsteps - done);
         const bool tile = h->variant == VARIANT_TILE;
-        if (h->variant == VARIANT_PLAIN) k = 1;
+        if (h->variant == VARIANT_PLAIN || h->variant == VARIANT_PLAIN2) k = 1;
         while (k > 1 && !(tile ? multistep_supported(h->model, h->g, k)
                                : wave_supported(h->model, h->g, k)))
             --k;
@@ -582,7 +585,7 @@ int lgca_sync(lgca_handle h)
     CK(h, cudaStreamSynchronize(h->stream));
     if (h->sync_err_host && *h->sync_err_host) {
         *h->sync_err_host = 0;
-        return fail(h, LGCA_ERR_TIMEOUT, "a grid-barrier wait of the persistent kernel timed out");
+        return fail(h, LGCA_ERR_TIMEOUT, "a neighbour wait of the persistent kernel timed out");
     }
     return LGCA_OK;
 }

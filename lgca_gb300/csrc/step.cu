@@ -42,13 +42,27 @@ struct StepIO {
     uint64_t ckey, fkey;  // chirality / forcing keys of the step
 };
 
-template <int MODEL, int GM>
+// State loads: the one-step kernels read buffers that no thread writes
+// during the launch (read-only path); the persistent band kernel reads
+// buffers that other blocks wrote earlier in the same launch, so it must
+// bypass the non-coherent L1 (ld.global.cg, cached in L2 only).
+template <bool CG> __device__ __forceinline__ uint64_t ld_state(const uint64_t *p)
+{
+    return CG ? __ldcg(p) : __ldg(p);
+}
+template <bool CG> __device__ __forceinline__ ulonglong2 ld_state2(const uint64_t *p)
+{
+    return CG ? __ldcg(reinterpret_cast<const ulonglong2 *>(p))
+              : __ldg(reinterpret_cast<const ulonglong2 *>(p));
+}
+
+template <int MODEL, int GM, bool CG = false>
 __device__ __forceinline__ uint64_t force_flip_at(const StepArgs &a, const StepIO &io, int y)
 {
     constexpr int WEST = (MODEL == M_HPP) ? 2 : 3;
     const int fw = a.fx >> 6, fb = a.fx & 63;
     const unsigned r0 = (unsigned)y * a.g.pitch + fw;
-    uint64_t n0 = io.src[r0], nw = io.src[WEST * (unsigned)a.g.ps + r0];
+    uint64_t n0 = ld_state<CG>(io.src + r0), nw = ld_state<CG>(io.src + (WEST * (unsigned)a.g.ps + r0));
     uint64_t fluid = ~0ull;
     if (GM >= GEOM_NOSLIP) fluid &= ~a.solid[r0];
     if (GM == GEOM_FULL) fluid &= ~a.slip[r0];
@@ -57,7 +71,7 @@ __device__ __forceinline__ uint64_t force_flip_at(const StepArgs &a, const StepI
     return (u < a.force_thr) ? cand : 0ull;
 }
 
-template <int MODEL, int GM>
+template <int MODEL, int GM, bool CG = false>
 __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, const int y,
                                           const int w, const int lane)
 {
@@ -83,7 +97,7 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
 
     uint64_t n[7];
 #pragma unroll
-    for (int d = 0; d < D; ++d) n[d] = active ? __ldg(s + (d * ps + row_of(d) + w)) : 0ull;
+    for (int d = 0; d < D; ++d) n[d] = active ? ld_state<CG>(s + (d * ps + row_of(d) + w)) : 0ull;
 
     uint64_t solid = 0, slip = 0;
     if (GM >= GEOM_NOSLIP && active) solid = __ldg(a.solid + row0 + w);
@@ -116,8 +130,9 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
         const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v >> 32), 1);
         uint64_t in = hi >> 31;
         if (need_w) {
-            in = (__ldg(s + (d * ps + row + widx)) >> wbit) & 1ull;
-            if (d == 0 && row == row0 && forcing && wx == a.fx) in |= force_flip_at<MODEL, GM>(a, io, y);
+            in = (ld_state<CG>(s + (d * ps + row + widx)) >> wbit) & 1ull;
+            if (d == 0 && row == row0 && forcing && wx == a.fx)
+                in |= force_flip_at<MODEL, GM, CG>(a, io, y);
         }
         return (v << 1) | in;
     };
@@ -126,9 +141,9 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
         const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v, 1);
         uint64_t in = lo & 1u;
         if (need_e) {
-            in = __ldg(s + (d * ps + row + eidx)) & 1ull;
+            in = ld_state<CG>(s + (d * ps + row + eidx)) & 1ull;
             if (d == WEST && row == row0 && forcing && ex == a.fx)
-                in &= ~force_flip_at<MODEL, GM>(a, io, y);
+                in &= ~force_flip_at<MODEL, GM, CG>(a, io, y);
         }
         return (v >> 1) | (in << epos);
     };
@@ -199,6 +214,168 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
     for (int d = 0; d < D; ++d) dp[d * ps] = out[d];
 }
 
+// Two words per lane (lattices with an even number of words per row, i.e.
+// W a multiple of 128): 16-byte loads and stores, one shuffle per shifted
+// plane for 128 sites, and half as many warps, so that an L2-resident lattice
+// fits in one wave of resident warps.  Same arithmetic as step_word.
+template <int MODEL, int GM, bool CG = false>
+__device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, const int y,
+                                          const int t, const int lane)
+{
+    constexpr int D = ModelTraits<MODEL>::D;
+    const PlaneGeom &g = a.g;
+    const int np = g.nw >> 1;
+    const bool active = t < np;
+    const int ym = (y == 0) ? g.H - 1 : y - 1;
+    const int yp = (y == g.H - 1) ? 0 : y + 1;
+    const unsigned rowm = (unsigned)ym * g.pitch, row0 = (unsigned)y * g.pitch,
+                   rowp = (unsigned)yp * g.pitch;
+    const uint64_t *__restrict__ s = io.src;
+    const unsigned ps = (unsigned)g.ps;
+    const bool even = (y & 1) == 0;
+    const int w0 = 2 * t;
+    auto row_of = [&](int d) -> unsigned {
+        if (MODEL == M_HPP) return d == 1 ? rowm : (d == 3 ? rowp : row0);
+        return (d == 1 || d == 2) ? rowm : ((d == 4 || d == 5) ? rowp : row0);
+    };
+    auto ld2 = [&](const uint64_t *base, unsigned off) -> ulonglong2 {  // state
+        return active ? ld_state2<CG>(base + off) : make_ulonglong2(0ull, 0ull);
+    };
+    auto ldg2 = [&](const uint64_t *base, unsigned off) -> ulonglong2 {  // read-only planes
+        return active ? __ldg(reinterpret_cast<const ulonglong2 *>(base + off))
+                      : make_ulonglong2(0ull, 0ull);
+    };
+
+    uint64_t n[2][7];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const ulonglong2 v = ld2(s, d * ps + row_of(d) + w0);
+        n[0][d] = v.x;
+        n[1][d] = v.y;
+    }
+    uint64_t solid[2] = {0, 0}, slip[2] = {0, 0};
+    if (GM >= GEOM_NOSLIP) {
+        const ulonglong2 v = ldg2(a.solid, row0 + w0);
+        solid[0] = v.x;
+        solid[1] = v.y;
+    }
+    if (GM == GEOM_FULL) {
+        const ulonglong2 v = ldg2(a.slip, row0 + w0);
+        slip[0] = v.x;
+        slip[1] = v.y;
+    }
+
+    constexpr int WEST = (MODEL == M_HPP) ? 2 : 3;
+    const bool forcing = a.force_thr != 0;
+    const int fw = a.fx >> 6;
+    if (forcing && active && (fw >> 1) == t) {
+        const uint64_t u =
+            lgca_rng_draw(io.fkey, lgca_rng_index((uint32_t)y, (uint32_t)a.fx)) >> 32;
+        const uint64_t bit = (u < a.force_thr) ? (1ull << (a.fx & 63)) : 0ull;
+        // masks per word of the pair (no run-time index into n, which would
+        // move the arrays to local memory)
+        const uint64_t m0 = (fw & 1) ? 0ull : bit, m1 = (fw & 1) ? bit : 0ull;
+        const uint64_t f0 = ~n[0][0] & n[0][WEST] & ~solid[0] & ~slip[0] & m0;
+        const uint64_t f1 = ~n[1][0] & n[1][WEST] & ~solid[1] & ~slip[1] & m1;
+        n[0][0] |= f0;
+        n[0][WEST] &= ~f0;
+        n[1][0] |= f1;
+        n[1][WEST] &= ~f1;
+    }
+
+    const bool need_w = active && (lane == 0 || t == 0);
+    const bool need_e = active && (lane == 31 || t == np - 1);
+    const int widx = (t == 0) ? g.nw - 1 : w0 - 1;
+    const int eidx = (t == np - 1) ? 0 : w0 + 2;
+    const int wx = (t == 0) ? g.W - 1 : 64 * w0 - 1;
+    const int ex = (t == np - 1) ? 0 : 64 * w0 + 128;
+
+    // x-1 pull of the pair (v0, v1)
+    auto shl = [&](uint64_t v0, uint64_t v1, int d, unsigned row, int k) -> uint64_t {
+        const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v1 >> 32), 1);
+        uint64_t in = hi >> 31;
+        if (need_w) {
+            in = ld_state<CG>(s + (d * ps + row + widx)) >> 63;
+            if (d == 0 && row == row0 && forcing && wx == a.fx)
+                in |= force_flip_at<MODEL, GM, CG>(a, io, y);
+        }
+        return k ? ((v1 << 1) | (v0 >> 63)) : ((v0 << 1) | in);
+    };
+    // x+1 pull of the pair
+    auto shr = [&](uint64_t v0, uint64_t v1, int d, unsigned row, int k) -> uint64_t {
+        const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v0, 1);
+        uint64_t in = lo & 1u;
+        if (need_e) {
+            in = ld_state<CG>(s + (d * ps + row + eidx)) & 1ull;
+            if (d == WEST && row == row0 && forcing && ex == a.fx)
+                in &= ~force_flip_at<MODEL, GM, CG>(a, io, y);
+        }
+        return k ? ((v1 >> 1) | (in << 63)) : ((v0 >> 1) | (v1 << 63));
+    };
+    // pulled values of word k of the pair
+    uint64_t q[2][7];
+    if (MODEL == M_HPP) {
+        const uint64_t a0 = shl(n[0][0], n[1][0], 0, row0, 0), a1 = shl(n[0][0], n[1][0], 0, row0, 1);
+        const uint64_t b0 = shr(n[0][2], n[1][2], 2, row0, 0), b1 = shr(n[0][2], n[1][2], 2, row0, 1);
+        q[0][0] = a0; q[1][0] = a1; q[0][2] = b0; q[1][2] = b1;
+        q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][3] = n[0][3]; q[1][3] = n[1][3];
+    } else {
+        const uint64_t a0 = shl(n[0][0], n[1][0], 0, row0, 0), a1 = shl(n[0][0], n[1][0], 0, row0, 1);
+        const uint64_t b0 = shr(n[0][3], n[1][3], 3, row0, 0), b1 = shr(n[0][3], n[1][3], 3, row0, 1);
+        q[0][0] = a0; q[1][0] = a1; q[0][3] = b0; q[1][3] = b1;
+        if (even) {
+            const uint64_t c0 = shl(n[0][1], n[1][1], 1, rowm, 0), c1 = shl(n[0][1], n[1][1], 1, rowm, 1);
+            const uint64_t e0 = shl(n[0][5], n[1][5], 5, rowp, 0), e1 = shl(n[0][5], n[1][5], 5, rowp, 1);
+            q[0][1] = c0; q[1][1] = c1; q[0][5] = e0; q[1][5] = e1;
+            q[0][2] = n[0][2]; q[1][2] = n[1][2]; q[0][4] = n[0][4]; q[1][4] = n[1][4];
+        } else {
+            const uint64_t c0 = shr(n[0][2], n[1][2], 2, rowm, 0), c1 = shr(n[0][2], n[1][2], 2, rowm, 1);
+            const uint64_t e0 = shr(n[0][4], n[1][4], 4, rowp, 0), e1 = shr(n[0][4], n[1][4], 4, rowp, 1);
+            q[0][2] = c0; q[1][2] = c1; q[0][4] = e0; q[1][4] = e1;
+            q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][5] = n[0][5]; q[1][5] = n[1][5];
+        }
+        if (D == 7) { q[0][6] = n[0][6]; q[1][6] = n[1][6]; }
+    }
+    if (!active) return;
+
+    const bool nsrow = (y == 0) || (y == g.H - 1);
+    uint64_t out[2][7];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        uint64_t p[7], c[7];
+#pragma unroll
+        for (int d = 0; d < D; ++d) c[d] = p[d] = q[k][d];
+        if (MODEL != M_HPP) {
+            const uint64_t chir =
+                a.chir ? __ldg(a.chir + row0 + w0 + k)
+                       : lgca_rng_draw(io.ckey, lgca_rng_index((uint32_t)y, (uint32_t)(w0 + k)));
+            collide<MODEL>(c, chir);
+        } else {
+            collide<MODEL>(c, 0ull);
+        }
+        if (GM == GEOM_NONE) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) out[k][d] = c[d];
+        } else {
+            const uint64_t fl = ~(solid[k] | slip[k]);
+            const uint64_t ew = (w0 + k == 0 ? 1ull : 0ull) | (w0 + k == g.nw - 1 ? (1ull << 63) : 0ull);
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                uint64_t o = (fl & c[d]) | (solid[k] & p[Dirs<MODEL>::inv(d)]);
+                if (GM == GEOM_FULL) {
+                    const uint64_t sx = nsrow ? p[Dirs<MODEL>::mirx(d)] : p[d];
+                    o |= slip[k] & ((ew & p[Dirs<MODEL>::miry(d)]) | (~ew & sx));
+                }
+                out[k][d] = o;
+            }
+        }
+    }
+    uint64_t *__restrict__ dp = io.dst + row0 + w0;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        *reinterpret_cast<ulonglong2 *>(dp + d * ps) = make_ulonglong2(out[0][d], out[1][d]);
+}
+
 // Grid: x = 32-word chunk of a row, y = group of STEP_WARPS rows; one warp
 // per (row, chunk).
 static constexpr int STEP_WARPS = 8;
@@ -212,9 +389,34 @@ __global__ void __launch_bounds__(32 * STEP_WARPS) k_step(const StepArgs a)
     step_word<MODEL, GM>(a, io, y, blockIdx.x * 32 + threadIdx.x, threadIdx.x);
 }
 
+template <int MODEL, int GM>
+__global__ void __launch_bounds__(32 * STEP_WARPS) k_step2(const __grid_constant__ StepArgs a)
+{
+    const int y = blockIdx.y * STEP_WARPS + threadIdx.y;
+    if (y >= a.g.H) return;
+    const StepIO io{a.src, a.dst, a.chir_key, a.force_key};
+    step_pair<MODEL, GM>(a, io, y, blockIdx.x * 32 + threadIdx.x, threadIdx.x);
+}
+
+template <int MODEL>
+static cudaError_t launch_model2(int gm, const StepArgs &a, cudaStream_t st)
+{
+    const int np = a.g.nw / 2;
+    const dim3 block(32, STEP_WARPS);
+    const dim3 grid((unsigned)((np + 31) / 32), (unsigned)((a.g.H + STEP_WARPS - 1) / STEP_WARPS));
+    if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
+    switch (gm) {
+    case GEOM_NONE: k_step2<MODEL, GEOM_NONE><<<grid, block, 0, st>>>(a); break;
+    case GEOM_NOSLIP: k_step2<MODEL, GEOM_NOSLIP><<<grid, block, 0, st>>>(a); break;
+    default: k_step2<MODEL, GEOM_FULL><<<grid, block, 0, st>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
 template <int MODEL>
 static cudaError_t launch_model(int gm, const StepArgs &a, cudaStream_t st)
 {
+    if (a.wpt == 2 && (a.g.nw % 2) == 0 && (a.g.W % 64) == 0) return launch_model2<MODEL>(gm, a, st);
     const dim3 block(32, STEP_WARPS);
     const dim3 grid((unsigned)a.chunks, (unsigned)((a.g.H + STEP_WARPS - 1) / STEP_WARPS));
     if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
@@ -227,9 +429,14 @@ static cudaError_t launch_model(int gm, const StepArgs &a, cudaStream_t st)
 }
 
 // ------------------------------------------------------------------
-// Persistent form: one cooperative launch advances nsteps steps, the blocks
-// meeting at a grid-wide barrier between steps.  For lattices that fit in L2
-// this removes the per-step launch, ramp-up and tail of the one-step kernel.
+// Persistent band form: one cooperative launch advances nsteps steps.  Block
+// b (one per SM) owns the rows of band b and steps them; a step of band b
+// needs only the edge rows of bands b-1 and b+1 from the previous step, and
+// must not overwrite the previous-step rows those bands still read.  So
+// after each step a block publishes its step count and waits for its two
+// neighbours to reach the same count -- no grid-wide barrier.  The waits are
+// bounded: past PERSIST_WAIT_NS, or when another block reported a timeout, a
+// block records the error and stops; the host reports LGCA_ERR_TIMEOUT.
 
 __device__ __forceinline__ uint64_t globaltimer_ns()
 {
@@ -238,123 +445,115 @@ __device__ __forceinline__ uint64_t globaltimer_ns()
     return t;
 }
 
-// Barrier over all blocks of a cooperative launch (all co-resident).  The
-// wait is bounded: a block that waits longer than PERSIST_WAIT_NS, or sees
-// the error flag, records the error and returns false; the kernel then stops
-// and the host reports LGCA_ERR_TIMEOUT.
 static constexpr uint64_t PERSIST_WAIT_NS = 2000000000ull;
 
-__device__ bool grid_barrier(PersistSync *sy, unsigned nblocks)
-{
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        ok = 1;
-        volatile unsigned *vgen = &sy->gen;
-        volatile int *verr = &sy->err;
-        const unsigned g = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(&sy->count, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(&sy->count, 0u);
-            __threadfence();
-            atomicAdd(&sy->gen, 1u);
-        } else {
-            const uint64_t t0 = globaltimer_ns();
-            while (*vgen == g) {
-                if (*verr) { ok = 0; break; }
-                if (globaltimer_ns() - t0 > PERSIST_WAIT_NS) {
-                    atomicExch(&sy->err, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return ok != 0;
-}
-
-template <int MODEL, int GM>
-__global__ void __launch_bounds__(32 * STEP_WARPS) k_persist(const StepArgs a, uint64_t *buf0,
-                                                             uint64_t *buf1, uint64_t seed,
-                                                             uint64_t t0, int nsteps,
-                                                             PersistSync *sy)
+template <int MODEL, int GM, int WPT>
+__global__ void k_band(const __grid_constant__ StepArgs a, uint64_t *buf0, uint64_t *buf1,
+                       uint64_t seed, uint64_t t0, int nsteps, int *flags, int *err)
 {
     __shared__ uint64_t keys[2];
-    const unsigned nblocks = gridDim.x;
-    const int lane = threadIdx.x;
-    const int gwarp = blockIdx.x * STEP_WARPS + threadIdx.y;
-    const int nwarps = gridDim.x * STEP_WARPS;
-    const int tasks = a.g.H * a.chunks;
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
+    __shared__ int stop;
+    const int nb = gridDim.x, b = blockIdx.x;
+    const int bl = (b + nb - 1) % nb, br = (b + 1) % nb;
+    const int y0 = (int)((long long)a.g.H * b / nb), y1 = (int)((long long)a.g.H * (b + 1) / nb);
+    const int per_row = WPT == 2 ? (a.g.nw / 2 + 31) / 32 : (a.g.nw + 31) / 32;
+    const int tasks = (y1 - y0) * per_row;
+    const int lane = threadIdx.x, warp = threadIdx.y, nwarps = blockDim.y;
+    const bool leader = lane == 0 && warp == 0;
+    if (leader) {
         keys[0] = lgca_rng_key(seed, LGCA_STREAM_CHIR, t0);
         keys[1] = lgca_rng_key(seed, LGCA_STREAM_FORCE, t0);
+        stop = 0;
     }
     __syncthreads();
     for (int s = 0; s < nsteps; ++s) {
         const StepIO io{(s & 1) ? buf1 : buf0, (s & 1) ? buf0 : buf1, keys[0], keys[1]};
-        for (int task = gwarp; task < tasks; task += nwarps) {
-            const int y = task / a.chunks;
-            const int chunk = task - y * a.chunks;
-            step_word<MODEL, GM>(a, io, y, chunk * 32 + lane, lane);
+        for (int task = warp; task < tasks; task += nwarps) {
+            const int y = y0 + task / per_row, c = task % per_row;
+            if (WPT == 2) step_pair<MODEL, GM, true>(a, io, y, c * 32 + lane, lane);
+            else step_word<MODEL, GM, true>(a, io, y, c * 32 + lane, lane);
         }
         if (s + 1 == nsteps) break;
-        __syncthreads();  // everyone has read this step's keys
-        if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __syncthreads();  // the band's step s is written; keys[] no longer read
+        if (leader) {
+            __threadfence();
+            atomicExch(flags + b, s + 1);
+            volatile int *vf = flags;
+            volatile int *verr = err;
+            const uint64_t tw = globaltimer_ns();
+            while (vf[bl] < s + 1 || vf[br] < s + 1) {
+                if (*verr || globaltimer_ns() - tw > PERSIST_WAIT_NS) {
+                    atomicExch(err, 1);
+                    stop = 1;
+                    break;
+                }
+                __nanosleep(32);
+            }
+            __threadfence();
             keys[0] = lgca_rng_key(seed, LGCA_STREAM_CHIR, t0 + s + 1);
             keys[1] = lgca_rng_key(seed, LGCA_STREAM_FORCE, t0 + s + 1);
         }
-        if (!grid_barrier(sy, nblocks)) return;
+        __syncthreads();
+        if (stop) return;
     }
 }
 
-template <int MODEL, int GM>
-static cudaError_t persist_launch(const StepArgs &a, uint64_t *buf0, uint64_t *buf1, uint64_t seed,
-                                  uint64_t t0, int nsteps, PersistSync *sy, cudaStream_t st)
+template <int MODEL, int GM, int WPT>
+static cudaError_t band_launch(const StepArgs &a, uint64_t *buf0, uint64_t *buf1, uint64_t seed,
+                               uint64_t t0, int nsteps, int *flags, int *err, int max_blocks,
+                               cudaStream_t st)
 {
-    auto kern = k_persist<MODEL, GM>;
-    int dev = 0, nsm = 0, per_sm = 0;
+    auto kern = k_band<MODEL, GM, WPT>;
+    int dev = 0, nsm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * STEP_WARPS, 0);
     if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorLaunchOutOfResources;
-    const int tasks = a.g.H * a.chunks;
-    int blocks = nsm * per_sm;
-    const int need = (tasks + STEP_WARPS - 1) / STEP_WARPS;
-    if (blocks > need) blocks = need;
+    // largest block (warps) of which one fits per SM
+    int warps = 0;
+    for (int w = 32; w >= 4; w /= 2) {
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * w, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm >= 1) { warps = w; break; }
+    }
+    if (warps == 0) return cudaErrorLaunchOutOfResources;
+    int blocks = nsm < a.g.H ? nsm : a.g.H;
+    if (blocks > max_blocks) blocks = max_blocks;
     StepArgs aa = a;
-    void *args[] = {(void *)&aa, (void *)&buf0, (void *)&buf1, (void *)&seed,
-                    (void *)&t0, (void *)&nsteps, (void *)&sy};
-    return cudaLaunchCooperativeKernel((void *)kern, dim3(blocks), dim3(32, STEP_WARPS), args, 0,
-                                       st);
+    void *args[] = {(void *)&aa, (void *)&buf0, (void *)&buf1, (void *)&seed, (void *)&t0,
+                    (void *)&nsteps, (void *)&flags, (void *)&err};
+    return cudaLaunchCooperativeKernel((void *)kern, dim3(blocks), dim3(32, warps), args, 0, st);
+}
+
+template <int MODEL, int GM>
+static cudaError_t band_wpt(const StepArgs &a, uint64_t *b0, uint64_t *b1, uint64_t seed,
+                            uint64_t t0, int n, int *flags, int *err, int maxb, cudaStream_t st)
+{
+    if (a.wpt == 2 && (a.g.nw % 2) == 0 && (a.g.W % 64) == 0)
+        return band_launch<MODEL, GM, 2>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
+    return band_launch<MODEL, GM, 1>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
 }
 
 template <int MODEL>
-static cudaError_t persist_model(int gm, const StepArgs &a, uint64_t *b0, uint64_t *b1,
-                                 uint64_t seed, uint64_t t0, int n, PersistSync *sy,
-                                 cudaStream_t st)
+static cudaError_t band_model(int gm, const StepArgs &a, uint64_t *b0, uint64_t *b1,
+                              uint64_t seed, uint64_t t0, int n, int *flags, int *err, int maxb,
+                              cudaStream_t st)
 {
     switch (gm) {
-    case GEOM_NONE: return persist_launch<MODEL, GEOM_NONE>(a, b0, b1, seed, t0, n, sy, st);
-    case GEOM_NOSLIP: return persist_launch<MODEL, GEOM_NOSLIP>(a, b0, b1, seed, t0, n, sy, st);
-    default: return persist_launch<MODEL, GEOM_FULL>(a, b0, b1, seed, t0, n, sy, st);
+    case GEOM_NONE: return band_wpt<MODEL, GEOM_NONE>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
+    case GEOM_NOSLIP: return band_wpt<MODEL, GEOM_NOSLIP>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
+    default: return band_wpt<MODEL, GEOM_FULL>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
     }
 }
 
 cudaError_t launch_persistent(int model, int gm, const StepArgs &a, uint64_t *buf0, uint64_t *buf1,
-                              uint64_t seed, uint64_t t0, int nsteps, PersistSync *sy,
-                              cudaStream_t st)
+                              uint64_t seed, uint64_t t0, int nsteps, int *flags, int *err,
+                              int max_blocks, cudaStream_t st)
 {
-    if ((long long)a.g.H * a.chunks > 0x7fffffffLL) return cudaErrorInvalidValue;
     switch (model) {
-    case M_HPP: return persist_model<M_HPP>(gm, a, buf0, buf1, seed, t0, nsteps, sy, st);
-    case M_FHP_I: return persist_model<M_FHP_I>(gm, a, buf0, buf1, seed, t0, nsteps, sy, st);
-    default: return persist_model<M_FHP_II>(gm, a, buf0, buf1, seed, t0, nsteps, sy, st);
+    case M_HPP: return band_model<M_HPP>(gm, a, buf0, buf1, seed, t0, nsteps, flags, err, max_blocks, st);
+    case M_FHP_I: return band_model<M_FHP_I>(gm, a, buf0, buf1, seed, t0, nsteps, flags, err, max_blocks, st);
+    default: return band_model<M_FHP_II>(gm, a, buf0, buf1, seed, t0, nsteps, flags, err, max_blocks, st);
     }
 }
 

@@ -227,3 +227,21 @@ def test_temporal_blocking_karman_config(gpu, depth, variant):
         assert sha(L.download()) == pins["t100_sha"]
         L.collide_and_propagate(100)
         assert sha(L.download()) == pins["t200_sha"]
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("geom", sorted(GEOMS))
+def test_one_step_kernels_one_and_two_words_per_lane(gpu, oracle, model, geom):
+    """Widths that are multiples of 128 run the two-words-per-lane kernel;
+    forcing columns sit on pair, word and chunk edges."""
+    rng = np.random.default_rng(3 * model + len(geom))
+    for W, H in [(128, 6), (256, 10), (384, 8), (1152, 12), (4096, 4)]:
+        types = GEOMS[geom](W, H)
+        seed = int(rng.integers(1 << 40))
+        st = oracle.init_bernoulli(model, W, H, types, seed=seed, p_move=0.35, p_rest=0.3)
+        for fx in sorted({0, 63, 64, 127, 128 % W, W - 64, W - 1, 4095 % W}):
+            kw = dict(types=types, seed=seed, force_x=fx, force_p=0.7, t0=int(rng.integers(50)))
+            want = oracle.run(model, st, 11, **kw)
+            for variant in (1, 5):
+                got = run_gpu(gpu, model, st, 11, variant=variant, **kw)
+                assert np.array_equal(got, want), (W, H, fx, variant)
