@@ -14,6 +14,7 @@ LIB = os.path.join(PKG, "liblgca_gpu.so")
 SOURCES = ["step.cu", "multistep.cu", "wave.cu", "aux.cu", "bodyforce.cu", "batch.cu",
            "lgca_gpu.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+APPS = {"lgca_headless": "apps/lgca_headless.cpp"}
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 
 
@@ -22,6 +23,10 @@ def nvcc() -> str:
         if cand and os.path.exists(cand):
             return cand
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblgca_gpu.so")
+
+
+def app_path(name: str) -> str:
+    return os.path.join(BUILD, name)
 
 
 def _deps() -> list[str]:
@@ -65,6 +70,17 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(LIB + ".tmp", LIB)
+    # headless application drivers (host C++ over the C ABI)
+    inc = os.path.join(os.path.dirname(PKG), "include")
+    for name, src in APPS.items():
+        out = app_path(name)
+        src = os.path.join(PKG, src)
+        if force or _stale(out, deps + [src, LIB]):
+            cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I", inc, src, "-o", out,
+                   "-L", PKG, "-llgca_gpu", "-Wl,-rpath,$ORIGIN/.."]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"g++ failed on {src}:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
