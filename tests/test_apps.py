@@ -130,7 +130,8 @@ def test_app_loops_conserve_particles(gpu, tmp_path, case, extra):
     summary, r = run_app(gpu, "--case", case, "--out", tmp_path, *extra)
     assert summary["particles_start"] == summary["particles_end"] > 0
     if case in ("pipe", "karman"):
-        p = P.lattice_parameters(3, case, 80.0, 0.3, 10 if case == "pipe" else 20)
+        model = {"FHP_I": 1}.get(extra[extra.index("--model") + 1], 3) if "--model" in extra else 3
+        p = P.lattice_parameters(model, case, 80.0, 0.3, 10 if case == "pipe" else 20)
         assert summary["dims"] == [p["dim_x"], p["dim_y"]]
         assert summary["mean_velocity"][0] > 0.0  # the forcing drives the flow in +x
     if "png" in extra:
