@@ -198,6 +198,40 @@ int lgca_set_stream(lgca_handle h, void *stream);
 int lgca_state_device(lgca_handle h, const uint64_t **planes, size_t *plane_stride,
                       int *row_pitch);
 
+/* Checkpoint / export of a lattice: state, geometry, frozen chirality, step
+ * and body-force counters, seed and settings, into a caller-owned host
+ * buffer of lgca_checkpoint_size bytes (a 96-byte header, then the planes
+ * packed row by row).  lgca_checkpoint_load restores it into a handle of the
+ * same model and dimensions, after which stepping continues bit for bit as
+ * if uninterrupted.  No reference counterpart (the reference only writes
+ * .vti output, src/lgca_io_vti.cpp:113-144). */
+int lgca_checkpoint_size(lgca_handle h, size_t *bytes);
+int lgca_checkpoint_save(lgca_handle h, void *buf, size_t bytes);
+int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes);
+
+/* Batches: many lattices (any sizes, models, geometries) advanced together,
+ * one launch per step and model family over a device work-list of the
+ * members' rows, the steps captured in CUDA graphs.  Members stay owned by
+ * the caller and keep their own state, counters and settings; each member
+ * gives exactly the bits it gives when stepped alone.  No reference
+ * counterpart (the reference steps one lattice per object).
+ *   lgca_batch_step_each: member i (in the order added) advances nsteps[i]
+ *   steps (0 = not at all); members with fewer steps drop out of the
+ *   work-list when done.  Work queued on a member's own stream before the
+ *   call runs first; the member's later calls run after the batch. */
+typedef struct lgca_batch *lgca_batch_handle;
+int lgca_batch_create(lgca_batch_handle *out);
+int lgca_batch_destroy(lgca_batch_handle b);
+int lgca_batch_add(lgca_batch_handle b, lgca_handle lattice);
+int lgca_batch_remove(lgca_batch_handle b, lgca_handle lattice);
+int lgca_batch_size(lgca_batch_handle b, int *n);
+int lgca_batch_step(lgca_batch_handle b, int nsteps);
+int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps);
+int lgca_batch_set_graph_steps(lgca_batch_handle b, int steps_per_graph); /* 0: no graphs */
+int lgca_batch_sync(lgca_batch_handle b);
+const char *lgca_batch_last_error(lgca_batch_handle b);
+void *lgca_batch_stream(lgca_batch_handle b);
+
 /* Bytes of device memory the handle holds. */
 int lgca_device_bytes(lgca_handle h, size_t *bytes);
 

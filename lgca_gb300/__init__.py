@@ -81,6 +81,20 @@ def lib() -> C.CDLL:
             "lgca_state_device": (C.c_int, [vp, C.POINTER(vp), C.POINTER(C.c_size_t),
                                             C.POINTER(C.c_int)]),
             "lgca_device_bytes": (C.c_int, [vp, C.POINTER(C.c_size_t)]),
+            "lgca_checkpoint_size": (C.c_int, [vp, C.POINTER(C.c_size_t)]),
+            "lgca_checkpoint_save": (C.c_int, [vp, vp, C.c_size_t]),
+            "lgca_checkpoint_load": (C.c_int, [vp, vp, C.c_size_t]),
+            "lgca_batch_create": (C.c_int, [C.POINTER(vp)]),
+            "lgca_batch_destroy": (C.c_int, [vp]),
+            "lgca_batch_add": (C.c_int, [vp, vp]),
+            "lgca_batch_remove": (C.c_int, [vp, vp]),
+            "lgca_batch_size": (C.c_int, [vp, C.POINTER(C.c_int)]),
+            "lgca_batch_step": (C.c_int, [vp, C.c_int]),
+            "lgca_batch_step_each": (C.c_int, [vp, vp]),
+            "lgca_batch_set_graph_steps": (C.c_int, [vp, C.c_int]),
+            "lgca_batch_sync": (C.c_int, [vp]),
+            "lgca_batch_last_error": (C.c_char_p, [vp]),
+            "lgca_batch_stream": (vp, [vp]),
             "lgca_apply_body_force_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, C.c_size_t,
                                                         C.c_int, vp, vp, u64, u64, C.c_int,
                                                         C.c_int, vp, vp]),
@@ -252,11 +266,80 @@ class GpuLattice:
         _check(self._h, lib().lgca_device_bytes(self._h, C.byref(n)))
         return n.value
 
+    def checkpoint(self) -> bytes:
+        n = C.c_size_t()
+        _check(self._h, lib().lgca_checkpoint_size(self._h, C.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        _check(self._h, lib().lgca_checkpoint_save(self._h, _ptr(buf), n.value))
+        return buf.tobytes()
+
+    def restore(self, blob: bytes) -> None:
+        buf = np.frombuffer(blob, np.uint8)
+        _check(self._h, lib().lgca_checkpoint_load(self._h, _ptr(buf), buf.size))
+
     def state_device(self):
         p, ps, pitch = C.c_void_p(), C.c_size_t(), C.c_int()
         _check(self._h, lib().lgca_state_device(self._h, C.byref(p), C.byref(ps), C.byref(pitch)))
         return p.value, ps.value, pitch.value
 
 
-__all__ = ["GpuLattice", "LgcaError", "build", "lib", "HPP", "FHP_I", "FHP_II", "FHP_III",
+class GpuBatch:
+    """Many lattices advanced together (lgca_batch_*); members stay owned by
+    the caller."""
+
+    def __init__(self, graph_steps: int | None = None):
+        h = C.c_void_p()
+        st = lib().lgca_batch_create(C.byref(h))
+        if st != 0:
+            raise LgcaError(st, lib().lgca_batch_last_error(None).decode(errors="replace"))
+        self._b = h
+        self.members: list[GpuLattice] = []
+        if graph_steps is not None:
+            self._chk(lib().lgca_batch_set_graph_steps(self._b, int(graph_steps)))
+
+    def _chk(self, st: int) -> None:
+        if st != 0:
+            raise LgcaError(st, lib().lgca_batch_last_error(self._b).decode(errors="replace"))
+
+    def add(self, lattice: "GpuLattice") -> None:
+        self._chk(lib().lgca_batch_add(self._b, lattice.handle))
+        self.members.append(lattice)
+
+    def remove(self, lattice: "GpuLattice") -> None:
+        self._chk(lib().lgca_batch_remove(self._b, lattice.handle))
+        self.members.remove(lattice)
+
+    def step(self, nsteps: int) -> None:
+        self._chk(lib().lgca_batch_step(self._b, int(nsteps)))
+
+    def step_each(self, nsteps) -> None:
+        arr = np.ascontiguousarray(nsteps, dtype=np.int32)
+        assert arr.size == len(self.members)
+        self._chk(lib().lgca_batch_step_each(self._b, _ptr(arr)))
+
+    def sync(self) -> None:
+        self._chk(lib().lgca_batch_sync(self._b))
+
+    def stream_ptr(self) -> int:
+        return lib().lgca_batch_stream(self._b) or 0
+
+    def close(self) -> None:
+        if getattr(self, "_b", None):
+            lib().lgca_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+__all__ = ["GpuBatch", "GpuLattice", "LgcaError", "build", "lib", "HPP", "FHP_I", "FHP_II", "FHP_III",
            "FLUID", "SOLID_NO_SLIP", "SOLID_SLIP", "NUM_DIR"]

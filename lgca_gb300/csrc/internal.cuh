@@ -45,6 +45,22 @@ struct StepArgs {
     int wpt;            // words per lane of the one-step kernel (1 or 2)
 };
 
+// One lattice of a batch (batch.cu): its step arguments (src/dst unused),
+// its two buffers (buf0 holds the state at the start of the batch call), the
+// keys' seed and first global step, the steps it advances in the call and
+// its place in the work-list.
+struct BatchEntry {
+    StepArgs a;
+    uint64_t *buf0, *buf1;
+    uint64_t seed, t0;
+    int nsteps;
+    int per_row;  // warp tasks per row
+    int gm, wpt;  // geometry mode, words per lane
+};
+cudaError_t launch_batch(int model_family, const BatchEntry *E, const int *prefix, int n_active,
+                         int total_tasks, int s_local, const int *s_base, cudaStream_t stream);
+cudaError_t launch_advance(int *s_base, int by, cudaStream_t stream);
+
 // One lattice step of `a` (k = 1), launched on `stream`.
 cudaError_t launch_step(int model, int geom_mode, const StepArgs &a, cudaStream_t stream);
 

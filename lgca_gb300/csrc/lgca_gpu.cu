@@ -13,6 +13,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 using namespace lgca_gpu;
 
@@ -610,11 +611,437 @@ int lgca_state_device(lgca_handle h, const uint64_t **planes, size_t *plane_stri
     return LGCA_OK;
 }
 
+// ---- checkpoint: header + packed planes (rows of nw words, no padding)
+namespace {
+struct CkptHeader {
+    char magic[8];  // "LGCAGB01"
+    int32_t model, dim_x, dim_y, flags;  // flags: 1 noslip, 2 slip, 4 frozen chirality
+    uint64_t seed, step, fcall;
+    int32_t force_x, depth;
+    uint64_t force_thr;
+    int32_t variant, wpt;
+    uint64_t reserved[3];
+};
+static_assert(sizeof(CkptHeader) == 96, "checkpoint header layout");
+
+size_t ckpt_planes(const lgca_lattice *h)
+{
+    return (size_t)h->D + (h->solid ? 2 : 0) + (h->frozen ? 1 : 0);
+}
+}  // namespace
+
+int lgca_checkpoint_size(lgca_handle h, size_t *bytes)
+{
+    CHECK_HANDLE(h);
+    if (!bytes) return fail(h, LGCA_ERR_INVALID, "bytes is NULL");
+    const size_t plane = (size_t)h->g.H * h->g.nw * sizeof(uint64_t);
+    *bytes = sizeof(CkptHeader) + ckpt_planes(h) * plane;
+    return LGCA_OK;
+}
+
+int lgca_checkpoint_save(lgca_handle h, void *buf, size_t bytes)
+{
+    CHECK_HANDLE(h);
+    size_t need = 0;
+    lgca_checkpoint_size(h, &need);
+    if (!buf || bytes < need) return fail(h, LGCA_ERR_INVALID, "checkpoint buffer of %zu bytes < %zu", bytes, need);
+    DeviceGuard dg(h->device);
+    CkptHeader hd;
+    memset(&hd, 0, sizeof(hd));
+    memcpy(hd.magic, "LGCAGB01", 8);
+    hd.model = h->model;
+    hd.dim_x = h->g.W;
+    hd.dim_y = h->g.H;
+    hd.flags = (h->solid && h->has_noslip ? 1 : 0) | (h->solid && h->has_slip ? 2 : 0) |
+               (h->frozen ? 4 : 0) | (h->solid ? 8 : 0);
+    hd.seed = h->seed;
+    hd.step = h->t;
+    hd.fcall = h->fcall;
+    hd.force_x = h->force_x;
+    hd.force_thr = h->force_thr;
+    hd.depth = h->depth;
+    hd.variant = h->variant;
+    hd.wpt = h->wpt;
+    memcpy(buf, &hd, sizeof(hd));
+    char *out = static_cast<char *>(buf) + sizeof(hd);
+    const size_t row = (size_t)h->g.nw * sizeof(uint64_t), pitch = (size_t)h->g.pitch * sizeof(uint64_t);
+    const size_t plane = row * h->g.H;
+    auto copy_plane = [&](const uint64_t *src) -> cudaError_t {
+        cudaError_t e = cudaMemcpy2DAsync(out, row, src, pitch, row, h->g.H, cudaMemcpyDeviceToHost,
+                                          h->stream);
+        out += plane;
+        return e;
+    };
+    for (int d = 0; d < h->D; ++d) CK(h, copy_plane(h->buf[h->cur] + (size_t)d * h->g.ps));
+    if (h->solid) {
+        CK(h, copy_plane(h->solid));
+        CK(h, copy_plane(h->slip));
+    }
+    if (h->frozen) CK(h, copy_plane(h->chir));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LGCA_OK;
+}
+
+int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes)
+{
+    CHECK_HANDLE(h);
+    if (!buf || bytes < sizeof(CkptHeader)) return fail(h, LGCA_ERR_INVALID, "checkpoint too short");
+    CkptHeader hd;
+    memcpy(&hd, buf, sizeof(hd));
+    if (memcmp(hd.magic, "LGCAGB01", 8) != 0) return fail(h, LGCA_ERR_INVALID, "not a checkpoint of this engine");
+    if (hd.model != h->model || hd.dim_x != h->g.W || hd.dim_y != h->g.H)
+        return fail(h, LGCA_ERR_INVALID, "checkpoint of model %d, %d x %d does not match the lattice",
+                    hd.model, hd.dim_x, hd.dim_y);
+    const bool has_geom = (hd.flags & 8) != 0, frozen = (hd.flags & 4) != 0;
+    const size_t row = (size_t)h->g.nw * sizeof(uint64_t), pitch = (size_t)h->g.pitch * sizeof(uint64_t);
+    const size_t plane = row * h->g.H;
+    const size_t need = sizeof(CkptHeader) + ((size_t)h->D + (has_geom ? 2 : 0) + (frozen ? 1 : 0)) * plane;
+    if (bytes < need) return fail(h, LGCA_ERR_INVALID, "checkpoint of %zu bytes < %zu", bytes, need);
+    DeviceGuard dg(h->device);
+    const size_t plane_bytes = h->g.ps * sizeof(uint64_t);
+    if (has_geom && !h->solid) {
+        CK(h, cudaMalloc(&h->solid, plane_bytes));
+        CK(h, cudaMalloc(&h->slip, plane_bytes));
+        CK(h, cudaMemsetAsync(h->solid, 0, plane_bytes, h->stream));
+        CK(h, cudaMemsetAsync(h->slip, 0, plane_bytes, h->stream));
+        h->bytes += 2 * plane_bytes;
+    }
+    if (frozen && !h->chir) {
+        CK(h, cudaMalloc(&h->chir, plane_bytes));
+        CK(h, cudaMemsetAsync(h->chir, 0, plane_bytes, h->stream));
+        h->bytes += plane_bytes;
+    }
+    const char *in = static_cast<const char *>(buf) + sizeof(CkptHeader);
+    auto copy_plane = [&](uint64_t *dst) -> cudaError_t {
+        cudaError_t e = cudaMemcpy2DAsync(dst, pitch, in, row, row, h->g.H, cudaMemcpyHostToDevice,
+                                          h->stream);
+        in += plane;
+        return e;
+    };
+    for (int d = 0; d < h->D; ++d) CK(h, copy_plane(h->buf[h->cur] + (size_t)d * h->g.ps));
+    if (has_geom) {
+        CK(h, copy_plane(h->solid));
+        CK(h, copy_plane(h->slip));
+    }
+    if (frozen) CK(h, copy_plane(h->chir));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->has_noslip = has_geom && (hd.flags & 1);
+    h->has_slip = has_geom && (hd.flags & 2);
+    h->frozen = frozen;
+    h->seed = hd.seed;
+    h->t = hd.step;
+    h->fcall = hd.fcall;
+    h->force_x = hd.force_x;
+    h->force_thr = hd.force_thr;
+    h->depth = hd.depth;
+    h->variant = hd.variant;
+    h->wpt = hd.wpt;
+    return LGCA_OK;
+}
+
 int lgca_device_bytes(lgca_handle h, size_t *bytes)
 {
     CHECK_HANDLE(h);
     if (bytes) *bytes = h->bytes;
     return LGCA_OK;
 }
+
+
+// ------------------------------------------------------------------ batches
+}  // extern "C"
+
+struct lgca_batch {
+    std::vector<lgca_lattice *> members;
+    std::vector<cudaEvent_t> ev;  // one per member: its stream's work before the batch
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    int *s_base = nullptr;       // device: first batch-local step of a graph replay
+    int graph_steps = 32;        // steps captured per CUDA graph (0: no graphs)
+    struct Family {
+        BatchEntry *dE = nullptr;
+        int *dP = nullptr;
+        size_t cap = 0;
+        std::vector<BatchEntry> E;
+        std::vector<int> P;
+        std::vector<int> nsteps;  // per entry, descending
+    } fam[3];
+    std::string err;
+};
+
+namespace {
+
+int bfail(lgca_batch *b, int status, const char *msg)
+{
+    g_err = msg;
+    if (b) b->err = msg;
+    return status;
+}
+
+int bcuda(lgca_batch *b, cudaError_t e, const char *what)
+{
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    return bfail(b, e == cudaErrorMemoryAllocation ? LGCA_ERR_NOMEM : LGCA_ERR_CUDA, buf);
+}
+
+#define BCK(b, expr)                                                \
+    do {                                                            \
+        cudaError_t e_ = (expr);                                    \
+        if (e_ != cudaSuccess) return bcuda((b), e_, #expr);        \
+    } while (0)
+
+int family_of(int model) { return model == LGCA_HPP ? 0 : (model == LGCA_FHP_I ? 1 : 2); }
+int family_model(int f) { return f == 0 ? M_HPP : (f == 1 ? M_FHP_I : M_FHP_II); }
+
+// Launches of batch-local steps [s0, s0 + n) of one segment (fixed active
+// sets), steps numbered from *s_base + s_local.
+int enqueue_steps(lgca_batch *b, const int *n_active, const int *tasks, int n)
+{
+    for (int s = 0; s < n; ++s)
+        for (int f = 0; f < 3; ++f)
+            if (n_active[f] > 0)
+                BCK(b, launch_batch(family_model(f), b->fam[f].dE, b->fam[f].dP, n_active[f],
+                                    tasks[f], s, b->s_base, b->stream));
+    BCK(b, launch_advance(b->s_base, n, b->stream));
+    return LGCA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lgca_batch_create(lgca_batch_handle *out)
+{
+    if (!out) return bfail(nullptr, LGCA_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    lgca_batch *b = new (std::nothrow) lgca_batch();
+    if (!b) return bfail(nullptr, LGCA_ERR_NOMEM, "host allocation failed");
+    cudaGetDevice(&b->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&b->s_base, sizeof(int));
+    if (e != cudaSuccess) {
+        int st = bcuda(nullptr, e, "lgca_batch_create");
+        lgca_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return LGCA_OK;
+}
+
+int lgca_batch_destroy(lgca_batch_handle b)
+{
+    if (!b) return LGCA_OK;
+    DeviceGuard dg(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
+    for (auto &f : b->fam) {
+        cudaFree(f.dE);
+        cudaFree(f.dP);
+    }
+    cudaFree(b->s_base);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return LGCA_OK;
+}
+
+int lgca_batch_add(lgca_batch_handle b, lgca_handle h)
+{
+    if (!b) return bfail(nullptr, LGCA_ERR_INVALID, "invalid batch");
+    if (!valid(h)) return bfail(b, LGCA_ERR_INVALID, "invalid lattice handle");
+    if (h->device != b->device) return bfail(b, LGCA_ERR_INVALID, "lattice on another device");
+    for (lgca_lattice *m : b->members)
+        if (m == h) return bfail(b, LGCA_ERR_INVALID, "lattice already in the batch");
+    DeviceGuard dg(b->device);
+    cudaEvent_t e;
+    BCK(b, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    b->members.push_back(h);
+    b->ev.push_back(e);
+    return LGCA_OK;
+}
+
+int lgca_batch_remove(lgca_batch_handle b, lgca_handle h)
+{
+    if (!b) return bfail(nullptr, LGCA_ERR_INVALID, "invalid batch");
+    DeviceGuard dg(b->device);
+    for (size_t i = 0; i < b->members.size(); ++i) {
+        if (b->members[i] == h) {
+            BCK(b, cudaStreamSynchronize(b->stream));
+            cudaEventDestroy(b->ev[i]);
+            b->members.erase(b->members.begin() + i);
+            b->ev.erase(b->ev.begin() + i);
+            return LGCA_OK;
+        }
+    }
+    return bfail(b, LGCA_ERR_INVALID, "lattice not in the batch");
+}
+
+int lgca_batch_size(lgca_batch_handle b, int *n)
+{
+    if (!b || !n) return bfail(b, LGCA_ERR_INVALID, "invalid argument");
+    *n = (int)b->members.size();
+    return LGCA_OK;
+}
+
+int lgca_batch_set_graph_steps(lgca_batch_handle b, int n)
+{
+    if (!b || n < 0) return bfail(b, LGCA_ERR_INVALID, "invalid argument");
+    b->graph_steps = n;
+    return LGCA_OK;
+}
+
+int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
+{
+    if (!b) return bfail(nullptr, LGCA_ERR_INVALID, "invalid batch");
+    if (!nsteps && !b->members.empty()) return bfail(b, LGCA_ERR_INVALID, "nsteps is NULL");
+    DeviceGuard dg(b->device);
+    const size_t nm = b->members.size();
+    for (size_t i = 0; i < nm; ++i)
+        if (nsteps[i] < 0) return bfail(b, LGCA_ERR_INVALID, "negative step count");
+    // the previous batch call's kernels still read the work-lists
+    BCK(b, cudaStreamSynchronize(b->stream));
+    // order after each member's own pending work
+    for (size_t i = 0; i < nm; ++i) {
+        if (nsteps[i] == 0) continue;
+        BCK(b, cudaEventRecord(b->ev[i], b->members[i]->stream));
+        BCK(b, cudaStreamWaitEvent(b->stream, b->ev[i], 0));
+    }
+    // work-lists per model family, lattices sorted by steps (descending)
+    std::vector<int> order(nm);
+    for (size_t i = 0; i < nm; ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return nsteps[x] > nsteps[y]; });
+    int max_steps = 0;
+    for (auto &f : b->fam) {
+        f.E.clear();
+        f.P.assign(1, 0);
+        f.nsteps.clear();
+    }
+    for (int i : order) {
+        if (nsteps[i] == 0) continue;
+        lgca_lattice *h = b->members[i];
+        auto &f = b->fam[family_of(h->model)];
+        BatchEntry e;
+        memset(&e, 0, sizeof(e));
+        e.a.solid = h->solid;
+        e.a.slip = h->slip;
+        e.a.chir = h->frozen ? h->chir : nullptr;
+        e.a.g = h->g;
+        e.a.chunks = (h->g.nw + 31) / 32;
+        e.a.force_thr = h->force_thr;
+        e.a.fx = h->force_x;
+        const bool pair = h->variant != VARIANT_PLAIN && h->wpt == 2 && (h->g.nw % 2) == 0 &&
+                          (h->g.W % 64) == 0;
+        e.a.wpt = pair ? 2 : 1;
+        e.wpt = e.a.wpt;
+        e.gm = geom_mode(h);
+        e.per_row = pair ? (h->g.nw / 2 + 31) / 32 : (h->g.nw + 31) / 32;
+        e.buf0 = h->buf[h->cur];
+        e.buf1 = h->buf[h->cur ^ 1];
+        e.seed = h->seed;
+        e.t0 = h->t;
+        e.nsteps = nsteps[i];
+        const long long tasks = (long long)f.P.back() + (long long)h->g.H * e.per_row;
+        if (tasks > 0x7fffffffLL) return bfail(b, LGCA_ERR_INVALID, "batch work-list too long");
+        f.E.push_back(e);
+        f.P.push_back((int)tasks);
+        f.nsteps.push_back(nsteps[i]);
+        max_steps = std::max(max_steps, nsteps[i]);
+    }
+    for (auto &f : b->fam) {
+        if (f.E.empty()) continue;
+        if (f.cap < f.E.size()) {
+            cudaFree(f.dE);
+            cudaFree(f.dP);
+            f.dE = nullptr;
+            f.dP = nullptr;
+            f.cap = 0;
+            BCK(b, cudaMalloc(&f.dE, f.E.size() * sizeof(BatchEntry)));
+            BCK(b, cudaMalloc(&f.dP, (f.E.size() + 1) * sizeof(int)));
+            f.cap = f.E.size();
+        }
+        // synchronous copies: the host vectors are reused by the next call
+        BCK(b, cudaMemcpy(f.dE, f.E.data(), f.E.size() * sizeof(BatchEntry), cudaMemcpyHostToDevice));
+        BCK(b, cudaMemcpy(f.dP, f.P.data(), f.P.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    // segments of constant active sets: [s0, s1) where no lattice finishes
+    int s0 = 0;
+    while (s0 < max_steps) {
+        int s1 = max_steps, n_active[3] = {0, 0, 0}, tasks[3] = {0, 0, 0};
+        for (int f = 0; f < 3; ++f) {
+            const auto &F = b->fam[f];
+            int k = 0;
+            while (k < (int)F.nsteps.size() && F.nsteps[k] > s0) ++k;
+            n_active[f] = k;
+            tasks[f] = F.P[k];
+            for (int j = 0; j < k; ++j) s1 = std::min(s1, F.nsteps[j]);
+        }
+        const int len = s1 - s0;
+        BCK(b, cudaMemcpyAsync(b->s_base, &s0, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+        // the copy reads s0 from the host stack: wait for it before s0 changes
+        BCK(b, cudaStreamSynchronize(b->stream));
+        const int G = b->graph_steps > 0 ? std::min(b->graph_steps, len) : 0;
+        int done = 0;
+        if (G > 1 && len >= 2 * G) {
+            cudaGraph_t graph = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            const int st = enqueue_steps(b, n_active, tasks, G);
+            cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+            if (st != LGCA_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                return st;
+            }
+            BCK(b, e);
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            BCK(b, e);
+            for (; done + G <= len; done += G) {
+                e = cudaGraphLaunch(exec, b->stream);
+                if (e != cudaSuccess) {
+                    cudaGraphExecDestroy(exec);
+                    return bcuda(b, e, "cudaGraphLaunch");
+                }
+            }
+            BCK(b, cudaStreamSynchronize(b->stream));
+            cudaGraphExecDestroy(exec);
+        }
+        if (done < len) {
+            const int st = enqueue_steps(b, n_active, tasks, len - done);
+            if (st != LGCA_OK) return st;
+        }
+        s0 = s1;
+    }
+    // members continue after the batch
+    BCK(b, cudaEventRecord(b->done, b->stream));
+    for (size_t i = 0; i < nm; ++i) {
+        if (nsteps[i] == 0) continue;
+        lgca_lattice *h = b->members[i];
+        BCK(b, cudaStreamWaitEvent(h->stream, b->done, 0));
+        if (nsteps[i] & 1) h->cur ^= 1;
+        h->t += (uint64_t)nsteps[i];
+    }
+    return LGCA_OK;
+}
+
+int lgca_batch_step(lgca_batch_handle b, int nsteps)
+{
+    if (!b) return bfail(nullptr, LGCA_ERR_INVALID, "invalid batch");
+    std::vector<int> n(b->members.size(), nsteps);
+    return lgca_batch_step_each(b, n.data());
+}
+
+int lgca_batch_sync(lgca_batch_handle b)
+{
+    if (!b) return bfail(nullptr, LGCA_ERR_INVALID, "invalid batch");
+    DeviceGuard dg(b->device);
+    BCK(b, cudaStreamSynchronize(b->stream));
+    return LGCA_OK;
+}
+
+const char *lgca_batch_last_error(lgca_batch_handle b) { return b ? b->err.c_str() : g_err.c_str(); }
+
+void *lgca_batch_stream(lgca_batch_handle b) { return b ? (void *)b->stream : nullptr; }
 
 }  // extern "C"

@@ -1,380 +1,9 @@
-// Plain lattice step (one step per pass over global memory).
-//
-// Reference: OMP_Lattice<M>::collide_and_propagate, keva92/lgca
-// src/omp_lattice.cpp:100-249.  The reference pulls, for every cell and
-// channel d, the bit of channel d of the cell at offset_to_neighbor[INV_DIR[d]]
-// plus the periodic edge corrections (src/lgca_models.h:79-132 HPP,
-// :292-365 / :483-566 / :701-784 FHP).  With an even number of rows those
-// tables describe a torus; the source cell of channel d of site (x, y) is
-//
-//   d   FHP, y even   FHP, y odd    HPP
-//   0   (x-1, y)      (x-1, y)      (x-1, y)
-//   1   (x-1, y-1)    (x,   y-1)    (x,   y-1)
-//   2   (x,   y-1)    (x+1, y-1)    (x+1, y)
-//   3   (x+1, y)      (x+1, y)      (x,   y+1)
-//   4   (x,   y+1)    (x+1, y+1)
-//   5   (x-1, y+1)    (x,   y+1)
-//   6   (x,   y)      (x,   y)
-//
-// all coordinates modulo (W, H).  On bit-planes every channel is read from a
-// single row, and an x offset of +-1 is a one-bit shift of the word with the
-// missing bit taken from the neighbouring word (a warp shuffle, or a load at
-// a warp edge / the periodic x seam).
-//
-// Mapping: one warp per (row, chunk of 32 words), one word (64 sites) per
-// lane.  Each lane loads D words and stores D words; the only other traffic
-// is one word per shifted plane at the two warp edges.
-#include "internal.cuh"
-#include "../../include/lgca/rng.h"
+// One-step kernels (one word or two words per lane), the persistent band
+// kernel and their launchers.  The per-word step itself (pull table,
+// forcing, collision, boundaries) is in step_body.cuh.
+#include "step_body.cuh"
 
 namespace lgca_gpu {
-
-static constexpr unsigned FULL = 0xffffffffu;
-
-// Forcing decision at site (fx, y): a FLUID cell with channel 0 empty and the
-// west-moving channel (3 for FHP, 2 for HPP) occupied reverses with
-// probability thr / 2^32.  Used by the lanes that fetch the forced word from
-// another chunk.
-// What changes from one step to the next: the two buffers and the keys.
-struct StepIO {
-    const uint64_t *__restrict__ src;
-    uint64_t *__restrict__ dst;
-    uint64_t ckey, fkey;  // chirality / forcing keys of the step
-};
-
-// State loads: the one-step kernels read buffers that no thread writes
-// during the launch (read-only path); the persistent band kernel reads
-// buffers that other blocks wrote earlier in the same launch, so it must
-// bypass the non-coherent L1 (ld.global.cg, cached in L2 only).
-template <bool CG> __device__ __forceinline__ uint64_t ld_state(const uint64_t *p)
-{
-    return CG ? __ldcg(p) : __ldg(p);
-}
-template <bool CG> __device__ __forceinline__ ulonglong2 ld_state2(const uint64_t *p)
-{
-    return CG ? __ldcg(reinterpret_cast<const ulonglong2 *>(p))
-              : __ldg(reinterpret_cast<const ulonglong2 *>(p));
-}
-
-template <int MODEL, int GM, bool CG = false>
-__device__ __forceinline__ uint64_t force_flip_at(const StepArgs &a, const StepIO &io, int y)
-{
-    constexpr int WEST = (MODEL == M_HPP) ? 2 : 3;
-    const int fw = a.fx >> 6, fb = a.fx & 63;
-    const unsigned r0 = (unsigned)y * a.g.pitch + fw;
-    uint64_t n0 = ld_state<CG>(io.src + r0), nw = ld_state<CG>(io.src + (WEST * (unsigned)a.g.ps + r0));
-    uint64_t fluid = ~0ull;
-    if (GM >= GEOM_NOSLIP) fluid &= ~a.solid[r0];
-    if (GM == GEOM_FULL) fluid &= ~a.slip[r0];
-    const uint64_t u = lgca_rng_draw(io.fkey, lgca_rng_index((uint32_t)y, (uint32_t)a.fx)) >> 32;
-    const uint64_t cand = (~n0 & nw & fluid) >> fb & 1ull;
-    return (u < a.force_thr) ? cand : 0ull;
-}
-
-template <int MODEL, int GM, bool CG = false>
-__device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, const int y,
-                                          const int w, const int lane)
-{
-    constexpr int D = ModelTraits<MODEL>::D;
-    const PlaneGeom &g = a.g;
-    const bool active = w < g.nw;
-    const int ym = (y == 0) ? g.H - 1 : y - 1;
-    const int yp = (y == g.H - 1) ? 0 : y + 1;
-    // 32-bit offsets: a lattice has at most 2^31 sites, so D * H * pitch < 2^29 words
-    const unsigned rowm = (unsigned)ym * g.pitch, row0 = (unsigned)y * g.pitch,
-                   rowp = (unsigned)yp * g.pitch;
-    const uint64_t *__restrict__ s = io.src;
-    const unsigned ps = (unsigned)g.ps;
-    const bool even = (y & 1) == 0;
-
-    // which plane comes from which row (see the table above)
-    // HPP: 0 -> row y, 1 -> row y-1, 2 -> row y, 3 -> row y+1
-    // FHP: 0,3,6 -> row y, 1,2 -> row y-1, 4,5 -> row y+1
-    auto row_of = [&](int d) -> unsigned {
-        if (MODEL == M_HPP) return d == 1 ? rowm : (d == 3 ? rowp : row0);
-        return (d == 1 || d == 2) ? rowm : ((d == 4 || d == 5) ? rowp : row0);
-    };
-
-    uint64_t n[7];
-#pragma unroll
-    for (int d = 0; d < D; ++d) n[d] = active ? ld_state<CG>(s + (d * ps + row_of(d) + w)) : 0ull;
-
-    uint64_t solid = 0, slip = 0;
-    if (GM >= GEOM_NOSLIP && active) solid = __ldg(a.solid + row0 + w);
-    if (GM == GEOM_FULL && active) slip = __ldg(a.slip + row0 + w);
-
-    // forcing column: applied to the source words before the pull
-    constexpr int WEST = (MODEL == M_HPP) ? 2 : 3;
-    const bool forcing = a.force_thr != 0;
-    if (forcing && active && w == (a.fx >> 6)) {
-        const int fb = a.fx & 63;
-        const uint64_t u =
-            lgca_rng_draw(io.fkey, lgca_rng_index((uint32_t)y, (uint32_t)a.fx)) >> 32;
-        const uint64_t fl = (u < a.force_thr) ? ((~n[0] & n[WEST] & ~solid & ~slip) >> fb & 1ull) : 0ull;
-        n[0] |= fl << fb;
-        n[WEST] &= ~(fl << fb);
-    }
-
-    // neighbour words at the warp edges and the periodic x seam
-    const bool need_w = active && (lane == 0 || w == 0);
-    const bool need_e = active && (lane == 31 || w == g.nw - 1);
-    const int widx = (w == 0) ? g.nw - 1 : w - 1;
-    const int wbit = (w == 0) ? g.L : 63;
-    const int eidx = (w == g.nw - 1) ? 0 : w + 1;
-    const int epos = (w == g.nw - 1) ? g.L : 63;
-    const int wx = (w == 0) ? g.W - 1 : 64 * w - 1;  // site of the fetched west bit
-    const int ex = (w == g.nw - 1) ? 0 : 64 * w + 64; // site of the fetched east bit
-
-    // x-1 pull: (v << 1) | bit of site x-1
-    auto shl = [&](uint64_t v, int d, unsigned row) -> uint64_t {
-        const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v >> 32), 1);
-        uint64_t in = hi >> 31;
-        if (need_w) {
-            in = (ld_state<CG>(s + (d * ps + row + widx)) >> wbit) & 1ull;
-            if (d == 0 && row == row0 && forcing && wx == a.fx)
-                in |= force_flip_at<MODEL, GM, CG>(a, io, y);
-        }
-        return (v << 1) | in;
-    };
-    // x+1 pull: (v >> 1) | bit of site x+1 placed at the last valid bit
-    auto shr = [&](uint64_t v, int d, unsigned row) -> uint64_t {
-        const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v, 1);
-        uint64_t in = lo & 1u;
-        if (need_e) {
-            in = ld_state<CG>(s + (d * ps + row + eidx)) & 1ull;
-            if (d == WEST && row == row0 && forcing && ex == a.fx)
-                in &= ~force_flip_at<MODEL, GM, CG>(a, io, y);
-        }
-        return (v >> 1) | (in << epos);
-    };
-
-    uint64_t p[7];
-    if (MODEL == M_HPP) {
-        p[0] = shl(n[0], 0, row0);
-        p[1] = n[1];
-        p[2] = shr(n[2], 2, row0);
-        p[3] = n[3];
-    } else {
-        p[0] = shl(n[0], 0, row0);
-        p[3] = shr(n[3], 3, row0);
-        if (even) {
-            p[1] = shl(n[1], 1, rowm);
-            p[5] = shl(n[5], 5, rowp);
-            p[2] = n[2];
-            p[4] = n[4];
-        } else {
-            p[2] = shr(n[2], 2, rowm);
-            p[4] = shr(n[4], 4, rowp);
-            p[1] = n[1];
-            p[5] = n[5];
-        }
-        if (D == 7) p[6] = n[6];
-    }
-    if (!active) return;
-
-    uint64_t c[7];
-#pragma unroll
-    for (int d = 0; d < D; ++d) c[d] = p[d];
-    if (MODEL != M_HPP) {
-        const uint64_t chir =
-            a.chir ? __ldg(a.chir + row0 + w)
-                   : lgca_rng_draw(io.ckey, lgca_rng_index((uint32_t)y, (uint32_t)w));
-        collide<MODEL>(c, chir);
-    } else {
-        collide<MODEL>(c, 0ull);
-    }
-
-    uint64_t out[7];
-    if (GM == GEOM_NONE) {
-#pragma unroll
-        for (int d = 0; d < D; ++d) out[d] = c[d];
-    } else {
-        const uint64_t fluid = ~(solid | slip);
-        // slip cells: mirror in x on the first/last row, in y on the first/last
-        // column (the latter wins at corners), unchanged elsewhere
-        const bool nsrow = (y == 0) || (y == g.H - 1);
-        const uint64_t ew = (w == 0 ? 1ull : 0ull) | (w == g.nw - 1 ? (1ull << g.L) : 0ull);
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-            uint64_t o = (fluid & c[d]) | (solid & p[Dirs<MODEL>::inv(d)]);
-            if (GM == GEOM_FULL) {
-                const uint64_t sx = nsrow ? p[Dirs<MODEL>::mirx(d)] : p[d];
-                const uint64_t sl = (ew & p[Dirs<MODEL>::miry(d)]) | (~ew & sx);
-                o |= slip & sl;
-            }
-            out[d] = o;
-        }
-    }
-    if (w == g.nw - 1) {  // clear the tail bits past site W-1
-#pragma unroll
-        for (int d = 0; d < D; ++d) out[d] &= g.lastmask;
-    }
-    uint64_t *__restrict__ dp = io.dst + row0 + w;
-#pragma unroll
-    for (int d = 0; d < D; ++d) dp[d * ps] = out[d];
-}
-
-// Two words per lane (lattices with an even number of words per row, i.e.
-// W a multiple of 128): 16-byte loads and stores, one shuffle per shifted
-// plane for 128 sites, and half as many warps, so that an L2-resident lattice
-// fits in one wave of resident warps.  Same arithmetic as step_word.
-template <int MODEL, int GM, bool CG = false>
-__device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, const int y,
-                                          const int t, const int lane)
-{
-    constexpr int D = ModelTraits<MODEL>::D;
-    const PlaneGeom &g = a.g;
-    const int np = g.nw >> 1;
-    const bool active = t < np;
-    const int ym = (y == 0) ? g.H - 1 : y - 1;
-    const int yp = (y == g.H - 1) ? 0 : y + 1;
-    const unsigned rowm = (unsigned)ym * g.pitch, row0 = (unsigned)y * g.pitch,
-                   rowp = (unsigned)yp * g.pitch;
-    const uint64_t *__restrict__ s = io.src;
-    const unsigned ps = (unsigned)g.ps;
-    const bool even = (y & 1) == 0;
-    const int w0 = 2 * t;
-    auto row_of = [&](int d) -> unsigned {
-        if (MODEL == M_HPP) return d == 1 ? rowm : (d == 3 ? rowp : row0);
-        return (d == 1 || d == 2) ? rowm : ((d == 4 || d == 5) ? rowp : row0);
-    };
-    auto ld2 = [&](const uint64_t *base, unsigned off) -> ulonglong2 {  // state
-        return active ? ld_state2<CG>(base + off) : make_ulonglong2(0ull, 0ull);
-    };
-    auto ldg2 = [&](const uint64_t *base, unsigned off) -> ulonglong2 {  // read-only planes
-        return active ? __ldg(reinterpret_cast<const ulonglong2 *>(base + off))
-                      : make_ulonglong2(0ull, 0ull);
-    };
-
-    uint64_t n[2][7];
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-        const ulonglong2 v = ld2(s, d * ps + row_of(d) + w0);
-        n[0][d] = v.x;
-        n[1][d] = v.y;
-    }
-    uint64_t solid[2] = {0, 0}, slip[2] = {0, 0};
-    if (GM >= GEOM_NOSLIP) {
-        const ulonglong2 v = ldg2(a.solid, row0 + w0);
-        solid[0] = v.x;
-        solid[1] = v.y;
-    }
-    if (GM == GEOM_FULL) {
-        const ulonglong2 v = ldg2(a.slip, row0 + w0);
-        slip[0] = v.x;
-        slip[1] = v.y;
-    }
-
-    constexpr int WEST = (MODEL == M_HPP) ? 2 : 3;
-    const bool forcing = a.force_thr != 0;
-    const int fw = a.fx >> 6;
-    if (forcing && active && (fw >> 1) == t) {
-        const uint64_t u =
-            lgca_rng_draw(io.fkey, lgca_rng_index((uint32_t)y, (uint32_t)a.fx)) >> 32;
-        const uint64_t bit = (u < a.force_thr) ? (1ull << (a.fx & 63)) : 0ull;
-        // masks per word of the pair (no run-time index into n, which would
-        // move the arrays to local memory)
-        const uint64_t m0 = (fw & 1) ? 0ull : bit, m1 = (fw & 1) ? bit : 0ull;
-        const uint64_t f0 = ~n[0][0] & n[0][WEST] & ~solid[0] & ~slip[0] & m0;
-        const uint64_t f1 = ~n[1][0] & n[1][WEST] & ~solid[1] & ~slip[1] & m1;
-        n[0][0] |= f0;
-        n[0][WEST] &= ~f0;
-        n[1][0] |= f1;
-        n[1][WEST] &= ~f1;
-    }
-
-    const bool need_w = active && (lane == 0 || t == 0);
-    const bool need_e = active && (lane == 31 || t == np - 1);
-    const int widx = (t == 0) ? g.nw - 1 : w0 - 1;
-    const int eidx = (t == np - 1) ? 0 : w0 + 2;
-    const int wx = (t == 0) ? g.W - 1 : 64 * w0 - 1;
-    const int ex = (t == np - 1) ? 0 : 64 * w0 + 128;
-
-    // x-1 pull of the pair (v0, v1)
-    auto shl = [&](uint64_t v0, uint64_t v1, int d, unsigned row, int k) -> uint64_t {
-        const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v1 >> 32), 1);
-        uint64_t in = hi >> 31;
-        if (need_w) {
-            in = ld_state<CG>(s + (d * ps + row + widx)) >> 63;
-            if (d == 0 && row == row0 && forcing && wx == a.fx)
-                in |= force_flip_at<MODEL, GM, CG>(a, io, y);
-        }
-        return k ? ((v1 << 1) | (v0 >> 63)) : ((v0 << 1) | in);
-    };
-    // x+1 pull of the pair
-    auto shr = [&](uint64_t v0, uint64_t v1, int d, unsigned row, int k) -> uint64_t {
-        const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v0, 1);
-        uint64_t in = lo & 1u;
-        if (need_e) {
-            in = ld_state<CG>(s + (d * ps + row + eidx)) & 1ull;
-            if (d == WEST && row == row0 && forcing && ex == a.fx)
-                in &= ~force_flip_at<MODEL, GM, CG>(a, io, y);
-        }
-        return k ? ((v1 >> 1) | (in << 63)) : ((v0 >> 1) | (v1 << 63));
-    };
-    // pulled values of word k of the pair
-    uint64_t q[2][7];
-    if (MODEL == M_HPP) {
-        const uint64_t a0 = shl(n[0][0], n[1][0], 0, row0, 0), a1 = shl(n[0][0], n[1][0], 0, row0, 1);
-        const uint64_t b0 = shr(n[0][2], n[1][2], 2, row0, 0), b1 = shr(n[0][2], n[1][2], 2, row0, 1);
-        q[0][0] = a0; q[1][0] = a1; q[0][2] = b0; q[1][2] = b1;
-        q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][3] = n[0][3]; q[1][3] = n[1][3];
-    } else {
-        const uint64_t a0 = shl(n[0][0], n[1][0], 0, row0, 0), a1 = shl(n[0][0], n[1][0], 0, row0, 1);
-        const uint64_t b0 = shr(n[0][3], n[1][3], 3, row0, 0), b1 = shr(n[0][3], n[1][3], 3, row0, 1);
-        q[0][0] = a0; q[1][0] = a1; q[0][3] = b0; q[1][3] = b1;
-        if (even) {
-            const uint64_t c0 = shl(n[0][1], n[1][1], 1, rowm, 0), c1 = shl(n[0][1], n[1][1], 1, rowm, 1);
-            const uint64_t e0 = shl(n[0][5], n[1][5], 5, rowp, 0), e1 = shl(n[0][5], n[1][5], 5, rowp, 1);
-            q[0][1] = c0; q[1][1] = c1; q[0][5] = e0; q[1][5] = e1;
-            q[0][2] = n[0][2]; q[1][2] = n[1][2]; q[0][4] = n[0][4]; q[1][4] = n[1][4];
-        } else {
-            const uint64_t c0 = shr(n[0][2], n[1][2], 2, rowm, 0), c1 = shr(n[0][2], n[1][2], 2, rowm, 1);
-            const uint64_t e0 = shr(n[0][4], n[1][4], 4, rowp, 0), e1 = shr(n[0][4], n[1][4], 4, rowp, 1);
-            q[0][2] = c0; q[1][2] = c1; q[0][4] = e0; q[1][4] = e1;
-            q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][5] = n[0][5]; q[1][5] = n[1][5];
-        }
-        if (D == 7) { q[0][6] = n[0][6]; q[1][6] = n[1][6]; }
-    }
-    if (!active) return;
-
-    const bool nsrow = (y == 0) || (y == g.H - 1);
-    uint64_t out[2][7];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        uint64_t p[7], c[7];
-#pragma unroll
-        for (int d = 0; d < D; ++d) c[d] = p[d] = q[k][d];
-        if (MODEL != M_HPP) {
-            const uint64_t chir =
-                a.chir ? __ldg(a.chir + row0 + w0 + k)
-                       : lgca_rng_draw(io.ckey, lgca_rng_index((uint32_t)y, (uint32_t)(w0 + k)));
-            collide<MODEL>(c, chir);
-        } else {
-            collide<MODEL>(c, 0ull);
-        }
-        if (GM == GEOM_NONE) {
-#pragma unroll
-            for (int d = 0; d < D; ++d) out[k][d] = c[d];
-        } else {
-            const uint64_t fl = ~(solid[k] | slip[k]);
-            const uint64_t ew = (w0 + k == 0 ? 1ull : 0ull) | (w0 + k == g.nw - 1 ? (1ull << 63) : 0ull);
-#pragma unroll
-            for (int d = 0; d < D; ++d) {
-                uint64_t o = (fl & c[d]) | (solid[k] & p[Dirs<MODEL>::inv(d)]);
-                if (GM == GEOM_FULL) {
-                    const uint64_t sx = nsrow ? p[Dirs<MODEL>::mirx(d)] : p[d];
-                    o |= slip[k] & ((ew & p[Dirs<MODEL>::miry(d)]) | (~ew & sx));
-                }
-                out[k][d] = o;
-            }
-        }
-    }
-    uint64_t *__restrict__ dp = io.dst + row0 + w0;
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-        *reinterpret_cast<ulonglong2 *>(dp + d * ps) = make_ulonglong2(out[0][d], out[1][d]);
-}
 
 // Grid: x = 32-word chunk of a row, y = group of STEP_WARPS rows; one warp
 // per (row, chunk).

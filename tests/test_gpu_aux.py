@@ -141,3 +141,42 @@ def test_body_force_matches_oracle_large(gpu, oracle, model):
             got = L.download()
         assert n == nrev
         assert np.array_equal(got, want), (forcing, d)
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_checkpoint_resume_is_bit_exact(gpu, oracle, model):
+    """Stop after 17 steps, save, restore into a fresh handle, run 23 more:
+    identical to 40 uninterrupted steps (geometry, forcing, chirality,
+    body-force counter and step counter all carried)."""
+    W, H = 320, 40
+    types = G.reflecting(W, H, "forward")
+    types[10:20, 100:120] = G.SOLID_NO_SLIP
+    rng = np.random.default_rng(model)
+    chir = rng.integers(0, 2, (H, W), dtype=np.uint8) if model == 2 else None
+
+    def fresh():
+        L = gpu.GpuLattice(model, W, H, seed=77)
+        L.set_cell_types(types)
+        L.init_random(0.3, 0.2)
+        L.set_forcing_column(5, 0.4)
+        if chir is not None:
+            L.set_chirality(chir)
+        return L
+
+    with fresh() as A:
+        A.collide_and_propagate(17)
+        A.apply_body_force(50, "x")
+        blob = A.checkpoint()
+        A.collide_and_propagate(23)
+        A.apply_body_force(30, "y")
+        want = A.download()
+    with gpu.GpuLattice(model, W, H, seed=0) as B:
+        B.restore(blob)
+        assert B.step_count == 17
+        B.collide_and_propagate(23)
+        B.apply_body_force(30, "y")
+        assert np.array_equal(B.download(), want)
+        assert np.array_equal(B.get_cell_types(), types)
+    with gpu.GpuLattice(model, W + 64, H) as C_:
+        with pytest.raises(gpu.LgcaError):
+            C_.restore(blob)

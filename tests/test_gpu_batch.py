@@ -1,0 +1,85 @@
+"""Batched lattices (lgca_batch_*): every member of a mixed batch -- models,
+sizes (ragged widths included), geometries, forcing, frozen chirality and
+different step counts -- ends with exactly the bits it reaches when stepped
+alone, with and without CUDA graphs."""
+import numpy as np
+import pytest
+
+from lgca_gb300 import geometry as G
+
+pytestmark = pytest.mark.gpu
+
+GEOMS = [lambda w, h: G.periodic(w, h), G.pipe, G.karman_reference,
+         lambda w, h: G.reflecting(w, h, "forward"),
+         lambda w, h: G.disc(w, h, w // 8, h // 2, max(1, h // 16))]
+
+
+def make_jobs(gpu, n, rng, max_side=700):
+    jobs = []
+    for i in range(n):
+        model = int(rng.integers(4))
+        W = int(rng.choice([64, 100, 128, 256, 300, 512, 640, max_side]))
+        H = 2 * int(rng.integers(2, max_side // 2))
+        types = GEOMS[int(rng.integers(len(GEOMS)))](W, H)
+        L = gpu.GpuLattice(model, W, H, seed=1000 + i)
+        L.set_cell_types(types)
+        L.init_random(float(rng.uniform(0.1, 0.4)), float(rng.uniform(0.1, 0.4)))
+        if rng.random() < 0.5:
+            L.set_forcing_column(int(rng.integers(W)), 0.05)
+        if model > 0 and rng.random() < 0.2:
+            L.set_chirality(rng.integers(0, 2, (H, W), dtype=np.uint8))
+        L.set_step(int(rng.integers(0, 1000)))
+        jobs.append(L)
+    return jobs
+
+
+@pytest.mark.parametrize("graph_steps", [0, 8, 32])
+def test_mixed_batch_equals_alone(gpu, graph_steps):
+    rng = np.random.default_rng(graph_steps + 1)
+    jobs = make_jobs(gpu, 24, rng)
+    steps = [int(x) for x in rng.integers(0, 90, len(jobs))]
+    steps[0] = 90
+    # reference: each lattice alone (its checkpoint restored into a twin)
+    want = []
+    for L, n in zip(jobs, steps):
+        twin = gpu.GpuLattice(L.model, L.dim_x, L.dim_y)
+        twin.restore(L.checkpoint())
+        twin.collide_and_propagate(n)
+        want.append((twin.download(), twin.step_count))
+        twin.close()
+    with gpu.GpuBatch(graph_steps=graph_steps) as B:
+        for L in jobs:
+            B.add(L)
+        B.step_each(steps)
+        for L, (w, t) in zip(jobs, want):
+            assert L.step_count == t
+            assert np.array_equal(L.download(), w), (L.model, L.dim_x, L.dim_y)
+    for L in jobs:
+        L.close()
+
+
+def test_batch_calls_interleave_with_member_calls(gpu, oracle):
+    """Work queued on a member before a batch call runs first, and the member
+    continues after it; several batch calls in a row; members removed."""
+    W, H = 256, 48
+    types = G.pipe(W, H)
+    A = gpu.GpuLattice(3, W, H, seed=5)
+    Bl = gpu.GpuLattice(1, 192, 30, seed=6)
+    A.set_cell_types(types)
+    st = oracle.init_bernoulli(3, W, H, types, seed=5, p_move=0.3, p_rest=0.3)
+    A.upload(st)  # queued on A's stream, not yet synchronised
+    A.set_forcing_column(9, 0.3)
+    Bl.init_random(0.3)
+    with gpu.GpuBatch(graph_steps=4) as B:
+        B.add(A)
+        B.add(Bl)
+        B.step_each([10, 3])
+        A.collide_and_propagate(5)  # member's own call after the batch
+        B.step(12)
+        B.remove(Bl)
+        B.step(7)
+    want = oracle.run(3, st, 34, types=types, seed=5, force_x=9, force_p=0.3)
+    assert A.step_count == 34 and Bl.step_count == 15
+    assert np.array_equal(A.download(), want)
+    A.close()
+    Bl.close()
