@@ -210,8 +210,8 @@ int lgca_checkpoint_save(lgca_handle h, void *buf, size_t bytes);
 int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes);
 
 /* Batches: many lattices (any sizes, models, geometries) advanced together,
- * one launch per step and model family over a device work-list of the
- * members' rows, the steps captured in CUDA graphs.  Members stay owned by
+ * one launch per step over a device work-list of the members' rows, the
+ * steps captured in CUDA graphs.  Members stay owned by
  * the caller and keep their own state, counters and settings; each member
  * gives exactly the bits it gives when stepped alone.  No reference
  * counterpart (the reference steps one lattice per object).

@@ -1,0 +1,126 @@
+"""Measured autotuning of the kernel choices.
+
+Two tables, both chosen by timing candidates on the GPU:
+
+* single lattice, per (model, size class): kernel family and steps per pass
+  over global memory -- one step per pass with one or two words per lane,
+  register wavefront or shared-memory tiles with 2, 4 or 8 steps per pass;
+* batch members, per (model family, size class): words per lane of the
+  batched one-step kernel.
+
+A size class is the power of two of the site count (W*H rounded down).
+Candidates are timed on a copy of the caller's lattice (checkpoint/restore),
+so tuning never changes a lattice's state.  Results are cached in memory and,
+optionally, in a JSON file.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import time
+
+import lgca_gb300 as gpu
+
+# (variant, depth): 5 = one step per pass, two words per lane; 1 = one word
+# per lane; 2 = register wavefront; 3 = shared-memory tiles
+SINGLE_CANDIDATES = [(5, 1), (1, 1), (2, 2), (2, 4), (2, 8), (3, 2), (3, 4), (3, 8)]
+WPT_CANDIDATES = {1: 1, 2: 5}  # words per lane -> kernel variant of a batch member
+
+
+def size_class(W: int, H: int) -> int:
+    return int(math.log2(max(1, W * H)))
+
+
+def family(model: int) -> int:
+    return 0 if model == gpu.HPP else (1 if model == gpu.FHP_I else 2)
+
+
+class Autotuner:
+    def __init__(self, cache_path: str | None = None):
+        self.cache_path = cache_path
+        self.single: dict[str, tuple[int, int]] = {}
+        self.batch: dict[str, int] = {}
+        if cache_path and os.path.exists(cache_path):
+            with open(cache_path) as f:
+                d = json.load(f)
+            self.single = {k: tuple(v) for k, v in d.get("single", {}).items()}
+            self.batch = {k: int(v) for k, v in d.get("batch", {}).items()}
+
+    def save(self) -> None:
+        if self.cache_path:
+            with open(self.cache_path, "w") as f:
+                json.dump({"single": self.single, "batch": self.batch}, f, indent=1)
+
+    # ------------------------------------------------------------ single lattice
+    def tune_lattice(self, L: "gpu.GpuLattice", steps: int = 16) -> tuple[int, int]:
+        """Choose (variant, depth) for L's (model, size class) by timing the
+        candidates on a twin of L; apply the choice to L and return it."""
+        key = f"{L.model}:{size_class(L.dim_x, L.dim_y)}"
+        if key not in self.single:
+            blob = L.checkpoint()
+            twin = gpu.GpuLattice(L.model, L.dim_x, L.dim_y)
+            best, best_t = (5, 1), float("inf")
+            for variant, depth in SINGLE_CANDIDATES:
+                twin.restore(blob)
+                twin.set_kernel_variant(variant)
+                twin.set_temporal_depth(depth)
+                n = max(steps, 2 * depth)
+                twin.collide_and_propagate(depth)  # warm-up (and kernel load)
+                twin.sync()
+                t0 = time.perf_counter()
+                twin.collide_and_propagate(n)
+                twin.sync()
+                t = (time.perf_counter() - t0) / n
+                if t < best_t:
+                    best, best_t = (variant, depth), t
+            twin.close()
+            self.single[key] = best
+        variant, depth = self.single[key]
+        L.set_kernel_variant(variant)
+        L.set_temporal_depth(depth)
+        return variant, depth
+
+    # ------------------------------------------------------------ batch members
+    def tune_batch_members(self, lattices, steps: int = 8, sample: int = 6) -> dict[str, int]:
+        """Choose words per lane per (model family, size class) by timing a
+        batch of up to `sample` twins of the class's members with each
+        candidate; apply the choice (as the members' kernel variant)."""
+        groups: dict[str, list] = {}
+        for L in lattices:
+            groups.setdefault(f"{family(L.model)}:{size_class(L.dim_x, L.dim_y)}", []).append(L)
+        for key, members in groups.items():
+            if key not in self.batch:
+                twins = []
+                for L in members[:sample]:
+                    T = gpu.GpuLattice(L.model, L.dim_x, L.dim_y)
+                    T.restore(L.checkpoint())
+                    twins.append(T)
+                best, best_t = 2, float("inf")
+                for wpt, variant in WPT_CANDIDATES.items():
+                    with gpu.GpuBatch() as B:
+                        for T in twins:
+                            T.set_kernel_variant(variant)
+                            B.add(T)
+                        B.step(2)
+                        B.sync()
+                        t0 = time.perf_counter()
+                        B.step(steps)
+                        B.sync()
+                        t = time.perf_counter() - t0
+                    if t < best_t:
+                        best, best_t = wpt, t
+                for T in twins:
+                    T.close()
+                self.batch[key] = best
+            for L in members:
+                L.set_kernel_variant(WPT_CANDIDATES[self.batch[key]])
+        return dict(self.batch)
+
+
+def describe(tuner: Autotuner) -> dict:
+    names = {1: "one-step/1 word", 5: "one-step/2 words", 2: "wavefront", 3: "smem tiles"}
+    return {k: f"{names.get(v[0], v[0])}, depth {v[1]}" for k, v in tuner.single.items()}
+
+
+__all__ = ["Autotuner", "size_class", "family", "SINGLE_CANDIDATES", "describe"]

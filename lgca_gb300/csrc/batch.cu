@@ -1,14 +1,15 @@
 // Batched step: many independent lattices of any sizes, models and
-// geometries advance together, one launch per step and model family over a
-// device-side work-list of warp tasks (lattice, row, chunk of words).  Each
+// geometries advance together, one launch per step over a device-side
+// work-list of warp tasks (lattice, row, chunk of words).  Each
 // task runs the same per-word step code as the single-lattice kernels, with
 // the lattice's own buffers, geometry, forcing and keys, so every lattice
 // gives exactly the bits it gives alone.
 //
-// Work-list: the lattices of one model family sorted by steps to do
-// (descending); prefix[l] = first task of lattice l.  At step s the active
-// lattices are a prefix of the list, so a launch covers tasks
-// [0, prefix[n_active]).  A warp finds its lattice by binary search.
+// Work-list: all members sorted by steps to do (descending); prefix[l] =
+// first task of lattice l, block_lat[b] = lattice of block b's first task.
+// At step s the active lattices are a prefix of the list, so a launch covers
+// tasks [0, prefix[n_active]).  The chirality and forcing keys of every
+// (member, step) are computed once per batch call into a table.
 #include "internal.cuh"
 #include "../../include/lgca/rng.h"
 
@@ -17,38 +18,55 @@
 
 namespace lgca_gpu {
 
-template <int MODEL>
+// One launch per step for all members: warp task g belongs to the lattice
+// found from the block's first lattice (block_lat) by a short forward scan;
+// the lattice's entry selects model, geometry mode and words per lane.
 __global__ void __launch_bounds__(256) k_batch(const BatchEntry *__restrict__ E,
-                                               const int *__restrict__ prefix, int n_active,
+                                               const int *__restrict__ prefix,
+                                               const int *__restrict__ block_lat, int n_active,
                                                int s_local, const int *__restrict__ s_base)
 {
     const int lane = threadIdx.x & 31;
     const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int total = prefix[n_active];
-    if (g >= total) return;
-    int lo = 0, hi = n_active - 1;  // largest l with prefix[l] <= g
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (prefix[mid] <= g) lo = mid;
-        else hi = mid - 1;
-    }
-    const BatchEntry &e = E[lo];
+    if (g >= prefix[n_active]) return;
+    int l = block_lat[blockIdx.x];
+    while (prefix[l + 1] <= g) ++l;
+    const BatchEntry &e = E[l];
     const int s = *s_base + s_local;
-    const int local = g - prefix[lo];
-    const int y = local / e.per_row, c = local - y * e.per_row;
-    const uint64_t t = e.t0 + (uint64_t)s;
-    const StepIO io{(s & 1) ? e.buf1 : e.buf0, (s & 1) ? e.buf0 : e.buf1,
-                    lgca_rng_key(e.seed, LGCA_STREAM_CHIR, t),
-                    lgca_rng_key(e.seed, LGCA_STREAM_FORCE, t)};
+    const int local = g - prefix[l];
+    const int rg = local / e.per_row, c = local - rg * e.per_row;
+    const int y = rg * (32 / e.width) + lane / e.width;  // rows of <= 16 items share a warp
+    const ulonglong2 k = __ldg(reinterpret_cast<const ulonglong2 *>(e.keys) + s);
+    const StepIO io{(s & 1) ? e.buf1 : e.buf0, (s & 1) ? e.buf0 : e.buf1, k.x, k.y};
     const StepArgs &a = e.a;
-    switch (e.gm * 2 + (e.wpt == 2 ? 1 : 0)) {
-    case GEOM_NONE * 2: step_word<MODEL, GEOM_NONE>(a, io, y, c * 32 + lane, lane); break;
-    case GEOM_NONE * 2 + 1: step_pair<MODEL, GEOM_NONE>(a, io, y, c * 32 + lane, lane); break;
-    case GEOM_NOSLIP * 2: step_word<MODEL, GEOM_NOSLIP>(a, io, y, c * 32 + lane, lane); break;
-    case GEOM_NOSLIP * 2 + 1: step_pair<MODEL, GEOM_NOSLIP>(a, io, y, c * 32 + lane, lane); break;
-    case GEOM_FULL * 2: step_word<MODEL, GEOM_FULL>(a, io, y, c * 32 + lane, lane); break;
-    default: step_pair<MODEL, GEOM_FULL>(a, io, y, c * 32 + lane, lane); break;
+    const int w = c * 32 + (lane & (e.width - 1)), wd = e.width;
+#define LGCA_BATCH_CASES(F, MODEL)                                                             \
+    case F * 6 + GEOM_NONE * 2: step_word<MODEL, GEOM_NONE>(a, io, y, w, lane, wd); break;        \
+    case F * 6 + GEOM_NONE * 2 + 1: step_pair<MODEL, GEOM_NONE>(a, io, y, w, lane, wd); break;    \
+    case F * 6 + GEOM_NOSLIP * 2: step_word<MODEL, GEOM_NOSLIP>(a, io, y, w, lane, wd); break;    \
+    case F * 6 + GEOM_NOSLIP * 2 + 1: step_pair<MODEL, GEOM_NOSLIP>(a, io, y, w, lane, wd); break;\
+    case F * 6 + GEOM_FULL * 2: step_word<MODEL, GEOM_FULL>(a, io, y, w, lane, wd); break;        \
+    case F * 6 + GEOM_FULL * 2 + 1: step_pair<MODEL, GEOM_FULL>(a, io, y, w, lane, wd); break;
+    switch (e.code) {
+        LGCA_BATCH_CASES(0, M_HPP)
+        LGCA_BATCH_CASES(1, M_FHP_I)
+        LGCA_BATCH_CASES(2, M_FHP_II)
+    default: break;
     }
+#undef LGCA_BATCH_CASES
+}
+
+// keys[l][s] = (chirality key, forcing key) of member l at its step t0 + s
+__global__ void k_batch_keys(const BatchEntry *__restrict__ E, int n, int max_steps)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)n * max_steps) return;
+    const int l = (int)(i / max_steps), s = (int)(i - (long long)l * max_steps);
+    const BatchEntry &e = E[l];
+    if (s >= e.nsteps) return;
+    const uint64_t t = e.t0 + (uint64_t)s;
+    e.keys[2 * s] = lgca_rng_key(e.seed, LGCA_STREAM_CHIR, t);
+    e.keys[2 * s + 1] = lgca_rng_key(e.seed, LGCA_STREAM_FORCE, t);
 }
 
 __global__ void k_advance(int *s_base, int by)
@@ -56,16 +74,21 @@ __global__ void k_advance(int *s_base, int by)
     if (threadIdx.x == 0 && blockIdx.x == 0) *s_base += by;
 }
 
-cudaError_t launch_batch(int model_family, const BatchEntry *E, const int *prefix, int n_active,
-                         int total_tasks, int s_local, const int *s_base, cudaStream_t st)
+cudaError_t launch_batch(const BatchEntry *E, const int *prefix, const int *block_lat,
+                         int n_active, int total_tasks, int s_local, const int *s_base,
+                         cudaStream_t st)
 {
     if (total_tasks <= 0) return cudaSuccess;
     const unsigned grid = (unsigned)((total_tasks + 7) / 8);
-    switch (model_family) {
-    case M_HPP: k_batch<M_HPP><<<grid, 256, 0, st>>>(E, prefix, n_active, s_local, s_base); break;
-    case M_FHP_I: k_batch<M_FHP_I><<<grid, 256, 0, st>>>(E, prefix, n_active, s_local, s_base); break;
-    default: k_batch<M_FHP_II><<<grid, 256, 0, st>>>(E, prefix, n_active, s_local, s_base); break;
-    }
+    k_batch<<<grid, 256, 0, st>>>(E, prefix, block_lat, n_active, s_local, s_base);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_keys(const BatchEntry *E, int n, int max_steps, cudaStream_t st)
+{
+    const long long work = (long long)n * max_steps;
+    if (work <= 0) return cudaSuccess;
+    k_batch_keys<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(E, n, max_steps);
     return cudaGetLastError();
 }
 

@@ -53,12 +53,17 @@ struct BatchEntry {
     StepArgs a;
     uint64_t *buf0, *buf1;
     uint64_t seed, t0;
+    uint64_t *keys;  // 2 * nsteps keys (chirality, forcing) per step of the call
     int nsteps;
-    int per_row;  // warp tasks per row
+    int per_row;  // warp tasks per row group
+    int width;    // lanes per row (32 / width rows per warp task)
     int gm, wpt;  // geometry mode, words per lane
+    int code;     // model family * 6 + geometry mode * 2 + (wpt == 2)
 };
-cudaError_t launch_batch(int model_family, const BatchEntry *E, const int *prefix, int n_active,
-                         int total_tasks, int s_local, const int *s_base, cudaStream_t stream);
+cudaError_t launch_batch(const BatchEntry *E, const int *prefix, const int *block_lat,
+                         int n_active, int total_tasks, int s_local, const int *s_base,
+                         cudaStream_t stream);
+cudaError_t launch_batch_keys(const BatchEntry *E, int n, int max_steps, cudaStream_t stream);
 cudaError_t launch_advance(int *s_base, int by, cudaStream_t stream);
 
 // One lattice step of `a` (k = 1), launched on `stream`.
@@ -139,6 +144,15 @@ cudaError_t launch_body_force(int model, const PlaneGeom &g, uint64_t *planes,
                               const uint64_t *solid, const uint64_t *slip, uint64_t key,
                               long long forcing, int bf_dir, void *scratch,
                               unsigned long long *reverted_dev, cudaStream_t s);
+
+// Lanes per row segment for a row of n lane-items: rows of 16 or fewer items
+// share a warp (32 / width rows per warp), wider rows take whole warps.
+__host__ __device__ __forceinline__ int seg_width(int n)
+{
+    int w = 1;
+    while (w < n && w < 32) w <<= 1;
+    return n > 16 ? 32 : w;
+}
 
 static inline int num_dir(int model) { return model == M_HPP ? 4 : (model == M_FHP_I ? 6 : 7); }
 

@@ -758,14 +758,13 @@ struct lgca_batch {
     cudaEvent_t done = nullptr;
     int *s_base = nullptr;       // device: first batch-local step of a graph replay
     int graph_steps = 32;        // steps captured per CUDA graph (0: no graphs)
-    struct Family {
-        BatchEntry *dE = nullptr;
-        int *dP = nullptr;
-        size_t cap = 0;
-        std::vector<BatchEntry> E;
-        std::vector<int> P;
-        std::vector<int> nsteps;  // per entry, descending
-    } fam[3];
+    // device work-list: entries, task prefix, block -> lattice map, key table
+    BatchEntry *dE = nullptr;
+    int *dP = nullptr, *dB = nullptr;  // dB points into dP's allocation
+    uint64_t *dK = nullptr;
+    size_t capE = 0, capB = 0, capK = 0;
+    std::vector<BatchEntry> E;
+    std::vector<int> P, Bl, nsteps;  // nsteps per entry, descending
     std::string err;
 };
 
@@ -791,19 +790,24 @@ int bcuda(lgca_batch *b, cudaError_t e, const char *what)
         if (e_ != cudaSuccess) return bcuda((b), e_, #expr);        \
     } while (0)
 
-int family_of(int model) { return model == LGCA_HPP ? 0 : (model == LGCA_FHP_I ? 1 : 2); }
-int family_model(int f) { return f == 0 ? M_HPP : (f == 1 ? M_FHP_I : M_FHP_II); }
-
-// Launches of batch-local steps [s0, s0 + n) of one segment (fixed active
-// sets), steps numbered from *s_base + s_local.
-int enqueue_steps(lgca_batch *b, const int *n_active, const int *tasks, int n)
+// Launches of batch-local steps [0, n) of one segment (fixed active set),
+// steps numbered from *s_base + s_local; then *s_base advances by n.
+int enqueue_steps(lgca_batch *b, int n_active, int tasks, int n)
 {
     for (int s = 0; s < n; ++s)
-        for (int f = 0; f < 3; ++f)
-            if (n_active[f] > 0)
-                BCK(b, launch_batch(family_model(f), b->fam[f].dE, b->fam[f].dP, n_active[f],
-                                    tasks[f], s, b->s_base, b->stream));
+        BCK(b, launch_batch(b->dE, b->dP, b->dB, n_active, tasks, s, b->s_base, b->stream));
     BCK(b, launch_advance(b->s_base, n, b->stream));
+    return LGCA_OK;
+}
+
+template <class T> int grow(lgca_batch *b, T *&p, size_t &cap, size_t n)
+{
+    if (cap >= n) return LGCA_OK;
+    cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    BCK(b, cudaMalloc(&p, n * sizeof(T)));
+    cap = n;
     return LGCA_OK;
 }
 
@@ -836,10 +840,9 @@ int lgca_batch_destroy(lgca_batch_handle b)
     DeviceGuard dg(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
-    for (auto &f : b->fam) {
-        cudaFree(f.dE);
-        cudaFree(f.dP);
-    }
+    cudaFree(b->dE);
+    cudaFree(b->dP);  // dB lives in the same allocation
+    cudaFree(b->dK);
     cudaFree(b->s_base);
     if (b->done) cudaEventDestroy(b->done);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -908,20 +911,17 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         BCK(b, cudaEventRecord(b->ev[i], b->members[i]->stream));
         BCK(b, cudaStreamWaitEvent(b->stream, b->ev[i], 0));
     }
-    // work-lists per model family, lattices sorted by steps (descending)
+    // one work-list, lattices sorted by steps (descending)
     std::vector<int> order(nm);
     for (size_t i = 0; i < nm; ++i) order[i] = (int)i;
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return nsteps[x] > nsteps[y]; });
-    int max_steps = 0;
-    for (auto &f : b->fam) {
-        f.E.clear();
-        f.P.assign(1, 0);
-        f.nsteps.clear();
-    }
+    b->E.clear();
+    b->P.assign(1, 0);
+    b->nsteps.clear();
+    size_t nkeys = 0;
     for (int i : order) {
         if (nsteps[i] == 0) continue;
         lgca_lattice *h = b->members[i];
-        auto &f = b->fam[family_of(h->model)];
         BatchEntry e;
         memset(&e, 0, sizeof(e));
         e.a.solid = h->solid;
@@ -936,48 +936,53 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         e.a.wpt = pair ? 2 : 1;
         e.wpt = e.a.wpt;
         e.gm = geom_mode(h);
-        e.per_row = pair ? (h->g.nw / 2 + 31) / 32 : (h->g.nw + 31) / 32;
+        const int fam = h->model == LGCA_HPP ? 0 : (h->model == LGCA_FHP_I ? 1 : 2);
+        e.code = fam * 6 + e.gm * 2 + (pair ? 1 : 0);
+        const int items = pair ? h->g.nw / 2 : h->g.nw;  // lane items per row
+        e.width = seg_width(items);
+        e.per_row = (items + 31) / 32;
+        const int row_groups = (h->g.H + (32 / e.width) - 1) / (32 / e.width);
         e.buf0 = h->buf[h->cur];
         e.buf1 = h->buf[h->cur ^ 1];
         e.seed = h->seed;
         e.t0 = h->t;
         e.nsteps = nsteps[i];
-        const long long tasks = (long long)f.P.back() + (long long)h->g.H * e.per_row;
+        e.keys = reinterpret_cast<uint64_t *>(nkeys);  // offset; rebased below
+        nkeys += 2 * (size_t)nsteps[i];
+        const long long tasks = (long long)b->P.back() + (long long)row_groups * e.per_row;
         if (tasks > 0x7fffffffLL) return bfail(b, LGCA_ERR_INVALID, "batch work-list too long");
-        f.E.push_back(e);
-        f.P.push_back((int)tasks);
-        f.nsteps.push_back(nsteps[i]);
-        max_steps = std::max(max_steps, nsteps[i]);
+        b->E.push_back(e);
+        b->P.push_back((int)tasks);
+        b->nsteps.push_back(nsteps[i]);
     }
-    for (auto &f : b->fam) {
-        if (f.E.empty()) continue;
-        if (f.cap < f.E.size()) {
-            cudaFree(f.dE);
-            cudaFree(f.dP);
-            f.dE = nullptr;
-            f.dP = nullptr;
-            f.cap = 0;
-            BCK(b, cudaMalloc(&f.dE, f.E.size() * sizeof(BatchEntry)));
-            BCK(b, cudaMalloc(&f.dP, (f.E.size() + 1) * sizeof(int)));
-            f.cap = f.E.size();
+    const int ne = (int)b->E.size();
+    const int max_steps = ne ? b->nsteps[0] : 0;
+    if (ne > 0) {
+        const int total = b->P.back();
+        const int nblocks = (total + 7) / 8;
+        b->Bl.resize(nblocks);
+        for (int blk = 0, l = 0; blk < nblocks; ++blk) {
+            while (b->P[l + 1] <= blk * 8) ++l;
+            b->Bl[blk] = l;
         }
+        int st;
+        if ((st = grow(b, b->dE, b->capE, (size_t)ne)) != LGCA_OK) return st;
+        if ((st = grow(b, b->dP, b->capB, (size_t)ne + 1 + nblocks)) != LGCA_OK) return st;
+        if ((st = grow(b, b->dK, b->capK, nkeys)) != LGCA_OK) return st;
+        b->dB = b->dP + ne + 1;
+        for (auto &e : b->E) e.keys = b->dK + reinterpret_cast<size_t>(e.keys);
         // synchronous copies: the host vectors are reused by the next call
-        BCK(b, cudaMemcpy(f.dE, f.E.data(), f.E.size() * sizeof(BatchEntry), cudaMemcpyHostToDevice));
-        BCK(b, cudaMemcpy(f.dP, f.P.data(), f.P.size() * sizeof(int), cudaMemcpyHostToDevice));
+        BCK(b, cudaMemcpy(b->dE, b->E.data(), ne * sizeof(BatchEntry), cudaMemcpyHostToDevice));
+        BCK(b, cudaMemcpy(b->dP, b->P.data(), (ne + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        BCK(b, cudaMemcpy(b->dB, b->Bl.data(), nblocks * sizeof(int), cudaMemcpyHostToDevice));
+        BCK(b, launch_batch_keys(b->dE, ne, max_steps, b->stream));
     }
     // segments of constant active sets: [s0, s1) where no lattice finishes
     int s0 = 0;
     while (s0 < max_steps) {
-        int s1 = max_steps, n_active[3] = {0, 0, 0}, tasks[3] = {0, 0, 0};
-        for (int f = 0; f < 3; ++f) {
-            const auto &F = b->fam[f];
-            int k = 0;
-            while (k < (int)F.nsteps.size() && F.nsteps[k] > s0) ++k;
-            n_active[f] = k;
-            tasks[f] = F.P[k];
-            for (int j = 0; j < k; ++j) s1 = std::min(s1, F.nsteps[j]);
-        }
-        const int len = s1 - s0;
+        int k = 0;
+        while (k < ne && b->nsteps[k] > s0) ++k;
+        const int s1 = b->nsteps[k - 1], len = s1 - s0, tasks = b->P[k];
         BCK(b, cudaMemcpyAsync(b->s_base, &s0, sizeof(int), cudaMemcpyHostToDevice, b->stream));
         // the copy reads s0 from the host stack: wait for it before s0 changes
         BCK(b, cudaStreamSynchronize(b->stream));
@@ -987,7 +992,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
             cudaGraph_t graph = nullptr;
             cudaGraphExec_t exec = nullptr;
             BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-            const int st = enqueue_steps(b, n_active, tasks, G);
+            const int st = enqueue_steps(b, k, tasks, G);
             cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
             if (st != LGCA_OK) {
                 if (graph) cudaGraphDestroy(graph);
@@ -1008,7 +1013,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
             cudaGraphExecDestroy(exec);
         }
         if (done < len) {
-            const int st = enqueue_steps(b, n_active, tasks, len - done);
+            const int st = enqueue_steps(b, k, tasks, len - done);
             if (st != LGCA_OK) return st;
         }
         s0 = s1;

@@ -12,27 +12,31 @@ static constexpr int STEP_WARPS = 8;
 template <int MODEL, int GM>
 __global__ void __launch_bounds__(32 * STEP_WARPS) k_step(const StepArgs a)
 {
-    const int y = blockIdx.y * STEP_WARPS + threadIdx.y;
-    if (y >= a.g.H) return;  // whole warp
+    // rows of <= 16 words: 32/width rows per warp
+    const int width = seg_width(a.g.nw), rpw = 32 / width;
+    const int y = (blockIdx.y * STEP_WARPS + threadIdx.y) * rpw + threadIdx.x / width;
+    if ((blockIdx.y * STEP_WARPS + threadIdx.y) * rpw >= a.g.H) return;  // whole warp
     const StepIO io{a.src, a.dst, a.chir_key, a.force_key};
-    step_word<MODEL, GM>(a, io, y, blockIdx.x * 32 + threadIdx.x, threadIdx.x);
+    step_word<MODEL, GM>(a, io, y, blockIdx.x * 32 + (threadIdx.x & (width - 1)), threadIdx.x, width);
 }
 
 template <int MODEL, int GM>
 __global__ void __launch_bounds__(32 * STEP_WARPS) k_step2(const __grid_constant__ StepArgs a)
 {
-    const int y = blockIdx.y * STEP_WARPS + threadIdx.y;
-    if (y >= a.g.H) return;
+    const int width = seg_width(a.g.nw / 2), rpw = 32 / width;
+    const int y = (blockIdx.y * STEP_WARPS + threadIdx.y) * rpw + threadIdx.x / width;
+    if ((blockIdx.y * STEP_WARPS + threadIdx.y) * rpw >= a.g.H) return;
     const StepIO io{a.src, a.dst, a.chir_key, a.force_key};
-    step_pair<MODEL, GM>(a, io, y, blockIdx.x * 32 + threadIdx.x, threadIdx.x);
+    step_pair<MODEL, GM>(a, io, y, blockIdx.x * 32 + (threadIdx.x & (width - 1)), threadIdx.x, width);
 }
 
 template <int MODEL>
 static cudaError_t launch_model2(int gm, const StepArgs &a, cudaStream_t st)
 {
-    const int np = a.g.nw / 2;
+    const int np = a.g.nw / 2, rpw = 32 / seg_width(np);
+    const int rows_per_block = STEP_WARPS * rpw;
     const dim3 block(32, STEP_WARPS);
-    const dim3 grid((unsigned)((np + 31) / 32), (unsigned)((a.g.H + STEP_WARPS - 1) / STEP_WARPS));
+    const dim3 grid((unsigned)((np + 31) / 32), (unsigned)((a.g.H + rows_per_block - 1) / rows_per_block));
     if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
     switch (gm) {
     case GEOM_NONE: k_step2<MODEL, GEOM_NONE><<<grid, block, 0, st>>>(a); break;
@@ -46,8 +50,9 @@ template <int MODEL>
 static cudaError_t launch_model(int gm, const StepArgs &a, cudaStream_t st)
 {
     if (a.wpt == 2 && (a.g.nw % 2) == 0 && (a.g.W % 64) == 0) return launch_model2<MODEL>(gm, a, st);
+    const int rows_per_block = STEP_WARPS * (32 / seg_width(a.g.nw));
     const dim3 block(32, STEP_WARPS);
-    const dim3 grid((unsigned)a.chunks, (unsigned)((a.g.H + STEP_WARPS - 1) / STEP_WARPS));
+    const dim3 grid((unsigned)a.chunks, (unsigned)((a.g.H + rows_per_block - 1) / rows_per_block));
     if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
     switch (gm) {
     case GEOM_NONE: k_step<MODEL, GEOM_NONE><<<grid, block, 0, st>>>(a); break;

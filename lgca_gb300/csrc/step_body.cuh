@@ -74,11 +74,12 @@ __device__ __forceinline__ uint64_t force_flip_at(const StepArgs &a, const StepI
 
 template <int MODEL, int GM, bool CG = false>
 __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, const int y,
-                                          const int w, const int lane)
+                                          const int w, const int lane, const int width = 32)
 {
     constexpr int D = ModelTraits<MODEL>::D;
     const PlaneGeom &g = a.g;
-    const bool active = w < g.nw;
+    const bool active = w < g.nw && y < g.H;
+    const int seg = lane & (width - 1);  // lane within its row segment
     const int ym = (y == 0) ? g.H - 1 : y - 1;
     const int yp = (y == g.H - 1) ? 0 : y + 1;
     // 32-bit offsets: a lattice has at most 2^31 sites, so D * H * pitch < 2^29 words
@@ -117,8 +118,8 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
     }
 
     // neighbour words at the warp edges and the periodic x seam
-    const bool need_w = active && (lane == 0 || w == 0);
-    const bool need_e = active && (lane == 31 || w == g.nw - 1);
+    const bool need_w = active && (seg == 0 || w == 0);
+    const bool need_e = active && (seg == width - 1 || w == g.nw - 1);
     const int widx = (w == 0) ? g.nw - 1 : w - 1;
     const int wbit = (w == 0) ? g.L : 63;
     const int eidx = (w == g.nw - 1) ? 0 : w + 1;
@@ -128,7 +129,7 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
 
     // x-1 pull: (v << 1) | bit of site x-1
     auto shl = [&](uint64_t v, int d, unsigned row) -> uint64_t {
-        const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v >> 32), 1);
+        const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v >> 32), 1, width);
         uint64_t in = hi >> 31;
         if (need_w) {
             in = (ld_state<CG>(s + (d * ps + row + widx)) >> wbit) & 1ull;
@@ -139,7 +140,7 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
     };
     // x+1 pull: (v >> 1) | bit of site x+1 placed at the last valid bit
     auto shr = [&](uint64_t v, int d, unsigned row) -> uint64_t {
-        const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v, 1);
+        const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v, 1, width);
         uint64_t in = lo & 1u;
         if (need_e) {
             in = ld_state<CG>(s + (d * ps + row + eidx)) & 1ull;
@@ -158,16 +159,27 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
     } else {
         p[0] = shl(n[0], 0, row0);
         p[3] = shr(n[3], 3, row0);
-        if (even) {
-            p[1] = shl(n[1], 1, rowm);
-            p[5] = shl(n[5], 5, rowp);
-            p[2] = n[2];
-            p[4] = n[4];
+        if (width == 32) {  // one row per warp: the parity is warp-uniform
+            if (even) {
+                p[1] = shl(n[1], 1, rowm);
+                p[5] = shl(n[5], 5, rowp);
+                p[2] = n[2];
+                p[4] = n[4];
+            } else {
+                p[2] = shr(n[2], 2, rowm);
+                p[4] = shr(n[4], 4, rowp);
+                p[1] = n[1];
+                p[5] = n[5];
+            }
         } else {
-            p[2] = shr(n[2], 2, rowm);
-            p[4] = shr(n[4], 4, rowp);
-            p[1] = n[1];
-            p[5] = n[5];
+            // rows of both parities share the warp: every lane takes part in
+            // every shuffle, then selects by its row's parity
+            const uint64_t l1 = shl(n[1], 1, rowm), l5 = shl(n[5], 5, rowp);
+            const uint64_t r2 = shr(n[2], 2, rowm), r4 = shr(n[4], 4, rowp);
+            p[1] = even ? l1 : n[1];
+            p[5] = even ? l5 : n[5];
+            p[2] = even ? n[2] : r2;
+            p[4] = even ? n[4] : r4;
         }
         if (D == 7) p[6] = n[6];
     }
@@ -221,12 +233,13 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
 // fits in one wave of resident warps.  Same arithmetic as step_word.
 template <int MODEL, int GM, bool CG = false>
 __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, const int y,
-                                          const int t, const int lane)
+                                          const int t, const int lane, const int width = 32)
 {
     constexpr int D = ModelTraits<MODEL>::D;
     const PlaneGeom &g = a.g;
     const int np = g.nw >> 1;
-    const bool active = t < np;
+    const bool active = t < np && y < g.H;
+    const int seg = lane & (width - 1);  // lane within its row segment
     const int ym = (y == 0) ? g.H - 1 : y - 1;
     const int yp = (y == g.H - 1) ? 0 : y + 1;
     const unsigned rowm = (unsigned)ym * g.pitch, row0 = (unsigned)y * g.pitch,
@@ -284,8 +297,8 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
         n[1][WEST] &= ~f1;
     }
 
-    const bool need_w = active && (lane == 0 || t == 0);
-    const bool need_e = active && (lane == 31 || t == np - 1);
+    const bool need_w = active && (seg == 0 || t == 0);
+    const bool need_e = active && (seg == width - 1 || t == np - 1);
     const int widx = (t == 0) ? g.nw - 1 : w0 - 1;
     const int eidx = (t == np - 1) ? 0 : w0 + 2;
     const int wx = (t == 0) ? g.W - 1 : 64 * w0 - 1;
@@ -293,7 +306,7 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
 
     // x-1 pull of the pair (v0, v1)
     auto shl = [&](uint64_t v0, uint64_t v1, int d, unsigned row, int k) -> uint64_t {
-        const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v1 >> 32), 1);
+        const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v1 >> 32), 1, width);
         uint64_t in = hi >> 31;
         if (need_w) {
             in = ld_state<CG>(s + (d * ps + row + widx)) >> 63;
@@ -304,7 +317,7 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
     };
     // x+1 pull of the pair
     auto shr = [&](uint64_t v0, uint64_t v1, int d, unsigned row, int k) -> uint64_t {
-        const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v0, 1);
+        const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v0, 1, width);
         uint64_t in = lo & 1u;
         if (need_e) {
             in = ld_state<CG>(s + (d * ps + row + eidx)) & 1ull;
@@ -324,16 +337,28 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
         const uint64_t a0 = shl(n[0][0], n[1][0], 0, row0, 0), a1 = shl(n[0][0], n[1][0], 0, row0, 1);
         const uint64_t b0 = shr(n[0][3], n[1][3], 3, row0, 0), b1 = shr(n[0][3], n[1][3], 3, row0, 1);
         q[0][0] = a0; q[1][0] = a1; q[0][3] = b0; q[1][3] = b1;
-        if (even) {
+        if (width == 32) {  // one row per warp: the parity is warp-uniform
+            if (even) {
+                const uint64_t c0 = shl(n[0][1], n[1][1], 1, rowm, 0), c1 = shl(n[0][1], n[1][1], 1, rowm, 1);
+                const uint64_t e0 = shl(n[0][5], n[1][5], 5, rowp, 0), e1 = shl(n[0][5], n[1][5], 5, rowp, 1);
+                q[0][1] = c0; q[1][1] = c1; q[0][5] = e0; q[1][5] = e1;
+                q[0][2] = n[0][2]; q[1][2] = n[1][2]; q[0][4] = n[0][4]; q[1][4] = n[1][4];
+            } else {
+                const uint64_t c0 = shr(n[0][2], n[1][2], 2, rowm, 0), c1 = shr(n[0][2], n[1][2], 2, rowm, 1);
+                const uint64_t e0 = shr(n[0][4], n[1][4], 4, rowp, 0), e1 = shr(n[0][4], n[1][4], 4, rowp, 1);
+                q[0][2] = c0; q[1][2] = c1; q[0][4] = e0; q[1][4] = e1;
+                q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][5] = n[0][5]; q[1][5] = n[1][5];
+            }
+        } else {
+            // rows of both parities share the warp: all lanes shuffle, then select
             const uint64_t c0 = shl(n[0][1], n[1][1], 1, rowm, 0), c1 = shl(n[0][1], n[1][1], 1, rowm, 1);
             const uint64_t e0 = shl(n[0][5], n[1][5], 5, rowp, 0), e1 = shl(n[0][5], n[1][5], 5, rowp, 1);
-            q[0][1] = c0; q[1][1] = c1; q[0][5] = e0; q[1][5] = e1;
-            q[0][2] = n[0][2]; q[1][2] = n[1][2]; q[0][4] = n[0][4]; q[1][4] = n[1][4];
-        } else {
-            const uint64_t c0 = shr(n[0][2], n[1][2], 2, rowm, 0), c1 = shr(n[0][2], n[1][2], 2, rowm, 1);
-            const uint64_t e0 = shr(n[0][4], n[1][4], 4, rowp, 0), e1 = shr(n[0][4], n[1][4], 4, rowp, 1);
-            q[0][2] = c0; q[1][2] = c1; q[0][4] = e0; q[1][4] = e1;
-            q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][5] = n[0][5]; q[1][5] = n[1][5];
+            const uint64_t f0 = shr(n[0][2], n[1][2], 2, rowm, 0), f1 = shr(n[0][2], n[1][2], 2, rowm, 1);
+            const uint64_t h0 = shr(n[0][4], n[1][4], 4, rowp, 0), h1 = shr(n[0][4], n[1][4], 4, rowp, 1);
+            q[0][1] = even ? c0 : n[0][1]; q[1][1] = even ? c1 : n[1][1];
+            q[0][5] = even ? e0 : n[0][5]; q[1][5] = even ? e1 : n[1][5];
+            q[0][2] = even ? n[0][2] : f0; q[1][2] = even ? n[1][2] : f1;
+            q[0][4] = even ? n[0][4] : h0; q[1][4] = even ? n[1][4] : h1;
         }
         if (D == 7) { q[0][6] = n[0][6]; q[1][6] = n[1][6]; }
     }

@@ -83,3 +83,30 @@ def test_batch_calls_interleave_with_member_calls(gpu, oracle):
     assert np.array_equal(A.download(), want)
     A.close()
     Bl.close()
+
+
+def test_batched_config_small_is_bit_exact_and_faster(gpu):
+    """The batched workload generator at reduced scale: batched and
+    one-at-a-time runs agree bit for bit (the full 512 x 1000 run is in the
+    benchmark)."""
+    from lgca_gb300 import batched
+    r = batched.compare(n_jobs=24, steps=60, tune=True)
+    assert r["bit_exact"]
+    assert r["batched_gsite_updates_s"] > 0
+
+
+def test_autotuner_single_lattice_choice_keeps_results(gpu, oracle):
+    from lgca_gb300.autotune import Autotuner
+    W, H = 1024, 96
+    types = G.pipe(W, H)
+    st = oracle.init_bernoulli(0, W, H, types, seed=2, p_move=0.3)
+    L = gpu.GpuLattice(0, W, H, seed=2)
+    L.set_cell_types(types)
+    L.upload(st)
+    L.set_forcing_column(8, 0.2)
+    choice = Autotuner().tune_lattice(L, steps=8)
+    assert choice[0] in (1, 2, 3, 5)
+    L.collide_and_propagate(40)
+    want = oracle.run(0, st, 40, types=types, seed=2, force_x=8, force_p=0.2)
+    assert np.array_equal(L.download(), want) and L.step_count == 40
+    L.close()
