@@ -311,6 +311,12 @@ def run_ours(args):
 
     gate = gate_measurement(gpu, torch, hbm_peak) if rank == 0 else None
     L.close()
+    batched = None
+    if rank == 0 and not args.no_batched:
+        # the batched workload: 512 mixed lattices x 1000 steps, batched vs one at a time
+        from lgca_gb300 import batched as BT
+        batched = BT.compare(512, 1000, tune=True)
+        batched.pop("tuned_words_per_lane", None)
     if rank == 0:
         cpu = cpu_baseline() if ws == 1 else None
         line = {
@@ -322,6 +328,7 @@ def run_ours(args):
                        "l2": "flushed between timed steps (256 MiB write, outside the events)",
                        "parallelism": f"replicas x{ws}"},
             "wall_s": t_wall, "e2e": e2e, "roofline": roofline, "roofline_gate": gate,
+            "batched": batched,
             "cpu_baseline": cpu, "clocks": clk.summary(),
             "gpu_launches": (STEPS_PER_CHUNK + 1) * args.steps,
         }
@@ -336,6 +343,8 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 512-lattice batched vs one-at-a-time comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

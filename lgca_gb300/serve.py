@@ -1,0 +1,337 @@
+"""Serving loop: simulation jobs arrive over time, are admitted as device
+memory frees up, run together (continuous batching: every resident lattice
+advances in the same batched launches, jobs join and leave between batch
+calls), stream back coarse-grained fields, and report latency.
+
+Job stream (defaults): Poisson arrivals at `rate` jobs/s for `duration` s;
+model, geometry and occupation as the batched workload; width log-uniform in
+[256, 8192] and height in [256, 4096] (multiples of 64); steps log-uniform in
+[100, 20000]; seed = arrival index.  Every `out_every` steps (and at the end)
+a job returns its 16 x 16 integer block sums (N, Jx2, Jy).  Admission keeps
+the resident lattices' device bytes within `budget` (150 GB).
+
+The scheduler (Server) talks to a backend: GpuBackend runs the engine;
+tests substitute a CPU fake to exercise admission, budgets and failures.
+
+    python -m lgca_gb300.serve --rate 50 --duration 60
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+GEOMETRIES = ("periodic", "pipe", "disc")
+
+
+@dataclass
+class Job:
+    index: int
+    arrival: float
+    model: int
+    W: int
+    H: int
+    geometry: str
+    p: float
+    steps: int
+    seed: int
+    done_steps: int = 0
+    admitted: float | None = None
+    finished: float | None = None
+    outputs: int = 0
+    last_fields: tuple | None = None
+    handle: object = None
+    error: str | None = None
+    bytes: int = 0
+
+    @property
+    def sites(self) -> int:
+        return self.W * self.H
+
+    def next_event(self, out_every: int) -> int:
+        """Steps to the next output or the end."""
+        to_out = out_every - (self.done_steps % out_every)
+        return min(to_out, self.steps - self.done_steps)
+
+
+def _round64(v: float) -> int:
+    return max(64, int(round(v / 64.0)) * 64)
+
+
+def make_jobs(rate: float, duration: float, rng_seed: int = 5, w_range=(256, 8192),
+              h_range=(256, 4096), steps_range=(100, 20000), max_jobs: int | None = None):
+    rng = np.random.default_rng(rng_seed)
+    t, jobs = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration or (max_jobs is not None and len(jobs) >= max_jobs):
+            break
+        i = len(jobs)
+        lu = lambda lo, hi: math.exp(rng.uniform(math.log(lo), math.log(hi)))
+        jobs.append(Job(index=i, arrival=t, model=int(rng.integers(4)),
+                        W=_round64(lu(*w_range)), H=_round64(lu(*h_range)),
+                        geometry=GEOMETRIES[int(rng.integers(3))],
+                        p=float(rng.uniform(0.1, 0.4)),
+                        steps=int(round(lu(*steps_range))), seed=i))
+    return jobs
+
+
+def lattice_bytes(model: int, W: int, H: int, geometry: str) -> int:
+    """Device bytes of a lattice (state buffers, geometry planes, scratch)."""
+    D = {0: 4, 1: 6, 2: 7, 3: 7}[model]
+    nw = (W + 63) // 64
+    pitch = nw + (nw & 1)
+    plane = H * pitch * 8
+    geo = 2 * plane if geometry != "periodic" else 0
+    scratch = W * H * 4 + 4096  # cell types staging / block sums
+    return 2 * D * plane + geo + scratch
+
+
+class GpuBackend:
+    """Runs jobs on the GPU through the C ABI (one batch for all residents)."""
+
+    def __init__(self, block: int = 16):
+        import lgca_gb300 as gpu
+        from lgca_gb300 import geometry as G
+        self.gpu, self.G, self.block = gpu, G, block
+        self.batch = gpu.GpuBatch()
+
+    def create(self, job: Job):
+        gpu, G = self.gpu, self.G
+        L = gpu.GpuLattice(job.model, job.W, job.H, seed=job.seed)
+        if job.geometry == "pipe":
+            L.set_cell_types(G.pipe(job.W, job.H))
+            L.set_forcing_column(8, 0.01)
+        elif job.geometry == "disc":
+            L.set_cell_types(G.disc(job.W, job.H, job.W // 8, job.H // 2, max(1, job.H // 16),
+                                    walls=False))
+        L.init_random(job.p, job.p)
+        self.batch.add(L)
+        return L
+
+    def step(self, handles, nsteps):
+        # members not in `handles` do not step
+        counts = {id(h): n for h, n in zip(handles, nsteps)}
+        self.batch.step_each([counts.get(id(m), 0) for m in self.batch.members])
+
+    def fields(self, handle):
+        return handle.block_sums(self.block)
+
+    def destroy(self, handle):
+        self.batch.remove(handle)
+        handle.close()
+
+    def close(self):
+        self.batch.close()
+
+
+class Server:
+    def __init__(self, backend, budget: float = 150e9, out_every: int = 500,
+                 clock=time.perf_counter, sleep=time.sleep, max_quantum: int = 500):
+        self.backend, self.budget, self.out_every = backend, budget, out_every
+        self.clock, self.sleep, self.max_quantum = clock, sleep, max_quantum
+        self.used = 0
+        self.active: list[Job] = []
+        self.waiting: list[Job] = []
+        self.done: list[Job] = []
+        self.rejected: list[Job] = []
+        self.site_updates = 0
+        self.batch_calls = 0
+
+    def _admit(self, now: float) -> None:
+        # first come, first admitted; a job that never fits is rejected
+        while self.waiting:
+            job = self.waiting[0]
+            need = lattice_bytes(job.model, job.W, job.H, job.geometry)
+            if need > self.budget:
+                self.waiting.pop(0)
+                job.error = "larger than the memory budget"
+                self.rejected.append(job)
+                continue
+            if self.used + need > self.budget:
+                return
+            self.waiting.pop(0)
+            try:
+                job.handle = self.backend.create(job)
+            except Exception as e:  # allocation failure: retry once memory frees
+                job.error = f"create failed: {e}"
+                if not self.active:
+                    self.rejected.append(job)
+                else:
+                    self.waiting.insert(0, job)
+                return
+            job.error = None
+            job.bytes = need
+            job.admitted = now
+            self.used += need
+            self.active.append(job)
+
+    def _finish(self, job: Job, now: float) -> None:
+        job.finished = now
+        self.backend.destroy(job.handle)
+        job.handle = None
+        self.used -= job.bytes
+        self.active.remove(job)
+        self.done.append(job)
+
+    def run(self, jobs, drain_limit: float = float("inf")) -> dict:
+        pending = sorted(jobs, key=lambda j: j.arrival)
+        t0 = self.clock()
+        k = 0
+        last_arrival = pending[-1].arrival if pending else 0.0
+        while k < len(pending) or self.waiting or self.active:
+            now = self.clock() - t0
+            while k < len(pending) and pending[k].arrival <= now:
+                self.waiting.append(pending[k])
+                k += 1
+            self._admit(now)
+            if now > last_arrival + drain_limit:
+                break
+            if not self.active:
+                if k < len(pending):  # idle until the next arrival
+                    self.sleep(max(0.0, pending[k].arrival - now))
+                elif self.waiting:  # nothing resident and nothing admissible
+                    for j in self.waiting:
+                        j.error = j.error or "could not be admitted"
+                    self.rejected.extend(self.waiting)
+                    self.waiting.clear()
+                continue
+            # every resident job advances to its next output or its end
+            n = [min(j.next_event(self.out_every), self.max_quantum) for j in self.active]
+            self.backend.step([j.handle for j in self.active], n)
+            self.batch_calls += 1
+            now = self.clock() - t0
+            for j, s in zip(list(self.active), n):
+                j.done_steps += s
+                self.site_updates += s * j.sites
+                if j.done_steps % self.out_every == 0 or j.done_steps == j.steps:
+                    j.last_fields = self.backend.fields(j.handle)
+                    j.outputs += 1
+                if j.done_steps == j.steps:
+                    self._finish(j, self.clock() - t0)
+        elapsed = self.clock() - t0
+        return self.report(jobs, elapsed)
+
+    def report(self, jobs, elapsed: float) -> dict:
+        lat = np.array([j.finished - j.arrival for j in self.done]) if self.done else np.zeros(0)
+        return {
+            "jobs": len(jobs), "completed": len(self.done), "rejected": len(self.rejected),
+            "backlog": len(jobs) - len(self.done) - len(self.rejected),
+            "elapsed_s": elapsed, "site_updates": self.site_updates,
+            "sustained_gsite_updates_s": self.site_updates / elapsed / 1e9 if elapsed else 0.0,
+            "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
+            "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
+            "batch_calls": self.batch_calls,
+        }
+
+
+def fcfs_baseline(jobs, step_time) -> dict:
+    """First-come-first-served single-lattice execution of the same jobs: one
+    job at a time, each taking steps * step_time(job) seconds (step times of
+    the plain kernel measured on the GPU), queueing simulated exactly."""
+    t, lat, busy = 0.0, [], 0.0
+    for j in sorted(jobs, key=lambda j: j.arrival):
+        start = max(t, j.arrival)
+        service = j.steps * step_time(j)
+        t = start + service
+        busy += service
+        lat.append(t - j.arrival)
+    lat = np.array(lat)
+    total = sum(j.steps * j.sites for j in jobs)
+    return {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "makespan_s": t, "sustained_gsite_updates_s": total / t / 1e9 if t else 0.0}
+
+
+class StepTimeTable:
+    """Per-step time of the plain single-lattice kernel by (model, W, H),
+    measured once per shape class on the GPU and interpolated by site count."""
+
+    def __init__(self, samples_per_model=(256, 512, 1024, 2048, 4096, 8192), steps: int = 30):
+        import lgca_gb300 as gpu
+        self.table = {}
+        for m in range(4):
+            pts = []
+            for s in samples_per_model:
+                W, H = s, max(256, s // 2)
+                L = gpu.GpuLattice(m, W, H, seed=1)
+                L.init_random(0.25, 0.25)
+                L.set_kernel_variant(1)
+                L.collide_and_propagate(5)
+                L.sync()
+                t0 = time.perf_counter()
+                L.collide_and_propagate(steps)
+                L.sync()
+                pts.append((W * H, (time.perf_counter() - t0) / steps))
+                L.close()
+            self.table[m] = pts
+
+    def __call__(self, job: Job) -> float:
+        pts = self.table[job.model]
+        xs = np.log([p[0] for p in pts])
+        ys = np.log([p[1] for p in pts])
+        return float(np.exp(np.interp(math.log(job.sites), xs, ys)))
+
+
+def verify_sample(jobs, n: int = 8, block: int = 16, seed: int = 0) -> bool:
+    """Rerun a sample of completed jobs alone with the plain kernel: their
+    final fields must equal the served ones."""
+    import lgca_gb300 as gpu
+    rng = np.random.default_rng(seed)
+    done = [j for j in jobs if j.finished is not None]
+    pick = [done[i] for i in rng.choice(len(done), size=min(n, len(done)), replace=False)]
+    backend = GpuBackend(block)
+    ok = True
+    for j in pick:
+        L = backend.create(j)
+        backend.batch.remove(L)
+        L.set_kernel_variant(1)
+        L.collide_and_propagate(j.steps)
+        f = L.block_sums(block)
+        ok &= all(np.array_equal(a, b) for a, b in zip(f, j.last_fields))
+        L.close()
+    backend.close()
+    return ok
+
+
+def serve(rate: float, duration: float, budget: float = 150e9, drain_limit: float = 60.0,
+          verify: int = 8, fcfs: bool = True, **job_kw) -> dict:
+    jobs = make_jobs(rate, duration, **job_kw)
+    backend = GpuBackend()
+    srv = Server(backend, budget=budget)
+    rep = srv.run(jobs, drain_limit=drain_limit)
+    backend.close()
+    rep.update(rate=rate, duration=duration)
+    if fcfs:
+        base = fcfs_baseline(jobs, StepTimeTable())
+        rep["fcfs"] = base
+        if rep["p50_latency_s"] and base["p50_latency_s"]:
+            rep["p50_speedup_vs_fcfs"] = base["p50_latency_s"] / rep["p50_latency_s"]
+        rep["throughput_speedup_vs_fcfs"] = (rep["sustained_gsite_updates_s"] /
+                                             base["sustained_gsite_updates_s"])
+    if verify:
+        rep["sample_bit_exact"] = verify_sample(srv.done, verify)
+    return rep
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rate", type=float, nargs="+", default=[50.0])
+    ap.add_argument("--duration", type=float, default=60.0)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--drain", type=float, default=60.0)
+    ap.add_argument("--verify", type=int, default=8)
+    a = ap.parse_args(argv)
+    import lgca_gb300 as gpu
+    gpu.build()
+    for r in a.rate:
+        print(json.dumps(serve(r, a.duration, a.budget_gb * 1e9, a.drain, a.verify)), flush=True)
+
+
+if __name__ == "__main__":
+    main()
+
+__all__ = ["Job", "Server", "GpuBackend", "make_jobs", "lattice_bytes", "fcfs_baseline", "serve"]

@@ -1,0 +1,129 @@
+"""Serving loop.  CPU tests drive the scheduler with a fake backend and a
+simulated clock: admission against the memory budget, rejection of jobs that
+can never fit, a failing allocation (host-side fault injection), output
+cadence, latency accounting and the FCFS baseline.  The GPU test runs a short
+served stream and checks that sampled jobs give the same fields alone."""
+import pytest
+
+from lgca_gb300 import serve as S
+
+
+class FakeClock:
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        return self.t
+
+    def sleep(self, dt):
+        self.t += dt
+
+
+class FakeBackend:
+    """Counts steps; each step call costs 1 ms of simulated time per 1e6
+    site-steps; create can be made to fail."""
+
+    def __init__(self, clock, fail_first=()):
+        self.clock, self.fail = clock, set(fail_first)
+        self.live, self.peak_live, self.created = set(), 0, []
+
+    def create(self, job):
+        if job.index in self.fail:
+            self.fail.discard(job.index)
+            raise MemoryError("injected allocation failure")
+        h = {"job": job.index, "steps": 0, "sites": job.sites}
+        self.live.add(job.index)
+        self.peak_live = max(self.peak_live, len(self.live))
+        self.created.append(job.index)
+        return h
+
+    def step(self, handles, nsteps):
+        work = 0
+        for h, n in zip(handles, nsteps):
+            h["steps"] += n
+            work += n * h["sites"]
+        self.clock.t += 1e-3 * work / 1e6 + 1e-4
+
+    def fields(self, h):
+        return (h["steps"],)
+
+    def destroy(self, h):
+        self.live.discard(h["job"])
+
+
+def jobs_small(n=40, rate=200.0, seed=1):
+    return S.make_jobs(rate, 10.0, rng_seed=seed, w_range=(64, 512), h_range=(64, 512),
+                       steps_range=(10, 3000), max_jobs=n)
+
+
+def test_budget_admission_and_completion():
+    clock = FakeClock()
+    be = FakeBackend(clock)
+    jobs = jobs_small()
+    budget = 3 * max(S.lattice_bytes(j.model, j.W, j.H, j.geometry) for j in jobs)
+    srv = S.Server(be, budget=budget, clock=clock, sleep=clock.sleep)
+    used_max = [0]
+    orig = srv._admit
+
+    def admit(now):
+        orig(now)
+        used_max[0] = max(used_max[0], srv.used)
+        assert srv.used <= budget
+
+    srv._admit = admit
+    rep = srv.run(jobs)
+    assert rep["completed"] == len(jobs) and rep["rejected"] == 0 and rep["backlog"] == 0
+    assert used_max[0] <= budget and srv.used == 0 and not be.live
+    for j in jobs:
+        assert j.done_steps == j.steps
+        assert j.outputs == -(-j.steps // 500)  # every 500 steps and at the end
+        assert j.last_fields == (j.steps,)
+        assert j.finished >= j.arrival and j.admitted >= j.arrival
+    assert rep["p99_latency_s"] >= rep["p50_latency_s"] > 0
+
+
+def test_job_larger_than_budget_is_rejected():
+    clock = FakeClock()
+    jobs = jobs_small(5)
+    big = max(jobs, key=lambda j: j.sites)
+    budget = S.lattice_bytes(big.model, big.W, big.H, big.geometry) - 1
+    rep = S.Server(FakeBackend(clock), budget=budget, clock=clock, sleep=clock.sleep).run(jobs)
+    assert rep["rejected"] >= 1 and rep["completed"] + rep["rejected"] == len(jobs)
+
+
+def test_failed_allocation_is_retried():
+    clock = FakeClock()
+    jobs = jobs_small(12)
+    be = FakeBackend(clock, fail_first={3, 7})
+    rep = S.Server(be, budget=1e12, clock=clock, sleep=clock.sleep).run(jobs)
+    assert rep["completed"] + rep["rejected"] == len(jobs)
+    assert be.created.count(3) <= 1 and be.created.count(7) <= 1
+
+
+def test_fcfs_baseline_queueing():
+    jobs = [S.Job(index=i, arrival=float(i), model=0, W=64, H=64, geometry="periodic", p=0.2,
+                  steps=100, seed=i) for i in range(3)]
+    base = S.fcfs_baseline(jobs, lambda j: 0.02)  # 2 s per job, arrivals 1 s apart
+    assert base["makespan_s"] == pytest.approx(6.0)
+    assert base["p50_latency_s"] == pytest.approx(3.0)
+
+
+def test_job_stream_shapes():
+    jobs = S.make_jobs(100.0, 5.0, rng_seed=3)
+    assert all(j.W % 64 == 0 and j.H % 64 == 0 and 256 <= j.W <= 8192 and 256 <= j.H <= 4096
+               for j in jobs)
+    assert all(100 <= j.steps <= 20000 for j in jobs)
+    assert [j.seed for j in jobs] == list(range(len(jobs)))
+    assert 300 < len(jobs) < 700
+
+
+@pytest.mark.gpu
+def test_short_served_stream_is_bit_exact(gpu):
+    jobs = S.make_jobs(40.0, 1.5, rng_seed=11, w_range=(256, 1024), h_range=(256, 512),
+                       steps_range=(100, 1500))
+    backend = S.GpuBackend()
+    srv = S.Server(backend, budget=20e9)
+    rep = srv.run(jobs)
+    backend.close()
+    assert rep["completed"] == len(jobs)
+    assert S.verify_sample(srv.done, n=6)
