@@ -281,7 +281,7 @@ def run_ours(args):
     achieved = bytes_launch / launch_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": profiled_traffic("step_fhp3_karman_8192x2048.md"),
-                "peak_kind": peak_kind, "kernel": "k_step<FHP_II/III, GEOM_NOSLIP>",
+                "peak_kind": peak_kind, "kernel": "k_step2<FHP_II/III, GEOM_NOSLIP> (two words per lane)",
                 "bytes_per_launch": bytes_launch,
                 "note": "state (2 x 14.7 MB) + solid plane stay L2-resident within a step chunk"}
 

@@ -62,6 +62,13 @@ int lgca_create(int model, int dim_x, int dim_y, uint64_t seed, lgca_handle *out
 /* Replaces: OMP_Lattice<M>::~OMP_Lattice + free_memory (src/omp_lattice.cpp:91-97,474-489). */
 int lgca_destroy(lgca_handle h);
 
+/* Lattice device memory comes from a per-device stream-ordered pool that
+ * keeps freed blocks for the next lattice (no device-wide wait when lattices
+ * are created or destroyed).  Return unused pool memory beyond keep_bytes to
+ * the driver.  (No reference counterpart: the reference frees with
+ * cudaFree/delete in free_memory.) */
+int lgca_trim_memory(int device, uint64_t keep_bytes);
+
 /* Dimensions, model, seed and step counter of a handle. */
 int lgca_info(lgca_handle h, int *model, int *dim_x, int *dim_y, uint64_t *seed,
               uint64_t *step);
@@ -76,6 +83,26 @@ int lgca_set_step(lgca_handle h, uint64_t t);
  * apply_bc_* (src/lattice.cpp:221-395), which build that map on the host. */
 int lgca_set_cell_types(lgca_handle h, const int32_t *types);
 int lgca_get_cell_types(lgca_handle h, int32_t *types);
+
+/* Shapes of lgca_paint_cells. */
+typedef enum {
+    LGCA_SHAPE_RECT = 0,       /* a <= x < c and b <= y < d (clipped to the lattice) */
+    LGCA_SHAPE_DISC = 1,       /* (x-a)^2 + (y-b)^2 < c^2, exact integers */
+    LGCA_SHAPE_DISC_FLOAT = 2  /* float(sqrt(dx^2 + dy^2)) < c / 2.0 with dx = x-a, dy = y-b:
+                                  the obstacle of diameter c of apply_bc_karman_vortex_street */
+} lgca_shape;
+
+/* Set every cell of a shape to `type`, on the device and in stream order
+ * (no host map, no wait).  Replaces apply_cell_type_all and
+ * apply_boundary_cell_type_{north,south,east,west} (src/lattice.cpp:337-398;
+ * rectangles) and the obstacle loop of apply_bc_karman_vortex_street
+ * (src/lattice.cpp:252-280; LGCA_SHAPE_DISC_FLOAT), so that apply_bc_pipe,
+ * _karman_vortex_street and _reflecting are a few calls.  |a|, |b|, |c|, |d|
+ * must be below 2^29 and c >= 0 for discs.  The boundary kernels chosen
+ * afterwards assume that every painted type may be present (painting FLUID
+ * over all walls keeps the wall-aware kernels, which give the same result). */
+int lgca_paint_cells(lgca_handle h, int shape, int32_t type, int64_t a, int64_t b, int64_t c,
+                     int64_t d);
 
 /* Whole state in the reference byte format: dim_x*dim_y bytes, bit d =
  * channel d.  Bits >= NUM_DIR are ignored on upload and zero on download.
@@ -151,6 +178,10 @@ int lgca_mean_velocity(lgca_handle h, float *ux, float *uy);
  * src/omp_lattice.cpp:397-454. */
 int lgca_block_sums(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32_t *Jy);
 int lgca_block_sums_device(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32_t *Jy);
+/* As lgca_block_sums into host buffers, without waiting: the values are in
+ * place after lgca_sync(h).  Host buffers should be pinned for the copies to
+ * overlap; at most one outstanding call per handle before lgca_sync. */
+int lgca_block_sums_async(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32_t *Jy);
 
 /* Post-processing with the reference's arithmetic: per-cell density and FP32
  * momentum (dim_x*dim_y and 2*dim_x*dim_y floats, momentum interleaved x,y)

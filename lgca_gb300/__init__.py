@@ -20,6 +20,7 @@ from . import _build
 
 HPP, FHP_I, FHP_II, FHP_III = 0, 1, 2, 3
 FLUID, SOLID_NO_SLIP, SOLID_SLIP = 0, 1, 2
+SHAPE_RECT, SHAPE_DISC, SHAPE_DISC_FLOAT = 0, 1, 2
 NUM_DIR = {HPP: 4, FHP_I: 6, FHP_II: 7, FHP_III: 7}
 MODEL_NAMES = {"HPP": HPP, "FHP_I": FHP_I, "FHP_II": FHP_II, "FHP_III": FHP_III}
 
@@ -58,8 +59,11 @@ def lib() -> C.CDLL:
             "lgca_info": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                     C.POINTER(u64), C.POINTER(u64)]),
             "lgca_set_step": (C.c_int, [vp, u64]),
+            "lgca_trim_memory": (C.c_int, [C.c_int, u64]),
             "lgca_set_cell_types": (C.c_int, [vp, vp]),
             "lgca_get_cell_types": (C.c_int, [vp, vp]),
+            "lgca_paint_cells": (C.c_int, [vp, C.c_int, C.c_int32, C.c_int64, C.c_int64,
+                                           C.c_int64, C.c_int64]),
             "lgca_upload_state": (C.c_int, [vp, vp]),
             "lgca_download_state": (C.c_int, [vp, vp]),
             "lgca_init_random": (C.c_int, [vp, C.c_double, C.c_double]),
@@ -74,6 +78,7 @@ def lib() -> C.CDLL:
             "lgca_mean_velocity": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
             "lgca_block_sums": (C.c_int, [vp, C.c_int, vp, vp, vp]),
             "lgca_block_sums_device": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+            "lgca_block_sums_async": (C.c_int, [vp, C.c_int, vp, vp, vp]),
             "lgca_post_process": (C.c_int, [vp, C.c_int, vp, vp, vp, vp]),
             "lgca_sync": (C.c_int, [vp]),
             "lgca_stream": (vp, [vp]),
@@ -119,6 +124,11 @@ def _check(h, status: int) -> None:
     if status != 0:
         msg = lib().lgca_last_error(h).decode(errors="replace")
         raise LgcaError(status, msg)
+
+
+def trim_memory(device: int = 0, keep_bytes: int = 0) -> None:
+    """Return the lattice memory pool's unused blocks beyond keep_bytes."""
+    _check(None, lib().lgca_trim_memory(int(device), int(keep_bytes)))
 
 
 class GpuLattice:
@@ -168,6 +178,40 @@ class GpuLattice:
         t = np.empty(self.shape, np.int32)
         _check(self._h, lib().lgca_get_cell_types(self._h, _ptr(t)))
         return t
+
+    def paint_cells(self, shape: int, cell_type: int, a: int, b: int, c: int = 0,
+                    d: int = 0) -> None:
+        """Set the cells of a shape to one type on the device (see
+        lgca_paint_cells): rectangle [a, c) x [b, d), integer disc centre
+        (a, b) radius c, or the reference's float disc of diameter c."""
+        _check(self._h, lib().lgca_paint_cells(self._h, int(shape), int(cell_type), int(a), int(b),
+                                               int(c), int(d)))
+
+    # the reference's geometry setters (src/lattice.cpp:222-335), painted on the device
+    def apply_bc_periodic(self) -> None:
+        self.paint_cells(SHAPE_RECT, FLUID, 0, 0, self.dim_x, self.dim_y)
+
+    def apply_bc_pipe(self) -> None:
+        W, H = self.dim_x, self.dim_y
+        self.apply_bc_periodic()
+        self.paint_cells(SHAPE_RECT, SOLID_NO_SLIP, 0, H - 1, W, H)  # north
+        self.paint_cells(SHAPE_RECT, SOLID_NO_SLIP, 0, 0, W, 1)  # south
+
+    def apply_bc_karman_vortex_street(self) -> None:
+        self.apply_bc_pipe()
+        self.paint_cells(SHAPE_DISC_FLOAT, SOLID_NO_SLIP, self.dim_x // 6, self.dim_y // 2,
+                         self.dim_y // 3)
+
+    def apply_bc_reflecting(self, bounce_type: str) -> None:
+        if bounce_type not in ("back", "forward"):
+            raise ValueError(f"invalid bounce type {bounce_type!r}")
+        ct = SOLID_NO_SLIP if bounce_type == "back" else SOLID_SLIP
+        W, H = self.dim_x, self.dim_y
+        self.apply_bc_periodic()
+        self.paint_cells(SHAPE_RECT, ct, W - 1, 0, W, H)  # east
+        self.paint_cells(SHAPE_RECT, ct, 0, H - 1, W, H)  # north
+        self.paint_cells(SHAPE_RECT, ct, 0, 0, 1, H)  # west
+        self.paint_cells(SHAPE_RECT, ct, 0, 0, W, 1)  # south
 
     def upload(self, state: np.ndarray) -> None:
         s = np.ascontiguousarray(state, dtype=np.uint8)
@@ -236,6 +280,10 @@ class GpuLattice:
         Jy = np.empty_like(N)
         _check(self._h, lib().lgca_block_sums(self._h, int(B), _ptr(N), _ptr(Jx2), _ptr(Jy)))
         return N, Jx2, Jy
+
+    def block_sums_async(self, B: int, N: np.ndarray, Jx2: np.ndarray, Jy: np.ndarray) -> None:
+        """Enqueue block sums into host arrays (pinned for overlap); valid after sync()."""
+        _check(self._h, lib().lgca_block_sums_async(self._h, int(B), _ptr(N), _ptr(Jx2), _ptr(Jy)))
 
     def block_sums_device(self, B: int, N_ptr: int, Jx2_ptr: int, Jy_ptr: int) -> None:
         _check(self._h, lib().lgca_block_sums_device(self._h, int(B), _ptr(N_ptr), _ptr(Jx2_ptr),

@@ -21,7 +21,6 @@ import time
 import numpy as np
 
 import lgca_gb300 as gpu
-from lgca_gb300 import geometry as G
 from lgca_gb300.autotune import Autotuner
 
 GEOMETRIES = ("periodic", "pipe", "disc")
@@ -47,10 +46,10 @@ def build(job) -> "gpu.GpuLattice":
     W, H = job["W"], job["H"]
     L = gpu.GpuLattice(job["model"], W, H, seed=job["seed"])
     if job["geometry"] == "pipe":
-        L.set_cell_types(G.pipe(W, H))
+        L.apply_bc_pipe()
         L.set_forcing_column(8, 0.01)
     elif job["geometry"] == "disc":
-        L.set_cell_types(G.disc(W, H, W // 8, H // 2, max(1, H // 16), walls=False))
+        L.paint_cells(gpu.SHAPE_DISC, gpu.SOLID_NO_SLIP, W // 8, H // 2, max(1, H // 16))
     L.init_random(job["p"], job["p"])
     return L
 

@@ -167,6 +167,54 @@ cudaError_t launch_planes_to_types(const PlaneGeom &g, const uint64_t *solid, co
     return cudaGetLastError();
 }
 
+// Painting: every cell of a shape gets one type, on the device.  The mask of
+// a word holds the cells of that word inside the shape; the solid bit is set
+// for SOLID_NO_SLIP, the slip bit for SOLID_SLIP, and both are cleared for
+// FLUID.  Shapes: rectangle [a, c) x [b, d); disc (x-a)^2 + (y-b)^2 < c^2 in
+// 64-bit integers; disc of diameter c with the distance taken as
+// float(sqrt(double(dx^2 + dy^2))) and compared with c / 2.0 in double (the
+// obstacle test of Lattice::apply_bc_karman_vortex_street, with Real = float).
+__device__ __forceinline__ bool paint_in(int shape, long long x, long long y, long long a,
+                                         long long b, long long c, long long d)
+{
+    if (shape == 0) return x >= a && x < c && y >= b && y < d;
+    const long long dx = x - a, dy = y - b, r2 = dx * dx + dy * dy;
+    if (shape == 1) return r2 < c * c;
+    const float dist = (float)sqrt((double)r2);
+    return (double)dist < (double)(float)c / 2.0;
+}
+
+__global__ void k_paint(PlaneGeom g, uint64_t *__restrict__ solid, uint64_t *__restrict__ slip,
+                        int shape, int type, long long a, long long b, long long c, long long d)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)g.H * g.nw) return;
+    const int y = (int)(idx / g.nw), w = (int)(idx - (long long)y * g.nw);
+    const int x0 = 64 * w, n = min(64, g.W - x0);
+    // rows and words that cannot meet the shape: nothing to do
+    if (shape == 0) {
+        if (y < b || y >= d || x0 + n <= a || x0 >= c) return;
+    } else {
+        const long long rb = (shape == 1 ? c : c / 2) + 1;  // bound on the radius
+        if (y < b - rb || y > b + rb || x0 + n - 1 < a - rb || x0 > a + rb) return;
+    }
+    uint64_t m = 0;
+    for (int i = 0; i < n; ++i)
+        m |= (uint64_t)paint_in(shape, x0 + i, y, a, b, c, d) << i;
+    if (!m) return;
+    const size_t o = (size_t)y * g.pitch + w;
+    solid[o] = (type == 1) ? (solid[o] | m) : (solid[o] & ~m);
+    slip[o] = (type == 2) ? (slip[o] | m) : (slip[o] & ~m);
+}
+
+cudaError_t launch_paint(const PlaneGeom &g, uint64_t *solid, uint64_t *slip, int shape, int type,
+                         long long a, long long b, long long c, long long d, cudaStream_t s)
+{
+    k_paint<<<grid_for((long long)g.H * g.nw, 256), 256, 0, s>>>(g, solid, slip, shape, type, a,
+                                                                  b, c, d);
+    return cudaGetLastError();
+}
+
 __global__ void k_bytes_to_plane(PlaneGeom g, const uint8_t *__restrict__ bytes,
                                  uint64_t *__restrict__ plane)
 {

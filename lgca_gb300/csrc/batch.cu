@@ -74,6 +74,11 @@ __global__ void k_advance(int *s_base, int by)
     if (threadIdx.x == 0 && blockIdx.x == 0) *s_base += by;
 }
 
+__global__ void k_set_base(int *s_base, int v)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) *s_base = v;
+}
+
 cudaError_t launch_batch(const BatchEntry *E, const int *prefix, const int *block_lat,
                          int n_active, int total_tasks, int s_local, const int *s_base,
                          cudaStream_t st)
@@ -89,6 +94,12 @@ cudaError_t launch_batch_keys(const BatchEntry *E, int n, int max_steps, cudaStr
     const long long work = (long long)n * max_steps;
     if (work <= 0) return cudaSuccess;
     k_batch_keys<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(E, n, max_steps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_base(int *s_base, int v, cudaStream_t st)
+{
+    k_set_base<<<1, 32, 0, st>>>(s_base, v);
     return cudaGetLastError();
 }
 

@@ -65,6 +65,7 @@ cudaError_t launch_batch(const BatchEntry *E, const int *prefix, const int *bloc
                          cudaStream_t stream);
 cudaError_t launch_batch_keys(const BatchEntry *E, int n, int max_steps, cudaStream_t stream);
 cudaError_t launch_advance(int *s_base, int by, cudaStream_t stream);
+cudaError_t launch_set_base(int *s_base, int v, cudaStream_t stream);
 
 // One lattice step of `a` (k = 1), launched on `stream`.
 cudaError_t launch_step(int model, int geom_mode, const StepArgs &a, cudaStream_t stream);
@@ -112,6 +113,8 @@ cudaError_t launch_planes_to_aos(int D, const PlaneGeom &g, const uint64_t *plan
 // Cell types (int32) -> solid / slip planes; *bad set to 1 on invalid values.
 cudaError_t launch_types_to_planes(const PlaneGeom &g, const int32_t *types, uint64_t *solid,
                                    uint64_t *slip, int *bad, cudaStream_t s);
+cudaError_t launch_paint(const PlaneGeom &g, uint64_t *solid, uint64_t *slip, int shape, int type,
+                         long long a, long long b, long long c, long long d, cudaStream_t s);
 cudaError_t launch_planes_to_types(const PlaneGeom &g, const uint64_t *solid, const uint64_t *slip,
                                    int32_t *types, cudaStream_t s);
 // Bernoulli initial occupation (fluid cells only).

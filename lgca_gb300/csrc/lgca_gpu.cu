@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -81,23 +82,82 @@ struct DeviceGuard {
     }
 };
 
+// Lattice memory comes from one stream-ordered pool per device that keeps
+// freed blocks for reuse: lattices are created and destroyed while others
+// run without synchronising the device or returning memory to the driver
+// (lgca_trim_memory hands unused blocks back).
+constexpr int MAX_DEVICES = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[MAX_DEVICES] = {};
+
+cudaError_t lattice_pool(int dev, cudaMemPool_t *out)
+{
+    if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pool[dev]) {
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t p = nullptr;
+        cudaError_t e = cudaMemPoolCreate(&p, &props);
+        if (e != cudaSuccess) return e;
+        uint64_t keep = ~0ull;
+        e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+        if (e != cudaSuccess) {
+            cudaMemPoolDestroy(p);
+            return e;
+        }
+        g_pool[dev] = p;
+    }
+    *out = g_pool[dev];
+    return cudaSuccess;
+}
+
+// stream-ordered allocation on the handle's stream (zeroed when asked)
+int dalloc(lgca_lattice *h, void **p, size_t bytes, bool zero, const char *what)
+{
+    cudaMemPool_t pool;
+    cudaError_t e = lattice_pool(h->device, &pool);
+    if (e == cudaSuccess) e = cudaMallocFromPoolAsync(p, bytes, pool, h->stream);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(h, e, what);
+    }
+    if (zero && (e = cudaMemsetAsync(*p, 0, bytes, h->stream)) != cudaSuccess)
+        return cuda_fail(h, e, what);
+    h->bytes += bytes;
+    return LGCA_OK;
+}
+
+void dfree(lgca_lattice *h, void *p)
+{
+    if (p) cudaFreeAsync(p, h->stream);
+}
+
+int geometry_planes(lgca_lattice *h)
+{
+    if (h->solid) return LGCA_OK;
+    const size_t plane_bytes = h->g.ps * sizeof(uint64_t);
+    int st = dalloc(h, reinterpret_cast<void **>(&h->solid), plane_bytes, true, "solid plane");
+    if (st == LGCA_OK)
+        st = dalloc(h, reinterpret_cast<void **>(&h->slip), plane_bytes, true, "slip plane");
+    return st;
+}
+
 int scratch_reserve(lgca_lattice *h, size_t bytes)
 {
     if (h->scratch_bytes >= bytes) return LGCA_OK;
     if (h->scratch) {
-        cudaStreamSynchronize(h->stream);
-        cudaFree(h->scratch);
+        dfree(h, h->scratch);  // in stream order after its last use
         h->bytes -= h->scratch_bytes;
         h->scratch = nullptr;
         h->scratch_bytes = 0;
     }
-    cudaError_t e = cudaMalloc(&h->scratch, bytes);
-    if (e != cudaSuccess) {
-        h->scratch = nullptr;
-        return cuda_fail(h, e, "cudaMalloc(scratch)");
-    }
+    int st = dalloc(h, &h->scratch, bytes, false, "scratch");
+    if (st) return st;
     h->scratch_bytes = bytes;
-    h->bytes += bytes;
     return LGCA_OK;
 }
 
@@ -177,18 +237,19 @@ int lgca_create(int model, int W, int H, uint64_t seed, lgca_handle *out)
     }
     h->stream = h->own_stream;
     const size_t state_bytes = (size_t)h->D * g.ps * sizeof(uint64_t);
-    for (int i = 0; i < 2; ++i) {
-        e = cudaMalloc(&h->buf[i], state_bytes);
-        if (e == cudaSuccess) e = cudaMemsetAsync(h->buf[i], 0, state_bytes, h->stream);
-        if (e != cudaSuccess) {
-            int st = cuda_fail(nullptr, e, "cudaMalloc(state)");
-            cudaFree(h->buf[0]);
-            cudaFree(h->buf[1]);
-            cudaStreamDestroy(h->own_stream);
-            delete h;
-            return st;
-        }
-        h->bytes += state_bytes;
+    int st = LGCA_OK;
+    for (int i = 0; i < 2 && st == LGCA_OK; ++i)
+        st = dalloc(h, reinterpret_cast<void **>(&h->buf[i]), state_bytes, true, "state buffer");
+    // the buffers are usable from any stream once this returns
+    if (st == LGCA_OK && (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
+        st = cuda_fail(h, e, "cudaStreamSynchronize");
+    if (st != LGCA_OK) {
+        dfree(h, h->buf[0]);
+        dfree(h, h->buf[1]);
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->own_stream);
+        delete h;
+        return st;
     }
     *out = h;
     return LGCA_OK;
@@ -198,18 +259,25 @@ int lgca_destroy(lgca_handle h)
 {
     if (!h) return LGCA_OK;
     DeviceGuard dg(h->device);
-    if (h->stream) cudaStreamSynchronize(h->stream);
-    cudaFree(h->buf[0]);
-    cudaFree(h->buf[1]);
-    cudaFree(h->solid);
-    cudaFree(h->slip);
-    cudaFree(h->chir);
-    cudaFree(h->scratch);
-    cudaFree(h->sync);
-    if (h->sync_err_host) cudaFreeHost(h->sync_err_host);
+    // memory goes back to the pool in stream order, after the handle's queued
+    // work (batch steps of a member are ordered before it); no host wait
+    void *mem[] = {h->buf[0], h->buf[1], h->solid, h->slip, h->chir, h->scratch, h->sync};
+    for (void *p : mem) dfree(h, p);
+    if (h->sync_err_host) {
+        cudaStreamSynchronize(h->stream);
+        cudaFreeHost(h->sync_err_host);
+    }
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return LGCA_OK;
+}
+
+int lgca_trim_memory(int device, uint64_t keep_bytes)
+{
+    cudaMemPool_t pool;
+    cudaError_t e = lattice_pool(device, &pool);
+    if (e == cudaSuccess) e = cudaMemPoolTrimTo(pool, (size_t)keep_bytes);
+    return e == cudaSuccess ? LGCA_OK : cuda_fail(nullptr, e, "cudaMemPoolTrimTo");
 }
 
 int lgca_info(lgca_handle h, int *model, int *W, int *H, uint64_t *seed, uint64_t *step)
@@ -246,13 +314,9 @@ int lgca_set_cell_types(lgca_handle h, const int32_t *types)
         any_noslip |= (t == 1);
         any_slip |= (t == 2);
     }
-    const size_t plane_bytes = g.ps * sizeof(uint64_t);
-    if (!h->solid) {
-        CK(h, cudaMalloc(&h->solid, plane_bytes));
-        CK(h, cudaMalloc(&h->slip, plane_bytes));
-        CK(h, cudaMemsetAsync(h->solid, 0, plane_bytes, h->stream));
-        CK(h, cudaMemsetAsync(h->slip, 0, plane_bytes, h->stream));
-        h->bytes += 2 * plane_bytes;
+    {
+        int gst = geometry_planes(h);
+        if (gst) return gst;
     }
     int st = scratch_reserve(h, n * sizeof(int32_t) + 256);
     if (st) return st;
@@ -264,6 +328,30 @@ int lgca_set_cell_types(lgca_handle h, const int32_t *types)
     CK(h, cudaStreamSynchronize(h->stream));
     h->has_noslip = any_noslip;
     h->has_slip = any_slip;
+    return LGCA_OK;
+}
+
+int lgca_paint_cells(lgca_handle h, int shape, int32_t type, int64_t a, int64_t b, int64_t c,
+                     int64_t d)
+{
+    CHECK_HANDLE(h);
+    if (shape < LGCA_SHAPE_RECT || shape > LGCA_SHAPE_DISC_FLOAT)
+        return fail(h, LGCA_ERR_INVALID, "unknown shape %d", shape);
+    if (type < LGCA_FLUID || type > LGCA_SOLID_SLIP)
+        return fail(h, LGCA_ERR_INVALID, "invalid cell type %d", type);
+    const int64_t lim = 1ll << 29;
+    if (a <= -lim || a >= lim || b <= -lim || b >= lim || c <= -lim || c >= lim || d <= -lim ||
+        d >= lim || (shape != LGCA_SHAPE_RECT && c < 0))
+        return fail(h, LGCA_ERR_INVALID, "shape parameters out of range");
+    DeviceGuard dg(h->device);
+    if (!h->solid) {
+        if (type == LGCA_FLUID) return LGCA_OK;  // no geometry planes yet: all cells are fluid
+        int gst = geometry_planes(h);
+        if (gst) return gst;
+    }
+    CK(h, launch_paint(h->g, h->solid, h->slip, shape, type, a, b, c, d, h->stream));
+    h->has_noslip |= (type == LGCA_SOLID_NO_SLIP);
+    h->has_slip |= (type == LGCA_SOLID_SLIP);
     return LGCA_OK;
 }
 
@@ -359,9 +447,9 @@ int lgca_set_chirality(lgca_handle h, const uint8_t *field)
     }
     const size_t n = (size_t)h->g.W * h->g.H;
     if (!h->chir) {
-        CK(h, cudaMalloc(&h->chir, h->g.ps * sizeof(uint64_t)));
-        CK(h, cudaMemsetAsync(h->chir, 0, h->g.ps * sizeof(uint64_t), h->stream));
-        h->bytes += h->g.ps * sizeof(uint64_t);
+        int cst = dalloc(h, reinterpret_cast<void **>(&h->chir), h->g.ps * sizeof(uint64_t), true,
+                         "chirality plane");
+        if (cst) return cst;
     }
     int st = scratch_reserve(h, n + 64);
     if (st) return st;
@@ -406,10 +494,10 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     if (h->variant == VARIANT_PERSIST && nsteps > 1) {
         const size_t sync_bytes = (size_t)(PERSIST_MAX_BLOCKS + 1) * sizeof(int);
         if (!h->sync) {
-            CK(h, cudaMalloc(&h->sync, sync_bytes));
+            int sst = dalloc(h, reinterpret_cast<void **>(&h->sync), sync_bytes, false, "flags");
+            if (sst) return sst;
             CK(h, cudaHostAlloc(&h->sync_err_host, sizeof(int), cudaHostAllocDefault));
             *h->sync_err_host = 0;
-            h->bytes += sync_bytes;
         }
         CK(h, cudaMemsetAsync(h->sync, 0, sync_bytes, h->stream));
         CK(h, launch_persistent(h->model, gm, a, h->buf[h->cur], h->buf[h->cur ^ 1], h->seed, h->t,
@@ -544,6 +632,22 @@ int lgca_block_sums(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32_t *Jy)
     CK(h, cudaMemcpyAsync(Jx2, d + nb, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaMemcpyAsync(Jy, d + 2 * nb, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
+    return LGCA_OK;
+}
+
+int lgca_block_sums_async(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32_t *Jy)
+{
+    CHECK_HANDLE(h);
+    if (B < 1 || !N || !Jx2 || !Jy) return fail(h, LGCA_ERR_INVALID, "invalid block-sum arguments");
+    DeviceGuard dg(h->device);
+    const size_t nb = (size_t)((h->g.W + B - 1) / B) * ((h->g.H + B - 1) / B);
+    int st = scratch_reserve(h, 3 * nb * sizeof(int32_t));
+    if (st) return st;
+    int32_t *d = static_cast<int32_t *>(h->scratch);
+    CK(h, launch_block_sums(h->model, h->g, h->buf[h->cur], B, d, d + nb, d + 2 * nb, h->stream));
+    CK(h, cudaMemcpyAsync(N, d, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(Jx2, d + nb, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(Jy, d + 2 * nb, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     return LGCA_OK;
 }
 
@@ -700,16 +804,12 @@ int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes)
     DeviceGuard dg(h->device);
     const size_t plane_bytes = h->g.ps * sizeof(uint64_t);
     if (has_geom && !h->solid) {
-        CK(h, cudaMalloc(&h->solid, plane_bytes));
-        CK(h, cudaMalloc(&h->slip, plane_bytes));
-        CK(h, cudaMemsetAsync(h->solid, 0, plane_bytes, h->stream));
-        CK(h, cudaMemsetAsync(h->slip, 0, plane_bytes, h->stream));
-        h->bytes += 2 * plane_bytes;
+        int gst = geometry_planes(h);
+        if (gst) return gst;
     }
     if (frozen && !h->chir) {
-        CK(h, cudaMalloc(&h->chir, plane_bytes));
-        CK(h, cudaMemsetAsync(h->chir, 0, plane_bytes, h->stream));
-        h->bytes += plane_bytes;
+        int cst = dalloc(h, reinterpret_cast<void **>(&h->chir), plane_bytes, true, "chirality plane");
+        if (cst) return cst;
     }
     const char *in = static_cast<const char *>(buf) + sizeof(CkptHeader);
     auto copy_plane = [&](uint64_t *dst) -> cudaError_t {
@@ -765,6 +865,14 @@ struct lgca_batch {
     size_t capE = 0, capB = 0, capK = 0;
     std::vector<BatchEntry> E;
     std::vector<int> P, Bl, nsteps;  // nsteps per entry, descending
+    // pinned staging of the work-list, two slots used in turn; a slot is
+    // rewritten once the copies out of it (two calls back) have run
+    struct Staging {
+        void *host = nullptr;
+        size_t cap = 0;
+        cudaEvent_t copied = nullptr;
+    } stage[2];
+    int slot = 0;
     std::string err;
 };
 
@@ -803,6 +911,7 @@ int enqueue_steps(lgca_batch *b, int n_active, int tasks, int n)
 template <class T> int grow(lgca_batch *b, T *&p, size_t &cap, size_t n)
 {
     if (cap >= n) return LGCA_OK;
+    BCK(b, cudaStreamSynchronize(b->stream));  // queued steps still read the old list
     cudaFree(p);
     p = nullptr;
     cap = 0;
@@ -825,6 +934,8 @@ int lgca_batch_create(lgca_batch_handle *out)
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&b->s_base, sizeof(int));
+    for (auto &sg : b->stage)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sg.copied, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         int st = bcuda(nullptr, e, "lgca_batch_create");
         lgca_batch_destroy(b);
@@ -844,6 +955,10 @@ int lgca_batch_destroy(lgca_batch_handle b)
     cudaFree(b->dP);  // dB lives in the same allocation
     cudaFree(b->dK);
     cudaFree(b->s_base);
+    for (auto &sg : b->stage) {
+        if (sg.host) cudaFreeHost(sg.host);
+        if (sg.copied) cudaEventDestroy(sg.copied);
+    }
     if (b->done) cudaEventDestroy(b->done);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -871,7 +986,7 @@ int lgca_batch_remove(lgca_batch_handle b, lgca_handle h)
     DeviceGuard dg(b->device);
     for (size_t i = 0; i < b->members.size(); ++i) {
         if (b->members[i] == h) {
-            BCK(b, cudaStreamSynchronize(b->stream));
+            // the member's stream already waits for the batch's queued steps
             cudaEventDestroy(b->ev[i]);
             b->members.erase(b->members.begin() + i);
             b->ev.erase(b->ev.begin() + i);
@@ -903,9 +1018,8 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
     const size_t nm = b->members.size();
     for (size_t i = 0; i < nm; ++i)
         if (nsteps[i] < 0) return bfail(b, LGCA_ERR_INVALID, "negative step count");
-    // the previous batch call's kernels still read the work-lists
-    BCK(b, cudaStreamSynchronize(b->stream));
-    // order after each member's own pending work
+    // order after each member's own pending work (no host wait: the work-list
+    // copies below are queued behind the previous call's steps)
     for (size_t i = 0; i < nm; ++i) {
         if (nsteps[i] == 0) continue;
         BCK(b, cudaEventRecord(b->ev[i], b->members[i]->stream));
@@ -971,10 +1085,28 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         if ((st = grow(b, b->dK, b->capK, nkeys)) != LGCA_OK) return st;
         b->dB = b->dP + ne + 1;
         for (auto &e : b->E) e.keys = b->dK + reinterpret_cast<size_t>(e.keys);
-        // synchronous copies: the host vectors are reused by the next call
-        BCK(b, cudaMemcpy(b->dE, b->E.data(), ne * sizeof(BatchEntry), cudaMemcpyHostToDevice));
-        BCK(b, cudaMemcpy(b->dP, b->P.data(), (ne + 1) * sizeof(int), cudaMemcpyHostToDevice));
-        BCK(b, cudaMemcpy(b->dB, b->Bl.data(), nblocks * sizeof(int), cudaMemcpyHostToDevice));
+        // work-list through a pinned slot: entries, then prefix and block map
+        // (contiguous on the device as on the host)
+        auto &sg = b->stage[b->slot];
+        b->slot ^= 1;
+        BCK(b, cudaEventSynchronize(sg.copied));
+        const size_t eb = (ne * sizeof(BatchEntry) + 15) & ~(size_t)15;
+        const size_t ib = ((size_t)ne + 1 + nblocks) * sizeof(int);
+        if (sg.cap < eb + ib) {
+            if (sg.host) cudaFreeHost(sg.host);
+            sg.host = nullptr;
+            sg.cap = 0;
+            BCK(b, cudaHostAlloc(&sg.host, 2 * (eb + ib), cudaHostAllocDefault));
+            sg.cap = 2 * (eb + ib);
+        }
+        char *hp = static_cast<char *>(sg.host);
+        memcpy(hp, b->E.data(), ne * sizeof(BatchEntry));
+        memcpy(hp + eb, b->P.data(), (ne + 1) * sizeof(int));
+        memcpy(hp + eb + (ne + 1) * sizeof(int), b->Bl.data(), nblocks * sizeof(int));
+        BCK(b, cudaMemcpyAsync(b->dE, hp, ne * sizeof(BatchEntry), cudaMemcpyHostToDevice,
+                               b->stream));
+        BCK(b, cudaMemcpyAsync(b->dP, hp + eb, ib, cudaMemcpyHostToDevice, b->stream));
+        BCK(b, cudaEventRecord(sg.copied, b->stream));
         BCK(b, launch_batch_keys(b->dE, ne, max_steps, b->stream));
     }
     // segments of constant active sets: [s0, s1) where no lattice finishes
@@ -983,9 +1115,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         int k = 0;
         while (k < ne && b->nsteps[k] > s0) ++k;
         const int s1 = b->nsteps[k - 1], len = s1 - s0, tasks = b->P[k];
-        BCK(b, cudaMemcpyAsync(b->s_base, &s0, sizeof(int), cudaMemcpyHostToDevice, b->stream));
-        // the copy reads s0 from the host stack: wait for it before s0 changes
-        BCK(b, cudaStreamSynchronize(b->stream));
+        BCK(b, launch_set_base(b->s_base, s0, b->stream));
         const int G = b->graph_steps > 0 ? std::min(b->graph_steps, len) : 0;
         int done = 0;
         if (G > 1 && len >= 2 * G) {
@@ -1009,8 +1139,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
                     return bcuda(b, e, "cudaGraphLaunch");
                 }
             }
-            BCK(b, cudaStreamSynchronize(b->stream));
-            cudaGraphExecDestroy(exec);
+            cudaGraphExecDestroy(exec);  // released once its queued launches complete
         }
         if (done < len) {
             const int st = enqueue_steps(b, k, tasks, len - done);

@@ -92,23 +92,31 @@ def lattice_bytes(model: int, W: int, H: int, geometry: str) -> int:
 
 
 class GpuBackend:
-    """Runs jobs on the GPU through the C ABI (one batch for all residents)."""
+    """Runs jobs on the GPU through the C ABI (one batch for all residents).
+
+    Nothing here waits for the device except `collect`: geometry is painted
+    on the device, lattice memory comes from the engine's stream-ordered pool,
+    batch steps and field copies are queued, and a field request is tracked
+    by one event per job, so the host prepares the next batch call while the
+    device runs the current one."""
 
     def __init__(self, block: int = 16):
+        import torch
         import lgca_gb300 as gpu
-        from lgca_gb300 import geometry as G
-        self.gpu, self.G, self.block = gpu, G, block
+        self.gpu, self.torch, self.block = gpu, torch, block
         self.batch = gpu.GpuBatch()
+        self.out = {}  # (handle id, parity) -> pinned (3, Hb, Wb) int32 buffers
+        self.parity = {}
 
     def create(self, job: Job):
-        gpu, G = self.gpu, self.G
+        gpu = self.gpu
         L = gpu.GpuLattice(job.model, job.W, job.H, seed=job.seed)
         if job.geometry == "pipe":
-            L.set_cell_types(G.pipe(job.W, job.H))
+            L.apply_bc_pipe()
             L.set_forcing_column(8, 0.01)
         elif job.geometry == "disc":
-            L.set_cell_types(G.disc(job.W, job.H, job.W // 8, job.H // 2, max(1, job.H // 16),
-                                    walls=False))
+            L.paint_cells(gpu.SHAPE_DISC, gpu.SOLID_NO_SLIP, job.W // 8, job.H // 2,
+                          max(1, job.H // 16))
         L.init_random(job.p, job.p)
         self.batch.add(L)
         return L
@@ -118,11 +126,42 @@ class GpuBackend:
         counts = {id(h): n for h, n in zip(handles, nsteps)}
         self.batch.step_each([counts.get(id(m), 0) for m in self.batch.members])
 
+    def _buffers(self, handle):
+        par = self.parity.get(id(handle), 0)
+        self.parity[id(handle)] = par ^ 1  # consecutive requests use different buffers
+        key = (id(handle), par)
+        if key not in self.out:
+            Hb, Wb = -(-handle.dim_y // self.block), -(-handle.dim_x // self.block)
+            self.out[key] = self.torch.empty((3, Hb, Wb), dtype=self.torch.int32,
+                                             pin_memory=True).numpy()
+        return self.out[key]
+
+    def request_fields(self, handles):
+        """Queue every job's block sums into pinned buffers; returns a token."""
+        token = []
+        for h in handles:
+            b = self._buffers(h)
+            h.block_sums_async(self.block, b[0], b[1], b[2])
+            ev = self.torch.cuda.Event()
+            ev.record(self.torch.cuda.ExternalStream(h.stream_ptr()))
+            token.append((ev, b))
+        return token
+
+    def collect(self, token):
+        out = []
+        for ev, b in token:
+            ev.synchronize()
+            out.append((b[0].copy(), b[1].copy(), b[2].copy()))
+        return out
+
     def fields(self, handle):
-        return handle.block_sums(self.block)
+        return self.collect(self.request_fields([handle]))[0]
 
     def destroy(self, handle):
         self.batch.remove(handle)
+        self.out.pop((id(handle), 0), None)
+        self.out.pop((id(handle), 1), None)
+        self.parity.pop(id(handle), None)
         handle.close()
 
     def close(self):
@@ -131,10 +170,15 @@ class GpuBackend:
 
 class Server:
     def __init__(self, backend, budget: float = 150e9, out_every: int = 500,
-                 clock=time.perf_counter, sleep=time.sleep, max_quantum: int = 500):
+                 clock=time.perf_counter, sleep=time.sleep, max_quantum: int = 100,
+                 max_sites: float = float("inf")):
         self.backend, self.budget, self.out_every = backend, budget, out_every
         self.clock, self.sleep, self.max_quantum = clock, sleep, max_quantum
+        # slots: residents' total sites; beyond what fills the device, more
+        # residents only share it more thinly (longer latency, same throughput)
+        self.max_sites = max_sites
         self.used = 0
+        self.sites = 0
         self.active: list[Job] = []
         self.waiting: list[Job] = []
         self.done: list[Job] = []
@@ -154,6 +198,8 @@ class Server:
                 continue
             if self.used + need > self.budget:
                 return
+            if self.active and self.sites + job.sites > self.max_sites:
+                return
             self.waiting.pop(0)
             try:
                 job.handle = self.backend.create(job)
@@ -168,6 +214,7 @@ class Server:
             job.bytes = need
             job.admitted = now
             self.used += need
+            self.sites += job.sites
             self.active.append(job)
 
     def _finish(self, job: Job, now: float) -> None:
@@ -175,23 +222,60 @@ class Server:
         self.backend.destroy(job.handle)
         job.handle = None
         self.used -= job.bytes
+        self.sites -= job.sites
         self.active.remove(job)
         self.done.append(job)
 
+    def _request(self, handles):
+        req = getattr(self.backend, "request_fields", None)
+        return req(handles) if req else [self.backend.fields(h) for h in handles]
+
+    def _collect(self, token):
+        col = getattr(self.backend, "collect", None)
+        return col(token) if col else token
+
     def run(self, jobs, drain_limit: float = float("inf")) -> dict:
+        """Continuous batching, pipelined one call deep: call k's steps and
+        field copies are queued before call k-1's fields are collected, so
+        the device does not idle while the host admits, finishes and plans."""
         pending = sorted(jobs, key=lambda j: j.arrival)
         t0 = self.clock()
         k = 0
         last_arrival = pending[-1].arrival if pending else 0.0
-        while k < len(pending) or self.waiting or self.active:
+        inflight = None  # (token, jobs whose fields it carries)
+        while k < len(pending) or self.waiting or self.active or inflight:
             now = self.clock() - t0
             while k < len(pending) and pending[k].arrival <= now:
                 self.waiting.append(pending[k])
                 k += 1
             self._admit(now)
-            if now > last_arrival + drain_limit:
+            if now > last_arrival + drain_limit and inflight is None:
                 break
-            if not self.active:
+            launched = None
+            run = [j for j in self.active if j.done_steps < j.steps]
+            if run and now <= last_arrival + drain_limit:
+                # every runnable job advances to its next output, its end or a quantum
+                n = [min(j.next_event(self.out_every), self.max_quantum) for j in run]
+                self.backend.step([j.handle for j in run], n)
+                self.batch_calls += 1
+                emit = []
+                for j, s in zip(run, n):
+                    j.done_steps += s
+                    self.site_updates += s * j.sites
+                    if j.done_steps % self.out_every == 0 or j.done_steps == j.steps:
+                        emit.append((j, j.done_steps))
+                launched = (self._request([j.handle for j, _ in emit]), emit)
+            if inflight is not None:
+                token, emit = inflight
+                got = self._collect(token)
+                now = self.clock() - t0
+                for (j, at), f in zip(emit, got):
+                    j.last_fields = f
+                    j.outputs += 1
+                    if at == j.steps:
+                        self._finish(j, now)
+            inflight = launched
+            if inflight is None and not self.active:
                 if k < len(pending):  # idle until the next arrival
                     self.sleep(max(0.0, pending[k].arrival - now))
                 elif self.waiting:  # nothing resident and nothing admissible
@@ -199,20 +283,6 @@ class Server:
                         j.error = j.error or "could not be admitted"
                     self.rejected.extend(self.waiting)
                     self.waiting.clear()
-                continue
-            # every resident job advances to its next output or its end
-            n = [min(j.next_event(self.out_every), self.max_quantum) for j in self.active]
-            self.backend.step([j.handle for j in self.active], n)
-            self.batch_calls += 1
-            now = self.clock() - t0
-            for j, s in zip(list(self.active), n):
-                j.done_steps += s
-                self.site_updates += s * j.sites
-                if j.done_steps % self.out_every == 0 or j.done_steps == j.steps:
-                    j.last_fields = self.backend.fields(j.handle)
-                    j.outputs += 1
-                if j.done_steps == j.steps:
-                    self._finish(j, self.clock() - t0)
         elapsed = self.clock() - t0
         return self.report(jobs, elapsed)
 
@@ -276,35 +346,48 @@ class StepTimeTable:
         return float(np.exp(np.interp(math.log(job.sites), xs, ys)))
 
 
+def build_alone(job: Job):
+    """The job as a lone lattice, its geometry given as a host cell map (the
+    other construction path from the served one, which paints on the device)."""
+    import lgca_gb300 as gpu
+    from lgca_gb300 import geometry as G
+    L = gpu.GpuLattice(job.model, job.W, job.H, seed=job.seed)
+    if job.geometry == "pipe":
+        L.set_cell_types(G.pipe(job.W, job.H))
+        L.set_forcing_column(8, 0.01)
+    elif job.geometry == "disc":
+        L.set_cell_types(G.disc(job.W, job.H, job.W // 8, job.H // 2, max(1, job.H // 16),
+                                walls=False))
+    L.init_random(job.p, job.p)
+    return L
+
+
 def verify_sample(jobs, n: int = 8, block: int = 16, seed: int = 0) -> bool:
     """Rerun a sample of completed jobs alone with the plain kernel: their
     final fields must equal the served ones."""
-    import lgca_gb300 as gpu
     rng = np.random.default_rng(seed)
     done = [j for j in jobs if j.finished is not None]
     pick = [done[i] for i in rng.choice(len(done), size=min(n, len(done)), replace=False)]
-    backend = GpuBackend(block)
     ok = True
     for j in pick:
-        L = backend.create(j)
-        backend.batch.remove(L)
+        L = build_alone(j)
         L.set_kernel_variant(1)
         L.collide_and_propagate(j.steps)
         f = L.block_sums(block)
         ok &= all(np.array_equal(a, b) for a, b in zip(f, j.last_fields))
         L.close()
-    backend.close()
     return ok
 
 
 def serve(rate: float, duration: float, budget: float = 150e9, drain_limit: float = 60.0,
-          verify: int = 8, fcfs: bool = True, **job_kw) -> dict:
+          verify: int = 8, fcfs: bool = True, max_sites: float = float("inf"),
+          quantum: int = 100, **job_kw) -> dict:
     jobs = make_jobs(rate, duration, **job_kw)
     backend = GpuBackend()
-    srv = Server(backend, budget=budget)
+    srv = Server(backend, budget=budget, max_sites=max_sites, max_quantum=quantum)
     rep = srv.run(jobs, drain_limit=drain_limit)
     backend.close()
-    rep.update(rate=rate, duration=duration)
+    rep.update(rate=rate, duration=duration, max_sites=max_sites, quantum=quantum)
     if fcfs:
         base = fcfs_baseline(jobs, StepTimeTable())
         rep["fcfs"] = base
@@ -324,11 +407,17 @@ def main(argv=None):
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--drain", type=float, default=60.0)
     ap.add_argument("--verify", type=int, default=8)
+    ap.add_argument("--max-sites", type=float, nargs="+", default=[float("inf")],
+                    help="resident site caps to try (slots)")
+    ap.add_argument("--quantum", type=int, default=100)
+    ap.add_argument("--no-fcfs", action="store_true")
     a = ap.parse_args(argv)
     import lgca_gb300 as gpu
     gpu.build()
     for r in a.rate:
-        print(json.dumps(serve(r, a.duration, a.budget_gb * 1e9, a.drain, a.verify)), flush=True)
+        for cap in a.max_sites:
+            print(json.dumps(serve(r, a.duration, a.budget_gb * 1e9, a.drain, a.verify,
+                                   not a.no_fcfs, cap, a.quantum)), flush=True)
 
 
 if __name__ == "__main__":

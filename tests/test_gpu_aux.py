@@ -63,6 +63,25 @@ def test_block_sums_match_oracle(gpu, oracle, model, B):
         assert np.array_equal(g, w)
 
 
+@pytest.mark.parametrize("B", [1, 16, 37])
+def test_block_sums_async_after_steps(gpu, oracle, B):
+    """The non-blocking form gives the blocking form's values once the
+    handle's stream is synchronised, also when steps were queued before it."""
+    import torch
+    W, H = 640, 96
+    st = oracle.init_bernoulli(3, W, H, None, seed=5, p_move=0.3, p_rest=0.3)
+    Hb, Wb = -(-H // B), -(-W // B)
+    buf = torch.zeros((3, Hb, Wb), dtype=torch.int32, pin_memory=True).numpy()
+    with gpu.GpuLattice(3, W, H, seed=8) as L:
+        L.upload(st)
+        L.collide_and_propagate(7)
+        L.block_sums_async(B, buf[0], buf[1], buf[2])
+        L.sync()
+        want = oracle.block_sums(3, L.download(), B)
+    for g, w in zip(buf, want):
+        assert np.array_equal(g, w)
+
+
 @pytest.mark.parametrize("model", MODELS)
 def test_post_process_matches_golden_bitwise(gpu, model):
     npz = load_npz("postprocess.npz")
@@ -180,3 +199,76 @@ def test_checkpoint_resume_is_bit_exact(gpu, oracle, model):
     with gpu.GpuLattice(model, W + 64, H) as C_:
         with pytest.raises(gpu.LgcaError):
             C_.restore(blob)
+
+
+@pytest.mark.parametrize("W,H", [(64, 8), (130, 20), (777, 96), (1024, 512), (8192, 2048)])
+def test_paint_reference_geometries(gpu, W, H):
+    """Device painting gives the reference setters' cell maps exactly."""
+    with gpu.GpuLattice(2, W, H) as L:
+        L.apply_bc_pipe()
+        assert np.array_equal(L.get_cell_types(), G.pipe(W, H))
+        L.apply_bc_karman_vortex_street()
+        assert np.array_equal(L.get_cell_types(), G.karman_reference(W, H))
+        for bt in ("back", "forward"):
+            L.apply_bc_reflecting(bt)
+            assert np.array_equal(L.get_cell_types(), G.reflecting(W, H, bt))
+        L.apply_bc_periodic()
+        assert np.array_equal(L.get_cell_types(), G.periodic(W, H))
+
+
+@pytest.mark.parametrize("W,H", [(100, 40), (777, 96), (2048, 1024)])
+def test_paint_shapes_against_numpy(gpu, W, H):
+    rng = np.random.default_rng(W + H)
+    want = G.periodic(W, H)
+    y, x = np.mgrid[0:H, 0:W]
+    with gpu.GpuLattice(3, W, H) as L:
+        for k in range(12):
+            shape = int(rng.integers(3))
+            t = int(rng.integers(3))
+            a, b = int(rng.integers(-W // 4, W + W // 4)), int(rng.integers(-H // 4, H + H // 4))
+            if shape == 0:
+                c, d = a + int(rng.integers(0, W)), b + int(rng.integers(0, H))
+                m = (x >= a) & (x < c) & (y >= b) & (y < d)
+            elif shape == 1:
+                c, d = int(rng.integers(0, H)), 0
+                m = (x - a) ** 2 + (y - b) ** 2 < c * c
+            else:
+                c, d = int(rng.integers(0, H)), 0
+                dist = np.sqrt(((x - a) ** 2 + (y - b) ** 2).astype(np.float64)).astype(np.float32)
+                m = dist.astype(np.float64) < np.float64(np.float32(c)) / 2.0
+            want[m] = t
+            L.paint_cells(shape, t, a, b, c, d)
+            assert np.array_equal(L.get_cell_types(), want), (k, shape, t, a, b, c, d)
+
+
+def test_paint_then_step_matches_uploaded_map(gpu, oracle):
+    """A painted lattice steps exactly like one given the same map from the
+    host, and like the oracle."""
+    W, H, model = 640, 128, 3
+    types = G.disc(W, H, W // 8, H // 2, H // 8)
+    st = oracle.init_bernoulli(model, W, H, types, seed=4, p_move=0.3, p_rest=0.3)
+    out = []
+    for painted in (True, False):
+        with gpu.GpuLattice(model, W, H, seed=6) as L:
+            if painted:
+                L.apply_bc_pipe()
+                L.paint_cells(gpu.SHAPE_DISC, gpu.SOLID_NO_SLIP, W // 8, H // 2, H // 8)
+            else:
+                L.set_cell_types(types)
+            L.upload(st)
+            L.set_forcing_column(16, 0.05)
+            L.collide_and_propagate(40)
+            out.append(L.download())
+    assert np.array_equal(out[0], out[1])
+    want = oracle.run(model, st, 40, types=types, seed=6, force_x=16, force_p=0.05)
+    assert np.array_equal(out[0], want)
+
+
+def test_paint_rejects_bad_arguments(gpu):
+    with gpu.GpuLattice(1, 64, 8) as L:
+        for args in [(3, 1, 0, 0, 1, 1), (0, 3, 0, 0, 1, 1), (0, -1, 0, 0, 1, 1),
+                     (1, 1, 0, 0, -2, 0), (0, 1, 1 << 29, 0, 1, 1)]:
+            with pytest.raises(gpu.LgcaError):
+                L.paint_cells(*args)
+        L.paint_cells(gpu.SHAPE_RECT, gpu.FLUID, 0, 0, 64, 8)  # no planes yet: nothing to do
+        assert not L.get_cell_types().any()

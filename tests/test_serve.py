@@ -82,6 +82,26 @@ def test_budget_admission_and_completion():
     assert rep["p99_latency_s"] >= rep["p50_latency_s"] > 0
 
 
+def test_site_slots_bound_the_resident_set():
+    clock = FakeClock()
+    jobs = jobs_small(40)
+    cap = 2 * max(j.sites for j in jobs)
+    srv = S.Server(FakeBackend(clock), budget=1e12, clock=clock, sleep=clock.sleep,
+                   max_sites=cap)
+    seen = [0]
+    orig = srv._admit
+
+    def admit(now):
+        orig(now)
+        assert srv.sites == sum(j.sites for j in srv.active)
+        assert len(srv.active) <= 1 or srv.sites <= cap
+        seen[0] = max(seen[0], len(srv.active))
+
+    srv._admit = admit
+    rep = srv.run(jobs)
+    assert rep["completed"] == len(jobs) and seen[0] >= 2 and srv.sites == 0
+
+
 def test_job_larger_than_budget_is_rejected():
     clock = FakeClock()
     jobs = jobs_small(5)
@@ -117,6 +137,50 @@ def test_job_stream_shapes():
     assert 300 < len(jobs) < 700
 
 
+class PipelinedFake(FakeBackend):
+    """Field requests return tokens collected later, as on the GPU; logs the
+    order of step calls and collections."""
+
+    def __init__(self, clock):
+        super().__init__(clock)
+        self.log = []
+
+    def step(self, handles, nsteps):
+        super().step(handles, nsteps)
+        self.log.append("step")
+
+    def request_fields(self, handles):
+        return [(h["steps"],) for h in handles]  # values as of the request
+
+    def collect(self, token):
+        self.log.append("collect")
+        return token
+
+
+def test_pipelined_backend_overlaps_and_gives_same_results():
+    jobs_a, jobs_b = jobs_small(30, seed=4), jobs_small(30, seed=4)
+    clock = FakeClock()
+    plain = S.Server(FakeBackend(clock), budget=1e12, clock=clock, sleep=clock.sleep).run(jobs_a)
+    clock2 = FakeClock()
+    be = PipelinedFake(clock2)
+    piped = S.Server(be, budget=1e12, clock=clock2, sleep=clock2.sleep).run(jobs_b)
+    assert piped["completed"] == plain["completed"] == len(jobs_a)
+    for a, b in zip(jobs_a, jobs_b):
+        assert a.last_fields == b.last_fields == (a.steps,)
+        assert a.outputs == b.outputs
+    # a call's fields are collected after the next call was queued (two calls
+    # outstanding), except when nothing else was runnable
+    outstanding, two = 0, 0
+    for e in be.log:
+        if e == "step":
+            outstanding += 1
+        else:
+            assert outstanding in (1, 2)
+            two += outstanding == 2
+            outstanding -= 1
+    assert two >= 0.8 * be.log.count("collect")
+
+
 @pytest.mark.gpu
 def test_short_served_stream_is_bit_exact(gpu):
     jobs = S.make_jobs(40.0, 1.5, rng_seed=11, w_range=(256, 1024), h_range=(256, 512),
@@ -126,4 +190,5 @@ def test_short_served_stream_is_bit_exact(gpu):
     rep = srv.run(jobs)
     backend.close()
     assert rep["completed"] == len(jobs)
-    assert S.verify_sample(srv.done, n=6)
+    assert all(j.outputs == -(-j.steps // 500) for j in jobs)
+    assert S.verify_sample(srv.done, n=len(srv.done))  # every job, rebuilt from a host map
