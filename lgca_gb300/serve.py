@@ -7,8 +7,9 @@ Job stream (defaults): Poisson arrivals at `rate` jobs/s for `duration` s;
 model, geometry and occupation as the batched workload; width log-uniform in
 [256, 8192] and height in [256, 4096] (multiples of 64); steps log-uniform in
 [100, 20000]; seed = arrival index.  Every `out_every` steps (and at the end)
-a job returns its 16 x 16 integer block sums (N, Jx2, Jy).  Admission keeps
-the resident lattices' device bytes within `budget` (150 GB).
+a job returns its 16 x 16 integer block sums (N, Jx2, Jy).  Admission is
+first come, first served and keeps the resident lattices' device bytes within
+`budget` (150 GB) and their sites within `max_sites` (slots).
 
 The scheduler (Server) talks to a backend: GpuBackend runs the engine;
 tests substitute a CPU fake to exercise admission, budgets and failures.
@@ -80,15 +81,17 @@ def make_jobs(rate: float, duration: float, rng_seed: int = 5, w_range=(256, 819
     return jobs
 
 
-def lattice_bytes(model: int, W: int, H: int, geometry: str) -> int:
-    """Device bytes of a lattice (state buffers, geometry planes, scratch)."""
+def lattice_bytes(model: int, W: int, H: int, geometry: str, block: int = 16) -> int:
+    """Device bytes of a served lattice: two state buffers, the geometry planes
+    when there are walls or obstacles, and the block-sum outputs (geometry is
+    painted on the device, so there is no cell-map staging)."""
     D = {0: 4, 1: 6, 2: 7, 3: 7}[model]
     nw = (W + 63) // 64
     pitch = nw + (nw & 1)
     plane = H * pitch * 8
     geo = 2 * plane if geometry != "periodic" else 0
-    scratch = W * H * 4 + 4096  # cell types staging / block sums
-    return 2 * D * plane + geo + scratch
+    sums = 3 * 4 * (-(-W // block)) * (-(-H // block))
+    return 2 * D * plane + geo + sums + 4096
 
 
 class GpuBackend:
@@ -379,8 +382,13 @@ def verify_sample(jobs, n: int = 8, block: int = 16, seed: int = 0) -> bool:
     return ok
 
 
+# resident-site slots of the served runs: 2^29 sites keep a 100-step batch
+# call near 30 ms on the GPU, which is already saturated well below that
+SERVE_MAX_SITES = float(1 << 29)
+
+
 def serve(rate: float, duration: float, budget: float = 150e9, drain_limit: float = 60.0,
-          verify: int = 8, fcfs: bool = True, max_sites: float = float("inf"),
+          verify: int = 8, fcfs: bool = True, max_sites: float = SERVE_MAX_SITES,
           quantum: int = 100, **job_kw) -> dict:
     jobs = make_jobs(rate, duration, **job_kw)
     backend = GpuBackend()
@@ -407,7 +415,7 @@ def main(argv=None):
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--drain", type=float, default=60.0)
     ap.add_argument("--verify", type=int, default=8)
-    ap.add_argument("--max-sites", type=float, nargs="+", default=[float("inf")],
+    ap.add_argument("--max-sites", type=float, nargs="+", default=[SERVE_MAX_SITES],
                     help="resident site caps to try (slots)")
     ap.add_argument("--quantum", type=int, default=100)
     ap.add_argument("--no-fcfs", action="store_true")
