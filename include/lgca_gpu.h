@@ -147,6 +147,12 @@ int lgca_set_temporal_depth(lgca_handle h, int depth);
  * No reference counterpart (a scheduling choice of this engine). */
 int lgca_set_kernel_variant(lgca_handle h, int variant);
 
+/* Launch shape of the one-step kernels: warps per block (1, 2, 4 or 8), or 0
+ * to choose per launch the largest block whose grid spreads over the SMs with
+ * the least wave-quantisation loss.  A tuning knob: results do not depend on
+ * it.  (No reference counterpart.) */
+int lgca_set_block_warps(lgca_handle h, int warps);
+
 /* Advance nsteps steps (forcing column, then pull-stream + collide by cell
  * type), enqueued on the handle's stream; the step counter advances by
  * nsteps.  Replaces: OMP_Lattice<M>::collide_and_propagate

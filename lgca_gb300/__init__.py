@@ -72,6 +72,7 @@ def lib() -> C.CDLL:
             "lgca_set_chirality": (C.c_int, [vp, vp]),
             "lgca_set_temporal_depth": (C.c_int, [vp, C.c_int]),
             "lgca_set_kernel_variant": (C.c_int, [vp, C.c_int]),
+            "lgca_set_block_warps": (C.c_int, [vp, C.c_int]),
             "lgca_collide_and_propagate": (C.c_int, [vp, C.c_int]),
             "lgca_apply_body_force": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(u64)]),
             "lgca_count_particles": (C.c_int, [vp, C.POINTER(u64)]),
@@ -239,6 +240,10 @@ class GpuLattice:
 
     def set_temporal_depth(self, depth: int) -> None:
         _check(self._h, lib().lgca_set_temporal_depth(self._h, int(depth)))
+
+    def set_block_warps(self, warps: int) -> None:
+        """Warps per block of the one-step kernels (0 = chosen per launch)."""
+        _check(self._h, lib().lgca_set_block_warps(self._h, int(warps)))
 
     def set_kernel_variant(self, variant: int) -> None:
         """0 auto, 1 one step per pass, 2 register wavefront, 3 shared-memory tiles."""

@@ -22,9 +22,11 @@ import time
 
 import lgca_gb300 as gpu
 
-# (variant, depth): 5 = one step per pass, two words per lane; 1 = one word
-# per lane; 2 = register wavefront; 3 = shared-memory tiles
-SINGLE_CANDIDATES = [(5, 1), (1, 1), (2, 2), (2, 4), (2, 8), (3, 2), (3, 4), (3, 8)]
+# (variant, depth, warps per block): 5 = one step per pass, two words per
+# lane; 1 = one word per lane; 2 = register wavefront; 3 = shared-memory
+# tiles.  Warps per block applies to the one-step kernels (0 = per launch).
+SINGLE_CANDIDATES = [(5, 1, 4), (5, 1, 8), (5, 1, 2), (1, 1, 4), (1, 1, 2),
+                     (2, 2, 0), (2, 4, 0), (2, 8, 0), (3, 2, 0), (3, 4, 0), (3, 8, 0)]
 WPT_CANDIDATES = {1: 1, 2: 5}  # words per lane -> kernel variant of a batch member
 
 
@@ -39,12 +41,12 @@ def family(model: int) -> int:
 class Autotuner:
     def __init__(self, cache_path: str | None = None):
         self.cache_path = cache_path
-        self.single: dict[str, tuple[int, int]] = {}
+        self.single: dict[str, tuple[int, int, int]] = {}
         self.batch: dict[str, int] = {}
         if cache_path and os.path.exists(cache_path):
             with open(cache_path) as f:
                 d = json.load(f)
-            self.single = {k: tuple(v) for k, v in d.get("single", {}).items()}
+            self.single = {k: tuple(v) for k, v in d.get("single", {}).items() if len(v) == 3}
             self.batch = {k: int(v) for k, v in d.get("batch", {}).items()}
 
     def save(self) -> None:
@@ -53,18 +55,20 @@ class Autotuner:
                 json.dump({"single": self.single, "batch": self.batch}, f, indent=1)
 
     # ------------------------------------------------------------ single lattice
-    def tune_lattice(self, L: "gpu.GpuLattice", steps: int = 16) -> tuple[int, int]:
-        """Choose (variant, depth) for L's (model, size class) by timing the
-        candidates on a twin of L; apply the choice to L and return it."""
+    def tune_lattice(self, L: "gpu.GpuLattice", steps: int = 16) -> tuple[int, int, int]:
+        """Choose (variant, depth, warps per block) for L's (model, size
+        class) by timing the candidates on a twin of L; apply the choice to L
+        and return it."""
         key = f"{L.model}:{size_class(L.dim_x, L.dim_y)}"
         if key not in self.single:
             blob = L.checkpoint()
             twin = gpu.GpuLattice(L.model, L.dim_x, L.dim_y)
-            best, best_t = (5, 1), float("inf")
-            for variant, depth in SINGLE_CANDIDATES:
+            best, best_t = (5, 1, 0), float("inf")
+            for variant, depth, bw in SINGLE_CANDIDATES:
                 twin.restore(blob)
                 twin.set_kernel_variant(variant)
                 twin.set_temporal_depth(depth)
+                twin.set_block_warps(bw)
                 n = max(steps, 2 * depth)
                 twin.collide_and_propagate(depth)  # warm-up (and kernel load)
                 twin.sync()
@@ -73,13 +77,14 @@ class Autotuner:
                 twin.sync()
                 t = (time.perf_counter() - t0) / n
                 if t < best_t:
-                    best, best_t = (variant, depth), t
+                    best, best_t = (variant, depth, bw), t
             twin.close()
             self.single[key] = best
-        variant, depth = self.single[key]
+        variant, depth, bw = self.single[key]
         L.set_kernel_variant(variant)
         L.set_temporal_depth(depth)
-        return variant, depth
+        L.set_block_warps(bw)
+        return variant, depth, bw
 
     # ------------------------------------------------------------ batch members
     def tune_batch_members(self, lattices, steps: int = 8, sample: int = 6) -> dict[str, int]:
@@ -120,7 +125,8 @@ class Autotuner:
 
 def describe(tuner: Autotuner) -> dict:
     names = {1: "one-step/1 word", 5: "one-step/2 words", 2: "wavefront", 3: "smem tiles"}
-    return {k: f"{names.get(v[0], v[0])}, depth {v[1]}" for k, v in tuner.single.items()}
+    return {k: f"{names.get(v[0], v[0])}, depth {v[1]}, {v[2] or 'auto'} warps/block"
+            for k, v in tuner.single.items()}
 
 
 __all__ = ["Autotuner", "size_class", "family", "SINGLE_CANDIDATES", "describe"]

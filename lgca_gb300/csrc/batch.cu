@@ -26,6 +26,8 @@ __global__ void __launch_bounds__(256) k_batch(const BatchEntry *__restrict__ E,
                                                const int *__restrict__ block_lat, int n_active,
                                                int s_local, const int *__restrict__ s_base)
 {
+    pdl_launch_dependents();
+    pdl_wait();  // keys, step counter and states come from earlier kernels
     const int lane = threadIdx.x & 31;
     const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (g >= prefix[n_active]) return;
@@ -85,8 +87,8 @@ cudaError_t launch_batch(const BatchEntry *E, const int *prefix, const int *bloc
 {
     if (total_tasks <= 0) return cudaSuccess;
     const unsigned grid = (unsigned)((total_tasks + 7) / 8);
-    k_batch<<<grid, 256, 0, st>>>(E, prefix, block_lat, n_active, s_local, s_base);
-    return cudaGetLastError();
+    return launch_pdl(k_batch, dim3(grid), dim3(256), 0, st, E, prefix, block_lat, n_active,
+                      s_local, s_base);
 }
 
 cudaError_t launch_batch_keys(const BatchEntry *E, int n, int max_steps, cudaStream_t st)

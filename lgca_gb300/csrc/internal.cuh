@@ -18,6 +18,38 @@
 
 namespace lgca_gpu {
 
+// Programmatic dependent launch.  The step kernels are launched with
+// programmatic stream serialisation: the next step's blocks may be scheduled
+// while the previous step drains, and wait in pdl_wait() -- which returns
+// once every earlier grid on the stream has completed and its writes are
+// visible -- before they touch memory.  Launched without that attribute,
+// pdl_wait() returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
 // Geometry modes of the step kernels: which cell-type planes exist.
 enum : int { GEOM_NONE = 0, GEOM_NOSLIP = 1, GEOM_FULL = 2 };
 
@@ -43,6 +75,7 @@ struct StepArgs {
     uint64_t force_thr; // 0 disables forcing
     int fx;             // forcing column (valid when force_thr > 0)
     int wpt;            // words per lane of the one-step kernel (1 or 2)
+    int bw;             // warps per block of the one-step kernels (0: chosen per launch)
 };
 
 // One lattice of a batch (batch.cu): its step arguments (src/dst unused),

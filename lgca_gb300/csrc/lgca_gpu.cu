@@ -31,6 +31,7 @@ struct lgca_lattice {
     int depth = 1;
     int variant = VARIANT_AUTO;
     int wpt = 2;  // words per lane of the one-step kernel where the width allows
+    int bw = 0;   // warps per block of the one-step kernels (0: chosen per launch)
     int device = 0;
     cudaStream_t own_stream = nullptr, stream = nullptr;
     void *scratch = nullptr;
@@ -476,6 +477,15 @@ int lgca_set_kernel_variant(lgca_handle h, int variant)
     return LGCA_OK;
 }
 
+int lgca_set_block_warps(lgca_handle h, int warps)
+{
+    CHECK_HANDLE(h);
+    if (!(warps == 0 || warps == 1 || warps == 2 || warps == 4 || warps == 8))
+        return fail(h, LGCA_ERR_INVALID, "warps per block must be 0, 1, 2, 4 or 8");
+    h->bw = warps;
+    return LGCA_OK;
+}
+
 int lgca_collide_and_propagate(lgca_handle h, int nsteps)
 {
     CHECK_HANDLE(h);
@@ -490,6 +500,7 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     a.force_thr = h->force_thr;
     a.fx = h->force_x;
     a.wpt = (h->variant == VARIANT_PLAIN) ? 1 : h->wpt;
+    a.bw = h->bw;
     const int gm = geom_mode(h);
     if (h->variant == VARIANT_PERSIST && nsteps > 1) {
         const size_t sync_bytes = (size_t)(PERSIST_MAX_BLOCKS + 1) * sizeof(int);

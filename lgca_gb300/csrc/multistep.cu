@@ -30,8 +30,10 @@ struct Tile {
 };
 
 template <int MODEL, int GM, int K, int THO>
-__global__ void __launch_bounds__(256) k_multistep(const MultiStepArgs m)
+__global__ void __launch_bounds__(256) k_multistep(const __grid_constant__ MultiStepArgs m)
 {
+    pdl_launch_dependents();
+    pdl_wait();
     using T = Tile<MODEL, GM, K, THO>;
     constexpr int D = T::D, R = T::R, PL = T::PLANE;
     extern __shared__ uint64_t smem[];
@@ -200,8 +202,7 @@ static cudaError_t launch_tile(const MultiStepArgs &m, cudaStream_t st)
     if (e != cudaSuccess) return e;
     const dim3 grid((unsigned)((m.base.g.nw + 31) / 32), (unsigned)((m.base.g.H + THO - 1) / THO));
     if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
-    kern<<<grid, 256, T::SMEM, st>>>(m);
-    return cudaGetLastError();
+    return launch_pdl(kern, grid, dim3(256), T::SMEM, st, m);
 }
 
 // Tile heights per depth: shared memory = (2 * D + geometry planes) * (THO + 2K) * 34 * 8 B.

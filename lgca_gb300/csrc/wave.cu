@@ -23,8 +23,11 @@ namespace lgca_gpu {
 static constexpr unsigned FULLW = 0xffffffffu;
 
 template <int MODEL, int GM, int K>
-__global__ void __launch_bounds__(128) k_wave(const MultiStepArgs m, int S, int nstrips)
+__global__ void __launch_bounds__(128) k_wave(const __grid_constant__ MultiStepArgs m, int S,
+                                              int nstrips)
 {
+    pdl_launch_dependents();
+    pdl_wait();
     constexpr int D = ModelTraits<MODEL>::D;
     constexpr int WEST = (MODEL == M_HPP) ? 2 : 3;
     const StepArgs &a = m.base;
@@ -200,8 +203,8 @@ static cudaError_t launch_k(const MultiStepArgs &m, cudaStream_t st)
     const long long warps = (long long)nstrips * ((g.H + S - 1) / S);
     const long long blocks = (warps + 3) / 4;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    k_wave<MODEL, GM, K><<<(unsigned)blocks, 128, 0, st>>>(m, S, nstrips);
-    return cudaGetLastError();
+    return launch_pdl(k_wave<MODEL, GM, K>, dim3((unsigned)blocks), dim3(128), 0, st, m, S,
+                      nstrips);
 }
 
 template <int MODEL, int GM>

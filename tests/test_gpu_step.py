@@ -18,9 +18,10 @@ def sha(a):
 
 
 def run_gpu(gpu, model, init, steps, types=None, seed=0, chir=None, force_x=-1, force_p=0.0, t0=0,
-            depth=1, chunks=None, variant=0):
+            depth=1, chunks=None, variant=0, block_warps=0):
     H, W = init.shape
     with gpu.GpuLattice(model, W, H, seed) as L:
+        L.set_block_warps(block_warps)
         if types is not None:
             L.set_cell_types(types)
         L.upload(init)
@@ -245,3 +246,23 @@ def test_one_step_kernels_one_and_two_words_per_lane(gpu, oracle, model, geom):
             for variant in (1, 5):
                 got = run_gpu(gpu, model, st, 11, variant=variant, **kw)
                 assert np.array_equal(got, want), (W, H, fx, variant)
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("block_warps", [1, 2, 4, 8])
+def test_launch_shapes_give_the_same_bits(gpu, oracle, model, block_warps):
+    """Warps per block of the one-step kernels (rows of one or several words
+    per lane, rows shared by a warp, partial last blocks) never change the
+    result; consecutive steps overlap on the GPU by programmatic dependent
+    launch, which must not let a step read its predecessor's input."""
+    rng = np.random.default_rng(model * 10 + block_warps)
+    for W, H, geom in [(100, 18, "pipe"), (640, 30, "karman"), (1024, 66, "reflecting_forward"),
+                       (4096, 12, "periodic")]:
+        types = GEOMS[geom](W, H)
+        seed = int(rng.integers(1 << 40))
+        st = oracle.init_bernoulli(model, W, H, types, seed=seed, p_move=0.3, p_rest=0.3)
+        kw = dict(types=types, seed=seed, force_x=W // 3, force_p=0.5)
+        want = oracle.run(model, st, 25, **kw)
+        for variant in (1, 5):
+            got = run_gpu(gpu, model, st, 25, variant=variant, block_warps=block_warps, **kw)
+            assert np.array_equal(got, want), (W, H, geom, variant)
