@@ -21,7 +21,11 @@ namespace lgca_gpu {
 // One launch per step for all members: warp task g belongs to the lattice
 // found from the block's first lattice (block_lat) by a short forward scan;
 // the lattice's entry selects model, geometry mode and words per lane.
-__global__ void __launch_bounds__(256) k_batch(const BatchEntry *__restrict__ E,
+// GMAX is the largest geometry mode among the members: batches without slip
+// cells use a kernel compiled without the slip-aware paths, held to 64
+// registers (4 blocks of 8 warps per SM) at the price of a few spilled words.
+template <int GMAX>
+__global__ void __launch_bounds__(256, GMAX == GEOM_FULL ? 3 : 4) k_batch(const BatchEntry *__restrict__ E,
                                                const int *__restrict__ prefix,
                                                const int *__restrict__ block_lat, int n_active,
                                                int s_local, const int *__restrict__ s_base)
@@ -37,18 +41,25 @@ __global__ void __launch_bounds__(256) k_batch(const BatchEntry *__restrict__ E,
     const int s = *s_base + s_local;
     const int local = g - prefix[l];
     const int rg = local / e.per_row, c = local - rg * e.per_row;
-    const int y = rg * (32 / e.width) + lane / e.width;  // rows of <= 16 items share a warp
+    // rows of <= 16 items share a warp, all of one parity: warp row rg holds
+    // rows (rg / 2) * 2R + (rg & 1) + 2i, R = 32 / width rows per warp
+    const int rpw = 32 / e.width;
+    const int y = (rg >> 1) * 2 * rpw + (rg & 1) + 2 * (lane / e.width);
     const ulonglong2 k = __ldg(reinterpret_cast<const ulonglong2 *>(e.keys) + s);
     const StepIO io{(s & 1) ? e.buf1 : e.buf0, (s & 1) ? e.buf0 : e.buf1, k.x, k.y};
     const StepArgs &a = e.a;
     const int w = c * 32 + (lane & (e.width - 1)), wd = e.width;
+#define LGCA_BATCH_CASE(F, MODEL, GM)                                                          \
+    case F * 6 + GM * 2:                                                                       \
+        if (GM <= GMAX) step_word<MODEL, GM, true>(a, io, y, w, lane, wd);                           \
+        break;                                                                                 \
+    case F * 6 + GM * 2 + 1:                                                                   \
+        if (GM <= GMAX) step_pair<MODEL, GM, true>(a, io, y, w, lane, wd);                           \
+        break;
 #define LGCA_BATCH_CASES(F, MODEL)                                                             \
-    case F * 6 + GEOM_NONE * 2: step_word<MODEL, GEOM_NONE>(a, io, y, w, lane, wd); break;        \
-    case F * 6 + GEOM_NONE * 2 + 1: step_pair<MODEL, GEOM_NONE>(a, io, y, w, lane, wd); break;    \
-    case F * 6 + GEOM_NOSLIP * 2: step_word<MODEL, GEOM_NOSLIP>(a, io, y, w, lane, wd); break;    \
-    case F * 6 + GEOM_NOSLIP * 2 + 1: step_pair<MODEL, GEOM_NOSLIP>(a, io, y, w, lane, wd); break;\
-    case F * 6 + GEOM_FULL * 2: step_word<MODEL, GEOM_FULL>(a, io, y, w, lane, wd); break;        \
-    case F * 6 + GEOM_FULL * 2 + 1: step_pair<MODEL, GEOM_FULL>(a, io, y, w, lane, wd); break;
+    LGCA_BATCH_CASE(F, MODEL, GEOM_NONE)                                                       \
+    LGCA_BATCH_CASE(F, MODEL, GEOM_NOSLIP)                                                     \
+    LGCA_BATCH_CASE(F, MODEL, GEOM_FULL)
     switch (e.code) {
         LGCA_BATCH_CASES(0, M_HPP)
         LGCA_BATCH_CASES(1, M_FHP_I)
@@ -56,6 +67,7 @@ __global__ void __launch_bounds__(256) k_batch(const BatchEntry *__restrict__ E,
     default: break;
     }
 #undef LGCA_BATCH_CASES
+#undef LGCA_BATCH_CASE
 }
 
 // keys[l][s] = (chirality key, forcing key) of member l at its step t0 + s
@@ -83,12 +95,21 @@ __global__ void k_set_base(int *s_base, int v)
 
 cudaError_t launch_batch(const BatchEntry *E, const int *prefix, const int *block_lat,
                          int n_active, int total_tasks, int s_local, const int *s_base,
-                         cudaStream_t st)
+                         int gmax, cudaStream_t st)
 {
     if (total_tasks <= 0) return cudaSuccess;
-    const unsigned grid = (unsigned)((total_tasks + 7) / 8);
-    return launch_pdl(k_batch, dim3(grid), dim3(256), 0, st, E, prefix, block_lat, n_active,
-                      s_local, s_base);
+    const dim3 grid((unsigned)((total_tasks + 7) / 8));
+    switch (gmax) {
+    case GEOM_NONE:
+        return launch_pdl(k_batch<GEOM_NONE>, grid, dim3(256), 0, st, E, prefix, block_lat,
+                          n_active, s_local, s_base);
+    case GEOM_NOSLIP:
+        return launch_pdl(k_batch<GEOM_NOSLIP>, grid, dim3(256), 0, st, E, prefix, block_lat,
+                          n_active, s_local, s_base);
+    default:
+        return launch_pdl(k_batch<GEOM_FULL>, grid, dim3(256), 0, st, E, prefix, block_lat,
+                          n_active, s_local, s_base);
+    }
 }
 
 cudaError_t launch_batch_keys(const BatchEntry *E, int n, int max_steps, cudaStream_t st)

@@ -24,6 +24,11 @@ namespace lgca_gpu {
 // once every earlier grid on the stream has completed and its writes are
 // visible -- before they touch memory.  Launched without that attribute,
 // pdl_wait() returns at once.
+//
+// Such kernels read the state through L2 only (ld.global.cg), never through
+// the non-coherent L1/texture path: grids of consecutive steps share SMs, so
+// an SM's L1 can still hold lines of a buffer that an older step read and the
+// step in between has since rewritten.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_launch_dependents()
 {
@@ -93,8 +98,9 @@ struct BatchEntry {
     int gm, wpt;  // geometry mode, words per lane
     int code;     // model family * 6 + geometry mode * 2 + (wpt == 2)
 };
+// gmax: the largest geometry mode among the launch's members
 cudaError_t launch_batch(const BatchEntry *E, const int *prefix, const int *block_lat,
-                         int n_active, int total_tasks, int s_local, const int *s_base,
+                         int n_active, int total_tasks, int s_local, const int *s_base, int gmax,
                          cudaStream_t stream);
 cudaError_t launch_batch_keys(const BatchEntry *E, int n, int max_steps, cudaStream_t stream);
 cudaError_t launch_advance(int *s_base, int by, cudaStream_t stream);

@@ -913,8 +913,10 @@ int bcuda(lgca_batch *b, cudaError_t e, const char *what)
 // steps numbered from *s_base + s_local; then *s_base advances by n.
 int enqueue_steps(lgca_batch *b, int n_active, int tasks, int n)
 {
+    int gmax = GEOM_NONE;  // the active members are the first n_active entries
+    for (int i = 0; i < n_active; ++i) gmax = std::max(gmax, b->E[i].gm);
     for (int s = 0; s < n; ++s)
-        BCK(b, launch_batch(b->dE, b->dP, b->dB, n_active, tasks, s, b->s_base, b->stream));
+        BCK(b, launch_batch(b->dE, b->dP, b->dB, n_active, tasks, s, b->s_base, gmax, b->stream));
     BCK(b, launch_advance(b->s_base, n, b->stream));
     return LGCA_OK;
 }
@@ -1066,7 +1068,8 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         const int items = pair ? h->g.nw / 2 : h->g.nw;  // lane items per row
         e.width = seg_width(items);
         e.per_row = (items + 31) / 32;
-        const int row_groups = (h->g.H + (32 / e.width) - 1) / (32 / e.width);
+        const int rpw = 32 / e.width;  // rows per warp task, of one parity
+        const int row_groups = 2 * ((h->g.H + 2 * rpw - 1) / (2 * rpw));
         e.buf0 = h->buf[h->cur];
         e.buf1 = h->buf[h->cur ^ 1];
         e.seed = h->seed;

@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256) k_multistep(const __grid_constant__ Multi
         const int r = it / TWI, i = it - r * TWI;
         const unsigned o = (unsigned)grow(r) * g.pitch + gword(i);
 #pragma unroll
-        for (int d = 0; d < D; ++d) buf0[d * PL + it] = __ldg(a.src + (d * ps + o));
+        for (int d = 0; d < D; ++d) buf0[d * PL + it] = __ldcg(a.src + (d * ps + o));  // L2: see pdl_wait
         if (GM >= GEOM_NOSLIP) s_solid[it] = __ldg(a.solid + o);
         if (GM == GEOM_FULL) s_slip[it] = __ldg(a.slip + o);
     }

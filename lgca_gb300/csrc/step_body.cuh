@@ -39,10 +39,10 @@ struct StepIO {
     uint64_t ckey, fkey;  // chirality / forcing keys of the step
 };
 
-// State loads: the one-step kernels read buffers that no thread writes
-// during the launch (read-only path); the persistent band kernel reads
-// buffers that other blocks wrote earlier in the same launch, so it must
-// bypass the non-coherent L1 (ld.global.cg, cached in L2 only).
+// State loads: CG = ld.global.cg, cached in L2 only, for kernels whose input
+// was written while they (or a kernel overlapping them on the same SMs) were
+// resident -- the persistent band kernel, and the step kernels chained by
+// programmatic dependent launch; otherwise the read-only path.
 template <bool CG> __device__ __forceinline__ uint64_t ld_state(const uint64_t *p)
 {
     return CG ? __ldcg(p) : __ldg(p);
@@ -72,9 +72,15 @@ __device__ __forceinline__ uint64_t force_flip_at(const StepArgs &a, const StepI
     return (u < a.force_thr) ? cand : 0ull;
 }
 
-template <int MODEL, int GM, bool CG = false>
+// Row mapping contract of both step bodies: the lanes of a warp hold rows of
+// one parity (FHP shifts depend on it, and the shuffles must be executed by
+// the whole warp), e.g. rows y, y+2, ... when rows are narrower than a warp.
+// `pre` carries chirality words drawn before the caller waited for the
+// previous step (PRE); they equal lgca_rng_draw(io.ckey, (y, word)).
+template <int MODEL, int GM, bool CG = false, bool PRE = false>
 __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, const int y,
-                                          const int w, const int lane, const int width = 32)
+                                          const int w, const int lane, const int width = 32,
+                                          const uint64_t pre = 0)
 {
     constexpr int D = ModelTraits<MODEL>::D;
     const PlaneGeom &g = a.g;
@@ -159,27 +165,16 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
     } else {
         p[0] = shl(n[0], 0, row0);
         p[3] = shr(n[3], 3, row0);
-        if (width == 32) {  // one row per warp: the parity is warp-uniform
-            if (even) {
-                p[1] = shl(n[1], 1, rowm);
-                p[5] = shl(n[5], 5, rowp);
-                p[2] = n[2];
-                p[4] = n[4];
-            } else {
-                p[2] = shr(n[2], 2, rowm);
-                p[4] = shr(n[4], 4, rowp);
-                p[1] = n[1];
-                p[5] = n[5];
-            }
+        if (even) {  // warp-uniform (row mapping contract)
+            p[1] = shl(n[1], 1, rowm);
+            p[5] = shl(n[5], 5, rowp);
+            p[2] = n[2];
+            p[4] = n[4];
         } else {
-            // rows of both parities share the warp: every lane takes part in
-            // every shuffle, then selects by its row's parity
-            const uint64_t l1 = shl(n[1], 1, rowm), l5 = shl(n[5], 5, rowp);
-            const uint64_t r2 = shr(n[2], 2, rowm), r4 = shr(n[4], 4, rowp);
-            p[1] = even ? l1 : n[1];
-            p[5] = even ? l5 : n[5];
-            p[2] = even ? n[2] : r2;
-            p[4] = even ? n[4] : r4;
+            p[2] = shr(n[2], 2, rowm);
+            p[4] = shr(n[4], 4, rowp);
+            p[1] = n[1];
+            p[5] = n[5];
         }
         if (D == 7) p[6] = n[6];
     }
@@ -191,7 +186,7 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
     if (MODEL != M_HPP) {
         const uint64_t chir =
             a.chir ? __ldg(a.chir + row0 + w)
-                   : lgca_rng_draw(io.ckey, lgca_rng_index((uint32_t)y, (uint32_t)w));
+                   : (PRE ? pre : lgca_rng_draw(io.ckey, lgca_rng_index((uint32_t)y, (uint32_t)w)));
         collide<MODEL>(c, chir);
     } else {
         collide<MODEL>(c, 0ull);
@@ -231,9 +226,10 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
 // W a multiple of 128): 16-byte loads and stores, one shuffle per shifted
 // plane for 128 sites, and half as many warps, so that an L2-resident lattice
 // fits in one wave of resident warps.  Same arithmetic as step_word.
-template <int MODEL, int GM, bool CG = false>
+template <int MODEL, int GM, bool CG = false, bool PRE = false>
 __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, const int y,
-                                          const int t, const int lane, const int width = 32)
+                                          const int t, const int lane, const int width = 32,
+                                          const uint64_t pre0 = 0, const uint64_t pre1 = 0)
 {
     constexpr int D = ModelTraits<MODEL>::D;
     const PlaneGeom &g = a.g;
@@ -337,28 +333,16 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
         const uint64_t a0 = shl(n[0][0], n[1][0], 0, row0, 0), a1 = shl(n[0][0], n[1][0], 0, row0, 1);
         const uint64_t b0 = shr(n[0][3], n[1][3], 3, row0, 0), b1 = shr(n[0][3], n[1][3], 3, row0, 1);
         q[0][0] = a0; q[1][0] = a1; q[0][3] = b0; q[1][3] = b1;
-        if (width == 32) {  // one row per warp: the parity is warp-uniform
-            if (even) {
-                const uint64_t c0 = shl(n[0][1], n[1][1], 1, rowm, 0), c1 = shl(n[0][1], n[1][1], 1, rowm, 1);
-                const uint64_t e0 = shl(n[0][5], n[1][5], 5, rowp, 0), e1 = shl(n[0][5], n[1][5], 5, rowp, 1);
-                q[0][1] = c0; q[1][1] = c1; q[0][5] = e0; q[1][5] = e1;
-                q[0][2] = n[0][2]; q[1][2] = n[1][2]; q[0][4] = n[0][4]; q[1][4] = n[1][4];
-            } else {
-                const uint64_t c0 = shr(n[0][2], n[1][2], 2, rowm, 0), c1 = shr(n[0][2], n[1][2], 2, rowm, 1);
-                const uint64_t e0 = shr(n[0][4], n[1][4], 4, rowp, 0), e1 = shr(n[0][4], n[1][4], 4, rowp, 1);
-                q[0][2] = c0; q[1][2] = c1; q[0][4] = e0; q[1][4] = e1;
-                q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][5] = n[0][5]; q[1][5] = n[1][5];
-            }
-        } else {
-            // rows of both parities share the warp: all lanes shuffle, then select
+        if (even) {  // warp-uniform (row mapping contract)
             const uint64_t c0 = shl(n[0][1], n[1][1], 1, rowm, 0), c1 = shl(n[0][1], n[1][1], 1, rowm, 1);
             const uint64_t e0 = shl(n[0][5], n[1][5], 5, rowp, 0), e1 = shl(n[0][5], n[1][5], 5, rowp, 1);
-            const uint64_t f0 = shr(n[0][2], n[1][2], 2, rowm, 0), f1 = shr(n[0][2], n[1][2], 2, rowm, 1);
-            const uint64_t h0 = shr(n[0][4], n[1][4], 4, rowp, 0), h1 = shr(n[0][4], n[1][4], 4, rowp, 1);
-            q[0][1] = even ? c0 : n[0][1]; q[1][1] = even ? c1 : n[1][1];
-            q[0][5] = even ? e0 : n[0][5]; q[1][5] = even ? e1 : n[1][5];
-            q[0][2] = even ? n[0][2] : f0; q[1][2] = even ? n[1][2] : f1;
-            q[0][4] = even ? n[0][4] : h0; q[1][4] = even ? n[1][4] : h1;
+            q[0][1] = c0; q[1][1] = c1; q[0][5] = e0; q[1][5] = e1;
+            q[0][2] = n[0][2]; q[1][2] = n[1][2]; q[0][4] = n[0][4]; q[1][4] = n[1][4];
+        } else {
+            const uint64_t c0 = shr(n[0][2], n[1][2], 2, rowm, 0), c1 = shr(n[0][2], n[1][2], 2, rowm, 1);
+            const uint64_t e0 = shr(n[0][4], n[1][4], 4, rowp, 0), e1 = shr(n[0][4], n[1][4], 4, rowp, 1);
+            q[0][2] = c0; q[1][2] = c1; q[0][4] = e0; q[1][4] = e1;
+            q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][5] = n[0][5]; q[1][5] = n[1][5];
         }
         if (D == 7) { q[0][6] = n[0][6]; q[1][6] = n[1][6]; }
     }
@@ -374,7 +358,8 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
         if (MODEL != M_HPP) {
             const uint64_t chir =
                 a.chir ? __ldg(a.chir + row0 + w0 + k)
-                       : lgca_rng_draw(io.ckey, lgca_rng_index((uint32_t)y, (uint32_t)(w0 + k)));
+                       : (PRE ? (k ? pre1 : pre0)
+                              : lgca_rng_draw(io.ckey, lgca_rng_index((uint32_t)y, (uint32_t)(w0 + k))));
             collide<MODEL>(c, chir);
         } else {
             collide<MODEL>(c, 0ull);

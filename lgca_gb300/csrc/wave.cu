@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(128) k_wave(const __grid_constant__ MultiStepA
         {
             const unsigned o = (unsigned)gyn * g.pitch + gw;
 #pragma unroll
-            for (int d = 0; d < D; ++d) cur[d] = __ldg(a.src + (d * ps + o));
+            for (int d = 0; d < D; ++d) cur[d] = __ldcg(a.src + (d * ps + o));  // L2: see pdl_wait
             force(cur, gyn, 0);
         }
 #pragma unroll
