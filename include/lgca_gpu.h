@@ -110,6 +110,12 @@ int lgca_paint_cells(lgca_handle h, int shape, int32_t type, int64_t a, int64_t 
  * (src/lattice.h:206-211, src/lattice.cpp:422-435). */
 int lgca_upload_state(lgca_handle h, const uint8_t *cells);
 int lgca_download_state(lgca_handle h, uint8_t *cells);
+/* Queued forms: lgca_upload_state returns once the copy is queued; from a
+ * pinned buffer the copy runs later, so keep the buffer unchanged until
+ * lgca_sync(h).  lgca_download_state_async queues the download; the bytes
+ * are in `cells` after lgca_sync(h).  At most one queued download per handle
+ * (both use the handle's scratch). */
+int lgca_download_state_async(lgca_handle h, uint8_t *cells);
 
 /* Occupy each channel of each FLUID cell independently with probability
  * p_move (moving channels) or p_rest (rest channel of FHP-II/III), drawn from

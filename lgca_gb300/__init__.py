@@ -66,6 +66,7 @@ def lib() -> C.CDLL:
                                            C.c_int64, C.c_int64]),
             "lgca_upload_state": (C.c_int, [vp, vp]),
             "lgca_download_state": (C.c_int, [vp, vp]),
+            "lgca_download_state_async": (C.c_int, [vp, vp]),
             "lgca_init_random": (C.c_int, [vp, C.c_double, C.c_double]),
             "lgca_init_zero": (C.c_int, [vp]),
             "lgca_set_forcing_column": (C.c_int, [vp, C.c_int, C.c_double]),
@@ -223,6 +224,11 @@ class GpuLattice:
         s = np.empty(self.shape, np.uint8) if out is None else out
         _check(self._h, lib().lgca_download_state(self._h, _ptr(s)))
         return s
+
+    def download_async(self, out: np.ndarray) -> None:
+        """Queue a download into `out` (pinned for overlap); valid after sync()."""
+        assert out.shape == self.shape and out.dtype == np.uint8 and out.flags.c_contiguous
+        _check(self._h, lib().lgca_download_state_async(self._h, _ptr(out)))
 
     def init_random(self, p_move: float, p_rest: float | None = None) -> None:
         p_rest = p_move if p_rest is None else p_rest

@@ -35,10 +35,19 @@ __device__ __forceinline__ void pdl_launch_dependents()
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+//
+// Not inside CUDA graphs: a stream under capture gets plain launches (the
+// kernels' pdl_wait() then returns at once).  With programmatic edges in
+// graphs that a batch call instantiates and releases while they run, the
+// served loop stalled the device after about ten thousand calls; graphs
+// already launch their kernels back to back.
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
                               cudaStream_t st, Args... args)
 {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = block;
@@ -48,7 +57,7 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
     attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr.val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = &attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = (cap == cudaStreamCaptureStatusNone) ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 

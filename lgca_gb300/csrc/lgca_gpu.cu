@@ -403,6 +403,20 @@ int lgca_download_state(lgca_handle h, uint8_t *cells)
     return LGCA_OK;
 }
 
+int lgca_download_state_async(lgca_handle h, uint8_t *cells)
+{
+    CHECK_HANDLE(h);
+    if (!cells) return fail(h, LGCA_ERR_INVALID, "cells is NULL");
+    DeviceGuard dg(h->device);
+    const size_t n = (size_t)h->g.W * h->g.H;
+    int st = scratch_reserve(h, n + 64);
+    if (st) return st;
+    CK(h, launch_planes_to_aos(h->D, h->g, h->buf[h->cur], static_cast<uint8_t *>(h->scratch),
+                               h->stream));
+    CK(h, cudaMemcpyAsync(cells, h->scratch, n, cudaMemcpyDeviceToHost, h->stream));
+    return LGCA_OK;
+}
+
 int lgca_init_random(lgca_handle h, double p_move, double p_rest)
 {
     CHECK_HANDLE(h);

@@ -266,3 +266,34 @@ def test_launch_shapes_give_the_same_bits(gpu, oracle, model, block_warps):
         for variant in (1, 5):
             got = run_gpu(gpu, model, st, 25, variant=variant, block_warps=block_warps, **kw)
             assert np.array_equal(got, want), (W, H, geom, variant)
+
+
+@pytest.mark.parametrize("model", [1, 3])
+def test_steps_captured_in_a_cuda_graph(gpu, oracle, model):
+    """Steps captured on a caller stream into a CUDA graph (plain launches
+    under capture) replay exactly.  A captured call fixes its steps' keys
+    and buffers: with an even number of steps per call, every replay repeats
+    steps t .. t+k-1 on the current state."""
+    torch = pytest.importorskip("torch")
+    W, H, k = 640, 64, 4
+    types = G.pipe(W, H)
+    st = oracle.init_bernoulli(model, W, H, types, seed=5, p_move=0.3, p_rest=0.3)
+    L = gpu.GpuLattice(model, W, H, seed=5)
+    L.set_cell_types(types)
+    L.upload(st)
+    L.set_forcing_column(10, 0.3)
+    L.sync()
+    s = torch.cuda.Stream()
+    L.set_stream(s.cuda_stream)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        L.collide_and_propagate(k)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    L.set_stream(None)
+    want = st
+    for _ in range(3):
+        want = oracle.run(model, want, k, types=types, seed=5, t0=0, force_x=10, force_p=0.3)
+    assert np.array_equal(L.download(), want)
+    L.close()
