@@ -39,22 +39,17 @@ __global__ void __launch_bounds__(256, GMAX == GEOM_FULL ? 3 : 4) k_batch(const 
     while (prefix[l + 1] <= g) ++l;
     const BatchEntry &e = E[l];
     const int s = *s_base + s_local;
-    const int local = g - prefix[l];
-    const int rg = local / e.per_row, c = local - rg * e.per_row;
-    // rows of <= 16 items share a warp, all of one parity: warp row rg holds
-    // rows (rg / 2) * 2R + (rg & 1) + 2i, R = 32 / width rows per warp
-    const int rpw = 32 / e.width;
-    const int y = (rg >> 1) * 2 * rpw + (rg & 1) + 2 * (lane / e.width);
+    int y, w;  // the lane's row and item (flattened same-parity mapping)
+    flat_site(g - prefix[l], lane, e.a.g.H, e.items, y, w);
     const ulonglong2 k = __ldg(reinterpret_cast<const ulonglong2 *>(e.keys) + s);
     const StepIO io{(s & 1) ? e.buf1 : e.buf0, (s & 1) ? e.buf0 : e.buf1, k.x, k.y};
     const StepArgs &a = e.a;
-    const int w = c * 32 + (lane & (e.width - 1)), wd = e.width;
 #define LGCA_BATCH_CASE(F, MODEL, GM)                                                          \
     case F * 6 + GM * 2:                                                                       \
-        if (GM <= GMAX) step_word<MODEL, GM, true>(a, io, y, w, lane, wd);                           \
+        if (GM <= GMAX) step_word<MODEL, GM, true>(a, io, y, w, lane);                           \
         break;                                                                                 \
     case F * 6 + GM * 2 + 1:                                                                   \
-        if (GM <= GMAX) step_pair<MODEL, GM, true>(a, io, y, w, lane, wd);                           \
+        if (GM <= GMAX) step_pair<MODEL, GM, true>(a, io, y, w, lane);                           \
         break;
 #define LGCA_BATCH_CASES(F, MODEL)                                                             \
     LGCA_BATCH_CASE(F, MODEL, GEOM_NONE)                                                       \

@@ -102,8 +102,7 @@ struct BatchEntry {
     uint64_t seed, t0;
     uint64_t *keys;  // 2 * nsteps keys (chirality, forcing) per step of the call
     int nsteps;
-    int per_row;  // warp tasks per row group
-    int width;    // lanes per row (32 / width rows per warp task)
+    int items;    // lane items per row (words, or word pairs when wpt == 2)
     int gm, wpt;  // geometry mode, words per lane
     int code;     // model family * 6 + geometry mode * 2 + (wpt == 2)
 };
@@ -196,13 +195,31 @@ cudaError_t launch_body_force(int model, const PlaneGeom &g, uint64_t *planes,
                               long long forcing, int bf_dir, void *scratch,
                               unsigned long long *reverted_dev, cudaStream_t s);
 
-// Lanes per row segment for a row of n lane-items: rows of 16 or fewer items
-// share a warp (32 / width rows per warp), wider rows take whole warps.
-__host__ __device__ __forceinline__ int seg_width(int n)
+// Lane mapping of the one-step kernels: the lane items (words, or pairs of
+// words) of all even rows, then of all odd rows, are numbered row by row, and
+// warp task k takes 32 consecutive numbers of one parity class.  Every lane
+// is used except at the end of a class, and the rows of a warp share one
+// parity (the step bodies' contract).  A lane whose left or right neighbour
+// lane holds another row loads that neighbour word instead of shuffling.
+__host__ __device__ __forceinline__ long long class_tasks(int H, int items, int parity)
 {
-    int w = 1;
-    while (w < n && w < 32) w <<= 1;
-    return n > 16 ? 32 : w;
+    const long long rows = parity ? (H / 2) : ((H + 1) / 2);
+    return (rows * items + 31) / 32;
+}
+__host__ __device__ __forceinline__ long long flat_tasks(int H, int items)
+{
+    return class_tasks(H, items, 0) + class_tasks(H, items, 1);
+}
+// Row y and item of `lane` in warp task `task` (y >= H past a class's end).
+__host__ __device__ __forceinline__ void flat_site(long long task, int lane, int H, int items,
+                                                   int &y, int &item)
+{
+    const long long even_tasks = class_tasks(H, items, 0);
+    const int p = task >= even_tasks ? 1 : 0;
+    const long long l = (p ? task - even_tasks : task) * 32 + lane;
+    const long long r = l / items;
+    item = (int)(l - r * items);
+    y = (int)(2 * r + p);
 }
 
 static inline int num_dir(int model) { return model == M_HPP ? 4 : (model == M_FHP_I ? 6 : 7); }

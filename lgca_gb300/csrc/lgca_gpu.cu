@@ -1079,11 +1079,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         e.gm = geom_mode(h);
         const int fam = h->model == LGCA_HPP ? 0 : (h->model == LGCA_FHP_I ? 1 : 2);
         e.code = fam * 6 + e.gm * 2 + (pair ? 1 : 0);
-        const int items = pair ? h->g.nw / 2 : h->g.nw;  // lane items per row
-        e.width = seg_width(items);
-        e.per_row = (items + 31) / 32;
-        const int rpw = 32 / e.width;  // rows per warp task, of one parity
-        const int row_groups = 2 * ((h->g.H + 2 * rpw - 1) / (2 * rpw));
+        e.items = pair ? h->g.nw / 2 : h->g.nw;  // lane items per row
         e.buf0 = h->buf[h->cur];
         e.buf1 = h->buf[h->cur ^ 1];
         e.seed = h->seed;
@@ -1091,7 +1087,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         e.nsteps = nsteps[i];
         e.keys = reinterpret_cast<uint64_t *>(nkeys);  // offset; rebased below
         nkeys += 2 * (size_t)nsteps[i];
-        const long long tasks = (long long)b->P.back() + (long long)row_groups * e.per_row;
+        const long long tasks = (long long)b->P.back() + flat_tasks(h->g.H, e.items);
         if (tasks > 0x7fffffffLL) return bfail(b, LGCA_ERR_INVALID, "batch work-list too long");
         b->E.push_back(e);
         b->P.push_back((int)tasks);

@@ -11,38 +11,34 @@ namespace lgca_gpu {
 // per (row, chunk), rows of <= 16 items sharing a warp.
 static constexpr int STEP_WARPS = 8;  // largest block: 8 warps
 
-// Row mapping: warp row wr of a grid covers rows g*2R + (wr & 1) + 2i
-// (g = wr / 2, i < R = rows per warp), so a warp holds rows of one parity.
-__device__ __forceinline__ int warp_first_row(int wr, int rpw) { return (wr >> 1) * 2 * rpw + (wr & 1); }
-static inline long long warp_rows_for(int H, int rpw) { return 2LL * ((H + 2 * rpw - 1) / (2 * rpw)); }
-
+// Grid: 1-D, blockDim.y warps per block; warp task = blockIdx.x * blockDim.y
+// + threadIdx.y in the flattened same-parity mapping (flat_site).
 template <int MODEL, int GM>
 __global__ void __launch_bounds__(32 * STEP_WARPS) k_step(const __grid_constant__ StepArgs a)
 {
     pdl_launch_dependents();
-    const int width = seg_width(a.g.nw), rpw = 32 / width;
-    const int y0 = warp_first_row(blockIdx.y * blockDim.y + threadIdx.y, rpw);
-    if (y0 >= a.g.H) return;  // whole warp
-    const int y = y0 + 2 * (threadIdx.x / width);
-    const int w = blockIdx.x * 32 + (threadIdx.x & (width - 1));
+    const long long task = (long long)blockIdx.x * blockDim.y + threadIdx.y;
+    if (task >= flat_tasks(a.g.H, a.g.nw)) return;  // whole warp
+    int y, w;
+    flat_site(task, threadIdx.x, a.g.H, a.g.nw, y, w);
     // the chirality word does not depend on the previous step: draw it first
     uint64_t ch = 0;
     if (MODEL != M_HPP && a.chir == nullptr)
         ch = lgca_rng_draw(a.chir_key, lgca_rng_index((uint32_t)y, (uint32_t)w));
     const StepIO io{a.src, a.dst, a.chir_key, a.force_key};
     pdl_wait();
-    step_word<MODEL, GM, true, true>(a, io, y, w, threadIdx.x, width, ch);
+    step_word<MODEL, GM, true, true>(a, io, y, w, threadIdx.x, 32, ch);
 }
 
 template <int MODEL, int GM>
 __global__ void __launch_bounds__(32 * STEP_WARPS) k_step2(const __grid_constant__ StepArgs a)
 {
     pdl_launch_dependents();
-    const int width = seg_width(a.g.nw / 2), rpw = 32 / width;
-    const int y0 = warp_first_row(blockIdx.y * blockDim.y + threadIdx.y, rpw);
-    if (y0 >= a.g.H) return;
-    const int y = y0 + 2 * (threadIdx.x / width);
-    const int t = blockIdx.x * 32 + (threadIdx.x & (width - 1));
+    const int np = a.g.nw >> 1;
+    const long long task = (long long)blockIdx.x * blockDim.y + threadIdx.y;
+    if (task >= flat_tasks(a.g.H, np)) return;
+    int y, t;
+    flat_site(task, threadIdx.x, a.g.H, np, y, t);
     uint64_t c0 = 0, c1 = 0;
     if (MODEL != M_HPP && a.chir == nullptr) {
         c0 = lgca_rng_draw(a.chir_key, lgca_rng_index((uint32_t)y, (uint32_t)(2 * t)));
@@ -50,7 +46,7 @@ __global__ void __launch_bounds__(32 * STEP_WARPS) k_step2(const __grid_constant
     }
     const StepIO io{a.src, a.dst, a.chir_key, a.force_key};
     pdl_wait();
-    step_pair<MODEL, GM, true, true>(a, io, y, t, threadIdx.x, width, c0, c1);
+    step_pair<MODEL, GM, true, true>(a, io, y, t, threadIdx.x, 32, c0, c1);
 }
 
 int sm_count()
@@ -92,12 +88,11 @@ static int pick_warps(int requested, long long chunks, long long warp_rows)
 template <int MODEL>
 static cudaError_t launch_model2(int gm, const StepArgs &a, cudaStream_t st)
 {
-    const int np = a.g.nw / 2, rpw = 32 / seg_width(np);
-    const long long chunks = (np + 31) / 32, warp_rows = warp_rows_for(a.g.H, rpw);
-    const int bw = pick_warps(a.bw, chunks, warp_rows);
-    const dim3 block(32, bw);
-    const dim3 grid((unsigned)chunks, (unsigned)((warp_rows + bw - 1) / bw));
-    if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
+    const long long tasks = flat_tasks(a.g.H, a.g.nw / 2);
+    const int bw = pick_warps(a.bw, 1, tasks);
+    const long long blocks = (tasks + bw - 1) / bw;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    const dim3 grid((unsigned)blocks), block(32, bw);
     switch (gm) {
     case GEOM_NONE: return launch_pdl(k_step2<MODEL, GEOM_NONE>, grid, block, 0, st, a);
     case GEOM_NOSLIP: return launch_pdl(k_step2<MODEL, GEOM_NOSLIP>, grid, block, 0, st, a);
@@ -109,12 +104,11 @@ template <int MODEL>
 static cudaError_t launch_model(int gm, const StepArgs &a, cudaStream_t st)
 {
     if (a.wpt == 2 && (a.g.nw % 2) == 0 && (a.g.W % 64) == 0) return launch_model2<MODEL>(gm, a, st);
-    const int rpw = 32 / seg_width(a.g.nw);
-    const long long warp_rows = warp_rows_for(a.g.H, rpw);
-    const int bw = pick_warps(a.bw, a.chunks, warp_rows);
-    const dim3 block(32, bw);
-    const dim3 grid((unsigned)a.chunks, (unsigned)((warp_rows + bw - 1) / bw));
-    if (grid.y > 65535u) return cudaErrorInvalidConfiguration;
+    const long long tasks = flat_tasks(a.g.H, a.g.nw);
+    const int bw = pick_warps(a.bw, 1, tasks);
+    const long long blocks = (tasks + bw - 1) / bw;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    const dim3 grid((unsigned)blocks), block(32, bw);
     switch (gm) {
     case GEOM_NONE: return launch_pdl(k_step<MODEL, GEOM_NONE>, grid, block, 0, st, a);
     case GEOM_NOSLIP: return launch_pdl(k_step<MODEL, GEOM_NOSLIP>, grid, block, 0, st, a);
