@@ -231,7 +231,11 @@ int lgca_apply_body_force_noalloc(int model, int dim_x, int dim_y, uint64_t *pla
 int lgca_sync(lgca_handle h);
 
 /* The cudaStream_t the handle enqueues on (as void*), and a way to replace
- * it by a caller-owned stream (NULL restores the handle's own stream). */
+ * it by a caller-owned stream (NULL restores the handle's own stream).
+ * Steps queued on a stream under CUDA graph capture are recorded with their
+ * buffers and random keys fixed at capture time: a replay repeats steps
+ * t .. t+k-1 of the capturing call, so capture an even number of steps to
+ * replay it on the current state. */
 void *lgca_stream(lgca_handle h);
 int lgca_set_stream(lgca_handle h, void *stream);
 

@@ -18,29 +18,28 @@
 
 namespace lgca_gpu {
 
-// One launch per step for all members: warp task g belongs to the lattice
-// found from the block's first lattice (block_lat) by a short forward scan;
-// the lattice's entry selects model, geometry mode and words per lane.
-// GMAX is the largest geometry mode among the members: batches without slip
-// cells use a kernel compiled without the slip-aware paths, held to 64
-// registers (4 blocks of 8 warps per SM) at the price of a few spilled words.
+// One launch per step for all members.  Each member's warp tasks are padded
+// to whole blocks of 8, so block b belongs to lattice block_lat[b] alone and
+// its warps need no search; the lattice's entry selects model, geometry mode
+// and words per lane.  GMAX is the largest geometry mode among the members:
+// batches without slip cells use a kernel compiled without the slip-aware
+// paths, held to 64 registers (4 blocks of 8 warps per SM) at the price of a
+// few spilled words.
 template <int GMAX>
-__global__ void __launch_bounds__(256, GMAX == GEOM_FULL ? 3 : 4) k_batch(const BatchEntry *__restrict__ E,
-                                               const int *__restrict__ prefix,
-                                               const int *__restrict__ block_lat, int n_active,
-                                               int s_local, const int *__restrict__ s_base)
+__global__ void __launch_bounds__(256, GMAX == GEOM_FULL ? 3 : 4)
+    k_batch(const BatchEntry *__restrict__ E, const int *__restrict__ block_lat, int s_local,
+            const int *__restrict__ s_base)
 {
     pdl_launch_dependents();
     pdl_wait();  // keys, step counter and states come from earlier kernels
     const int lane = threadIdx.x & 31;
     const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (g >= prefix[n_active]) return;
-    int l = block_lat[blockIdx.x];
-    while (prefix[l + 1] <= g) ++l;
-    const BatchEntry &e = E[l];
+    const BatchEntry &e = E[block_lat[blockIdx.x]];
+    const int local = g - e.task0;
+    if (local >= e.tasks) return;  // padding warp
     const int s = *s_base + s_local;
     int y, w;  // the lane's row and item (flattened same-parity mapping)
-    flat_site(g - prefix[l], lane, e.a.g.H, e.items, y, w);
+    flat_site(local, lane, e.a.g.H, e.items, y, w);
     const ulonglong2 k = __ldg(reinterpret_cast<const ulonglong2 *>(e.keys) + s);
     const StepIO io{(s & 1) ? e.buf1 : e.buf0, (s & 1) ? e.buf0 : e.buf1, k.x, k.y};
     const StepArgs &a = e.a;
@@ -88,22 +87,19 @@ __global__ void k_set_base(int *s_base, int v)
     if (threadIdx.x == 0 && blockIdx.x == 0) *s_base = v;
 }
 
-cudaError_t launch_batch(const BatchEntry *E, const int *prefix, const int *block_lat,
-                         int n_active, int total_tasks, int s_local, const int *s_base,
-                         int gmax, cudaStream_t st)
+cudaError_t launch_batch(const BatchEntry *E, const int *block_lat, int total_tasks, int s_local,
+                         const int *s_base, int gmax, cudaStream_t st)
 {
     if (total_tasks <= 0) return cudaSuccess;
-    const dim3 grid((unsigned)((total_tasks + 7) / 8));
+    const dim3 grid((unsigned)(total_tasks / 8));  // tasks come in whole blocks
     switch (gmax) {
     case GEOM_NONE:
-        return launch_pdl(k_batch<GEOM_NONE>, grid, dim3(256), 0, st, E, prefix, block_lat,
-                          n_active, s_local, s_base);
+        return launch_pdl(k_batch<GEOM_NONE>, grid, dim3(256), 0, st, E, block_lat, s_local, s_base);
     case GEOM_NOSLIP:
-        return launch_pdl(k_batch<GEOM_NOSLIP>, grid, dim3(256), 0, st, E, prefix, block_lat,
-                          n_active, s_local, s_base);
+        return launch_pdl(k_batch<GEOM_NOSLIP>, grid, dim3(256), 0, st, E, block_lat, s_local,
+                          s_base);
     default:
-        return launch_pdl(k_batch<GEOM_FULL>, grid, dim3(256), 0, st, E, prefix, block_lat,
-                          n_active, s_local, s_base);
+        return launch_pdl(k_batch<GEOM_FULL>, grid, dim3(256), 0, st, E, block_lat, s_local, s_base);
     }
 }
 

@@ -930,7 +930,7 @@ int enqueue_steps(lgca_batch *b, int n_active, int tasks, int n)
     int gmax = GEOM_NONE;  // the active members are the first n_active entries
     for (int i = 0; i < n_active; ++i) gmax = std::max(gmax, b->E[i].gm);
     for (int s = 0; s < n; ++s)
-        BCK(b, launch_batch(b->dE, b->dP, b->dB, n_active, tasks, s, b->s_base, gmax, b->stream));
+        BCK(b, launch_batch(b->dE, b->dB, tasks, s, b->s_base, gmax, b->stream));
     BCK(b, launch_advance(b->s_base, n, b->stream));
     return LGCA_OK;
 }
@@ -1087,7 +1087,10 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         e.nsteps = nsteps[i];
         e.keys = reinterpret_cast<uint64_t *>(nkeys);  // offset; rebased below
         nkeys += 2 * (size_t)nsteps[i];
-        const long long tasks = (long long)b->P.back() + flat_tasks(h->g.H, e.items);
+        const long long own = flat_tasks(h->g.H, e.items);
+        e.task0 = b->P.back();
+        e.tasks = (int)std::min(own, 0x7fffffffLL);
+        const long long tasks = (long long)b->P.back() + (own + 7) / 8 * 8;  // whole blocks
         if (tasks > 0x7fffffffLL) return bfail(b, LGCA_ERR_INVALID, "batch work-list too long");
         b->E.push_back(e);
         b->P.push_back((int)tasks);
@@ -1097,12 +1100,10 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
     const int max_steps = ne ? b->nsteps[0] : 0;
     if (ne > 0) {
         const int total = b->P.back();
-        const int nblocks = (total + 7) / 8;
+        const int nblocks = total / 8;  // every member's tasks fill whole blocks
         b->Bl.resize(nblocks);
-        for (int blk = 0, l = 0; blk < nblocks; ++blk) {
-            while (b->P[l + 1] <= blk * 8) ++l;
-            b->Bl[blk] = l;
-        }
+        for (int l = 0; l < ne; ++l)
+            for (int blk = b->P[l] / 8; blk < b->P[l + 1] / 8; ++blk) b->Bl[blk] = l;
         int st;
         if ((st = grow(b, b->dE, b->capE, (size_t)ne)) != LGCA_OK) return st;
         if ((st = grow(b, b->dP, b->capB, (size_t)ne + 1 + nblocks)) != LGCA_OK) return st;
