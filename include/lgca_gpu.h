@@ -275,6 +275,12 @@ int lgca_batch_size(lgca_batch_handle b, int *n);
 int lgca_batch_step(lgca_batch_handle b, int nsteps);
 int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps);
 int lgca_batch_set_graph_steps(lgca_batch_handle b, int steps_per_graph); /* 0: no graphs */
+/* Warp tasks (32 lane items of one member) each warp of the batched kernel
+ * takes per step: 1, 2, 4 or 8 (default 4; 4 ran 10 % faster than 1 on the
+ * 512-lattice workload).  More tasks per warp pay the member lookup less
+ * often; fewer give more, smaller blocks.  A tuning knob: results do not
+ * depend on it.  (No reference counterpart.) */
+int lgca_batch_set_warp_tasks(lgca_batch_handle b, int n);
 int lgca_batch_sync(lgca_batch_handle b);
 const char *lgca_batch_last_error(lgca_batch_handle b);
 void *lgca_batch_stream(lgca_batch_handle b);

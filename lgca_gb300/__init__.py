@@ -99,6 +99,7 @@ def lib() -> C.CDLL:
             "lgca_batch_step": (C.c_int, [vp, C.c_int]),
             "lgca_batch_step_each": (C.c_int, [vp, vp]),
             "lgca_batch_set_graph_steps": (C.c_int, [vp, C.c_int]),
+            "lgca_batch_set_warp_tasks": (C.c_int, [vp, C.c_int]),
             "lgca_batch_sync": (C.c_int, [vp]),
             "lgca_batch_last_error": (C.c_char_p, [vp]),
             "lgca_batch_stream": (vp, [vp]),
@@ -370,6 +371,10 @@ class GpuBatch:
 
     def step(self, nsteps: int) -> None:
         self._chk(lib().lgca_batch_step(self._b, int(nsteps)))
+
+    def set_warp_tasks(self, n: int) -> None:
+        """Warp tasks per warp of the batched kernel (1, 2, 4 or 8)."""
+        self._chk(lib().lgca_batch_set_warp_tasks(self._b, int(n)))
 
     def step_each(self, nsteps) -> None:
         arr = np.ascontiguousarray(nsteps, dtype=np.int32)

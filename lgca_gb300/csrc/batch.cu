@@ -19,49 +19,53 @@
 namespace lgca_gpu {
 
 // One launch per step for all members.  Each member's warp tasks are padded
-// to whole blocks of 8, so block b belongs to lattice block_lat[b] alone and
-// its warps need no search; the lattice's entry selects model, geometry mode
-// and words per lane.  GMAX is the largest geometry mode among the members:
-// batches without slip cells use a kernel compiled without the slip-aware
-// paths, held to 64 registers (4 blocks of 8 warps per SM) at the price of a
-// few spilled words.
-template <int GMAX>
+// to whole blocks (8 warps x T tasks per warp), so block b belongs to lattice
+// block_lat[b] alone and needs no search; warp w of a block takes the
+// block's tasks w, w + 8, ... (T of them), reusing the lattice's entry, keys
+// and buffer pointers, so the entry's load latency is paid once per T tasks.
+// The entry selects model, geometry mode and words per lane.  GMAX is the
+// largest geometry mode among the members: batches without slip cells use a
+// kernel compiled without the slip-aware paths, held to 64 registers (4
+// blocks of 8 warps per SM).
+template <int GMAX, int T>
 __global__ void __launch_bounds__(256, GMAX == GEOM_FULL ? 3 : 4)
     k_batch(const BatchEntry *__restrict__ E, const int *__restrict__ block_lat, int s_local,
             const int *__restrict__ s_base)
 {
     pdl_launch_dependents();
     pdl_wait();  // keys, step counter and states come from earlier kernels
-    const int lane = threadIdx.x & 31;
-    const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const BatchEntry &e = E[block_lat[blockIdx.x]];
-    const int local = g - e.task0;
-    if (local >= e.tasks) return;  // padding warp
+    const int base = blockIdx.x * 8 * T - e.task0;  // the block's first task of its lattice
     const int s = *s_base + s_local;
-    int y, w;  // the lane's row and item (flattened same-parity mapping)
-    flat_site(local, lane, e.a.g.H, e.items, y, w);
     const ulonglong2 k = __ldg(reinterpret_cast<const ulonglong2 *>(e.keys) + s);
     const StepIO io{(s & 1) ? e.buf1 : e.buf0, (s & 1) ? e.buf0 : e.buf1, k.x, k.y};
     const StepArgs &a = e.a;
+    for (int i = 0; i < T; ++i) {
+        const int local = base + warp + 8 * i;
+        if (local >= e.tasks) break;  // padding: warp-uniform
+        int y, w;  // the lane's row and item (flattened same-parity mapping)
+        flat_site(local, lane, e.a.g.H, e.items, y, w);
 #define LGCA_BATCH_CASE(F, MODEL, GM)                                                          \
     case F * 6 + GM * 2:                                                                       \
-        if (GM <= GMAX) step_word<MODEL, GM, true>(a, io, y, w, lane);                           \
+        if (GM <= GMAX) step_word<MODEL, GM, true>(a, io, y, w, lane);                         \
         break;                                                                                 \
     case F * 6 + GM * 2 + 1:                                                                   \
-        if (GM <= GMAX) step_pair<MODEL, GM, true>(a, io, y, w, lane);                           \
+        if (GM <= GMAX) step_pair<MODEL, GM, true>(a, io, y, w, lane);                         \
         break;
 #define LGCA_BATCH_CASES(F, MODEL)                                                             \
     LGCA_BATCH_CASE(F, MODEL, GEOM_NONE)                                                       \
     LGCA_BATCH_CASE(F, MODEL, GEOM_NOSLIP)                                                     \
     LGCA_BATCH_CASE(F, MODEL, GEOM_FULL)
-    switch (e.code) {
-        LGCA_BATCH_CASES(0, M_HPP)
-        LGCA_BATCH_CASES(1, M_FHP_I)
-        LGCA_BATCH_CASES(2, M_FHP_II)
-    default: break;
-    }
+        switch (e.code) {
+            LGCA_BATCH_CASES(0, M_HPP)
+            LGCA_BATCH_CASES(1, M_FHP_I)
+            LGCA_BATCH_CASES(2, M_FHP_II)
+        default: break;
+        }
 #undef LGCA_BATCH_CASES
 #undef LGCA_BATCH_CASE
+    }
 }
 
 // keys[l][s] = (chirality key, forcing key) of member l at its step t0 + s
@@ -87,19 +91,32 @@ __global__ void k_set_base(int *s_base, int v)
     if (threadIdx.x == 0 && blockIdx.x == 0) *s_base = v;
 }
 
-cudaError_t launch_batch(const BatchEntry *E, const int *block_lat, int total_tasks, int s_local,
-                         const int *s_base, int gmax, cudaStream_t st)
+template <int T>
+static cudaError_t launch_batch_t(const BatchEntry *E, const int *block_lat, int total_tasks,
+                                  int s_local, const int *s_base, int gmax, cudaStream_t st)
 {
-    if (total_tasks <= 0) return cudaSuccess;
-    const dim3 grid((unsigned)(total_tasks / 8));  // tasks come in whole blocks
+    const dim3 grid((unsigned)(total_tasks / (8 * T)));  // tasks come in whole blocks
     switch (gmax) {
     case GEOM_NONE:
-        return launch_pdl(k_batch<GEOM_NONE>, grid, dim3(256), 0, st, E, block_lat, s_local, s_base);
+        return launch_pdl(k_batch<GEOM_NONE, T>, grid, dim3(256), 0, st, E, block_lat, s_local, s_base);
     case GEOM_NOSLIP:
-        return launch_pdl(k_batch<GEOM_NOSLIP>, grid, dim3(256), 0, st, E, block_lat, s_local,
+        return launch_pdl(k_batch<GEOM_NOSLIP, T>, grid, dim3(256), 0, st, E, block_lat, s_local,
                           s_base);
     default:
-        return launch_pdl(k_batch<GEOM_FULL>, grid, dim3(256), 0, st, E, block_lat, s_local, s_base);
+        return launch_pdl(k_batch<GEOM_FULL, T>, grid, dim3(256), 0, st, E, block_lat, s_local, s_base);
+    }
+}
+
+cudaError_t launch_batch(const BatchEntry *E, const int *block_lat, int total_tasks, int s_local,
+                         const int *s_base, int gmax, int warp_tasks, cudaStream_t st)
+{
+    if (total_tasks <= 0) return cudaSuccess;
+    switch (warp_tasks) {
+    case 1: return launch_batch_t<1>(E, block_lat, total_tasks, s_local, s_base, gmax, st);
+    case 2: return launch_batch_t<2>(E, block_lat, total_tasks, s_local, s_base, gmax, st);
+    case 4: return launch_batch_t<4>(E, block_lat, total_tasks, s_local, s_base, gmax, st);
+    case 8: return launch_batch_t<8>(E, block_lat, total_tasks, s_local, s_base, gmax, st);
+    default: return cudaErrorInvalidValue;
     }
 }
 

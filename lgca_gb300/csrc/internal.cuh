@@ -103,16 +103,17 @@ struct BatchEntry {
     uint64_t *keys;  // 2 * nsteps keys (chirality, forcing) per step of the call
     int nsteps;
     int items;    // lane items per row (words, or word pairs when wpt == 2)
-    int task0;    // first warp task (a multiple of 8) and number of real tasks
+    int task0;    // first warp task (a multiple of the block's tasks) and real tasks
     int tasks;
     int gm, wpt;  // geometry mode, words per lane
     int code;     // model family * 6 + geometry mode * 2 + (wpt == 2)
 };
-// total_tasks: warp tasks of the active members (a multiple of 8, each
-// member's tasks padded to whole blocks); block_lat[b] = member of block b;
-// gmax: the largest geometry mode among the launch's members
+// total_tasks: warp tasks of the active members (each member's tasks padded
+// to whole blocks of 8 * warp_tasks); block_lat[b] = member of block b;
+// gmax: the largest geometry mode among the launch's members; warp_tasks:
+// tasks per warp (1, 2, 4 or 8)
 cudaError_t launch_batch(const BatchEntry *E, const int *block_lat, int total_tasks, int s_local,
-                         const int *s_base, int gmax, cudaStream_t stream);
+                         const int *s_base, int gmax, int warp_tasks, cudaStream_t stream);
 cudaError_t launch_batch_keys(const BatchEntry *E, int n, int max_steps, cudaStream_t stream);
 cudaError_t launch_advance(int *s_base, int by, cudaStream_t stream);
 cudaError_t launch_set_base(int *s_base, int v, cudaStream_t stream);

@@ -883,6 +883,7 @@ struct lgca_batch {
     cudaEvent_t done = nullptr;
     int *s_base = nullptr;       // device: first batch-local step of a graph replay
     int graph_steps = 32;        // steps captured per CUDA graph (0: no graphs)
+    int warp_tasks = 4;          // warp tasks per warp of the batched kernel (1, 2, 4 or 8)
     // device work-list: entries, task prefix, block -> lattice map, key table
     BatchEntry *dE = nullptr;
     int *dP = nullptr, *dB = nullptr;  // dB points into dP's allocation
@@ -930,7 +931,7 @@ int enqueue_steps(lgca_batch *b, int n_active, int tasks, int n)
     int gmax = GEOM_NONE;  // the active members are the first n_active entries
     for (int i = 0; i < n_active; ++i) gmax = std::max(gmax, b->E[i].gm);
     for (int s = 0; s < n; ++s)
-        BCK(b, launch_batch(b->dE, b->dB, tasks, s, b->s_base, gmax, b->stream));
+        BCK(b, launch_batch(b->dE, b->dB, tasks, s, b->s_base, gmax, b->warp_tasks, b->stream));
     BCK(b, launch_advance(b->s_base, n, b->stream));
     return LGCA_OK;
 }
@@ -1030,6 +1031,14 @@ int lgca_batch_size(lgca_batch_handle b, int *n)
     return LGCA_OK;
 }
 
+int lgca_batch_set_warp_tasks(lgca_batch_handle b, int n)
+{
+    if (!b || !(n == 1 || n == 2 || n == 4 || n == 8))
+        return bfail(b, LGCA_ERR_INVALID, "warp tasks must be 1, 2, 4 or 8");
+    b->warp_tasks = n;
+    return LGCA_OK;
+}
+
 int lgca_batch_set_graph_steps(lgca_batch_handle b, int n)
 {
     if (!b || n < 0) return bfail(b, LGCA_ERR_INVALID, "invalid argument");
@@ -1090,7 +1099,8 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         const long long own = flat_tasks(h->g.H, e.items);
         e.task0 = b->P.back();
         e.tasks = (int)std::min(own, 0x7fffffffLL);
-        const long long tasks = (long long)b->P.back() + (own + 7) / 8 * 8;  // whole blocks
+        const long long per_block = 8LL * b->warp_tasks;
+        const long long tasks = (long long)b->P.back() + (own + per_block - 1) / per_block * per_block;
         if (tasks > 0x7fffffffLL) return bfail(b, LGCA_ERR_INVALID, "batch work-list too long");
         b->E.push_back(e);
         b->P.push_back((int)tasks);
@@ -1099,11 +1109,11 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
     const int ne = (int)b->E.size();
     const int max_steps = ne ? b->nsteps[0] : 0;
     if (ne > 0) {
-        const int total = b->P.back();
-        const int nblocks = total / 8;  // every member's tasks fill whole blocks
+        const int total = b->P.back(), per_block = 8 * b->warp_tasks;
+        const int nblocks = total / per_block;  // every member's tasks fill whole blocks
         b->Bl.resize(nblocks);
         for (int l = 0; l < ne; ++l)
-            for (int blk = b->P[l] / 8; blk < b->P[l + 1] / 8; ++blk) b->Bl[blk] = l;
+            for (int blk = b->P[l] / per_block; blk < b->P[l + 1] / per_block; ++blk) b->Bl[blk] = l;
         int st;
         if ((st = grow(b, b->dE, b->capE, (size_t)ne)) != LGCA_OK) return st;
         if ((st = grow(b, b->dP, b->capB, (size_t)ne + 1 + nblocks)) != LGCA_OK) return st;

@@ -33,8 +33,9 @@ def make_jobs(gpu, n, rng, max_side=700):
     return jobs
 
 
-@pytest.mark.parametrize("graph_steps", [0, 8, 32])
-def test_mixed_batch_equals_alone(gpu, graph_steps):
+@pytest.mark.parametrize("graph_steps,warp_tasks", [(0, 4), (8, 4), (32, 4), (0, 1), (32, 2),
+                                                    (8, 8)])
+def test_mixed_batch_equals_alone(gpu, graph_steps, warp_tasks):
     rng = np.random.default_rng(graph_steps + 1)
     jobs = make_jobs(gpu, 24, rng)
     steps = [int(x) for x in rng.integers(0, 90, len(jobs))]
@@ -48,6 +49,7 @@ def test_mixed_batch_equals_alone(gpu, graph_steps):
         want.append((twin.download(), twin.step_count))
         twin.close()
     with gpu.GpuBatch(graph_steps=graph_steps) as B:
+        B.set_warp_tasks(warp_tasks)
         for L in jobs:
             B.add(L)
         B.step_each(steps)
