@@ -373,7 +373,7 @@ class GpuBatch:
         self._chk(lib().lgca_batch_step(self._b, int(nsteps)))
 
     def set_warp_tasks(self, n: int) -> None:
-        """Warp tasks per warp of the batched kernel (1, 2, 4 or 8)."""
+        """Warp tasks per warp of the batched kernel (1, 2, 4 or 8; 0 = per call)."""
         self._chk(lib().lgca_batch_set_warp_tasks(self._b, int(n)))
 
     def step_each(self, nsteps) -> None:

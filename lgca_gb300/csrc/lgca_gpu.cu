@@ -883,7 +883,8 @@ struct lgca_batch {
     cudaEvent_t done = nullptr;
     int *s_base = nullptr;       // device: first batch-local step of a graph replay
     int graph_steps = 32;        // steps captured per CUDA graph (0: no graphs)
-    int warp_tasks = 4;          // warp tasks per warp of the batched kernel (1, 2, 4 or 8)
+    int warp_tasks = 0;          // warp tasks per warp of the batched kernel (0: per call)
+    int call_wt = 1;             // the value used by the current call
     // device work-list: entries, task prefix, block -> lattice map, key table
     BatchEntry *dE = nullptr;
     int *dP = nullptr, *dB = nullptr;  // dB points into dP's allocation
@@ -931,7 +932,7 @@ int enqueue_steps(lgca_batch *b, int n_active, int tasks, int n)
     int gmax = GEOM_NONE;  // the active members are the first n_active entries
     for (int i = 0; i < n_active; ++i) gmax = std::max(gmax, b->E[i].gm);
     for (int s = 0; s < n; ++s)
-        BCK(b, launch_batch(b->dE, b->dB, tasks, s, b->s_base, gmax, b->warp_tasks, b->stream));
+        BCK(b, launch_batch(b->dE, b->dB, tasks, s, b->s_base, gmax, b->call_wt, b->stream));
     BCK(b, launch_advance(b->s_base, n, b->stream));
     return LGCA_OK;
 }
@@ -1033,8 +1034,8 @@ int lgca_batch_size(lgca_batch_handle b, int *n)
 
 int lgca_batch_set_warp_tasks(lgca_batch_handle b, int n)
 {
-    if (!b || !(n == 1 || n == 2 || n == 4 || n == 8))
-        return bfail(b, LGCA_ERR_INVALID, "warp tasks must be 1, 2, 4 or 8");
+    if (!b || !(n == 0 || n == 1 || n == 2 || n == 4 || n == 8))
+        return bfail(b, LGCA_ERR_INVALID, "warp tasks must be 0, 1, 2, 4 or 8");
     b->warp_tasks = n;
     return LGCA_OK;
 }
@@ -1061,6 +1062,24 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         BCK(b, cudaEventRecord(b->ev[i], b->members[i]->stream));
         BCK(b, cudaStreamWaitEvent(b->stream, b->ev[i], 0));
     }
+    // lane items per row of a member: word pairs where the width allows
+    auto pair_of = [](const lgca_lattice *h) {
+        return h->variant != VARIANT_PLAIN && h->wpt == 2 && (h->g.nw % 2) == 0 && (h->g.W % 64) == 0;
+    };
+    // warp tasks per warp: the caller's choice, else 4 / 2 / 1 as the call's
+    // work keeps at least four waves of resident warps busy (4 blocks of 8
+    // warps per SM); small calls keep one task per warp for parallelism
+    b->call_wt = b->warp_tasks;
+    if (b->call_wt == 0) {
+        long long all = 0;
+        for (size_t i = 0; i < nm; ++i)
+            if (nsteps[i] > 0) {
+                const lgca_lattice *h = b->members[i];
+                all += flat_tasks(h->g.H, pair_of(h) ? h->g.nw / 2 : h->g.nw);
+            }
+        const long long wave = 32LL * sm_count();
+        b->call_wt = all >= 16 * wave ? 4 : (all >= 8 * wave ? 2 : 1);
+    }
     // one work-list, lattices sorted by steps (descending)
     std::vector<int> order(nm);
     for (size_t i = 0; i < nm; ++i) order[i] = (int)i;
@@ -1081,8 +1100,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         e.a.chunks = (h->g.nw + 31) / 32;
         e.a.force_thr = h->force_thr;
         e.a.fx = h->force_x;
-        const bool pair = h->variant != VARIANT_PLAIN && h->wpt == 2 && (h->g.nw % 2) == 0 &&
-                          (h->g.W % 64) == 0;
+        const bool pair = pair_of(h);
         e.a.wpt = pair ? 2 : 1;
         e.wpt = e.a.wpt;
         e.gm = geom_mode(h);
@@ -1099,7 +1117,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         const long long own = flat_tasks(h->g.H, e.items);
         e.task0 = b->P.back();
         e.tasks = (int)std::min(own, 0x7fffffffLL);
-        const long long per_block = 8LL * b->warp_tasks;
+        const long long per_block = 8LL * b->call_wt;
         const long long tasks = (long long)b->P.back() + (own + per_block - 1) / per_block * per_block;
         if (tasks > 0x7fffffffLL) return bfail(b, LGCA_ERR_INVALID, "batch work-list too long");
         b->E.push_back(e);
@@ -1109,7 +1127,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
     const int ne = (int)b->E.size();
     const int max_steps = ne ? b->nsteps[0] : 0;
     if (ne > 0) {
-        const int total = b->P.back(), per_block = 8 * b->warp_tasks;
+        const int total = b->P.back(), per_block = 8 * b->call_wt;
         const int nblocks = total / per_block;  // every member's tasks fill whole blocks
         b->Bl.resize(nblocks);
         for (int l = 0; l < ne; ++l)
