@@ -25,6 +25,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -81,7 +82,9 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{index}.csv")
+        # raw samples go to $LGCA_CLOCKS_CSV when set, else to a temporary file
+        self.path = os.environ.get("LGCA_CLOCKS_CSV") or os.path.join(
+            tempfile.gettempdir(), f"lgca_clocks_{index}.csv")
 
     def __enter__(self):
         try:

@@ -1,5 +1,5 @@
 """Run one lattice workload on the GPU for a fixed number of steps: a small,
-self-contained driver for profilers (ncu) and for quick timings.
+self-contained program for profilers (ncu) and for quick timings.
 
     python -m lgca_gb300.profile_case --model 3 --W 32768 --H 16384 --steps 3
     python -m lgca_gb300.profile_case --geometry karman --W 8192 --H 2048 --force-x 16 --force-p 0.02

@@ -34,7 +34,7 @@ def make_jobs(gpu, n, rng, max_side=700):
 
 
 @pytest.mark.parametrize("graph_steps,warp_tasks", [(0, 4), (8, 4), (32, 4), (0, 1), (32, 2),
-                                                    (8, 8)])
+                                                    (8, 8), (32, 0)])
 def test_mixed_batch_equals_alone(gpu, graph_steps, warp_tasks):
     rng = np.random.default_rng(graph_steps + 1)
     jobs = make_jobs(gpu, 24, rng)
