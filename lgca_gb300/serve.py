@@ -7,9 +7,12 @@ Job stream (defaults): Poisson arrivals at `rate` jobs/s for `duration` s;
 model, geometry and occupation as the batched workload; width log-uniform in
 [256, 8192] and height in [256, 4096] (multiples of 64); steps log-uniform in
 [100, 20000]; seed = arrival index.  Every `out_every` steps (and at the end)
-a job returns its 16 x 16 integer block sums (N, Jx2, Jy).  Admission is
-first come, first served and keeps the resident lattices' device bytes within
-`budget` (150 GB) and their sites within `max_sites` (slots).
+a job returns its 16 x 16 integer block sums (N, Jx2, Jy).  Admission keeps
+the resident lattices' device bytes within `budget` (150 GB) and their sites
+within `max_sites` (slots), in one of two orders: first come, first served
+("fcfs"), or least remaining work first ("srpt"), where a waiting job with a
+small fraction of a resident's remaining work evicts that resident -- its
+state is checkpointed to host memory and restored later, bit-exactly.
 
 The scheduler (Server) talks to a backend: GpuBackend runs the engine;
 tests substitute a CPU fake to exercise admission, budgets and failures.
@@ -19,9 +22,11 @@ tests substitute a CPU fake to exercise admission, budgets and failures.
 from __future__ import annotations
 
 import argparse
+import heapq
 import json
 import math
 import time
+from collections import deque
 from dataclasses import dataclass
 
 import numpy as np
@@ -48,10 +53,17 @@ class Job:
     handle: object = None
     error: str | None = None
     bytes: int = 0
+    ckpt: bytes | None = None  # state of an evicted job, restored on resume
+    evictions: int = 0
 
     @property
     def sites(self) -> int:
         return self.W * self.H
+
+    @property
+    def remaining(self) -> int:
+        """Site updates still to do."""
+        return (self.steps - self.done_steps) * self.sites
 
     def next_event(self, out_every: int) -> int:
         """Steps to the next output or the end."""
@@ -167,58 +179,138 @@ class GpuBackend:
         self.parity.pop(id(handle), None)
         handle.close()
 
+    def evict(self, handle) -> bytes:
+        """Checkpoint a resident lattice to host memory and free it (its
+        queued steps and field copies complete first, in stream order)."""
+        blob = handle.checkpoint()
+        self.destroy(handle)
+        return blob
+
+    def resume(self, job: Job, blob: bytes):
+        L = self.gpu.GpuLattice(job.model, job.W, job.H, seed=job.seed)
+        L.restore(blob)
+        self.batch.add(L)
+        return L
+
     def close(self):
         self.batch.close()
+
+
+class _Queue:
+    """Waiting jobs: first come, first served ("fcfs"), or least remaining
+    work first ("srpt", ties by arrival)."""
+
+    def __init__(self, policy: str):
+        if policy not in ("fcfs", "srpt"):
+            raise ValueError(f"unknown policy {policy!r}")
+        self.policy = policy
+        self.q = deque() if policy == "fcfs" else []
+
+    def push(self, job: Job) -> None:
+        if self.policy == "fcfs":
+            self.q.append(job)
+        else:
+            heapq.heappush(self.q, (job.remaining, job.arrival, job.index, job))
+
+    def push_front(self, job: Job) -> None:
+        if self.policy == "fcfs":
+            self.q.appendleft(job)
+        else:
+            self.push(job)
+
+    def peek(self) -> Job:
+        return self.q[0] if self.policy == "fcfs" else self.q[0][3]
+
+    def pop(self) -> Job:
+        return self.q.popleft() if self.policy == "fcfs" else heapq.heappop(self.q)[3]
+
+    def jobs(self):
+        return list(self.q) if self.policy == "fcfs" else [e[3] for e in self.q]
+
+    def clear(self) -> None:
+        self.q.clear()
+
+    def __len__(self) -> int:
+        return len(self.q)
 
 
 class Server:
     def __init__(self, backend, budget: float = 150e9, out_every: int = 500,
                  clock=time.perf_counter, sleep=time.sleep, max_quantum: int = 100,
-                 max_sites: float = float("inf")):
+                 max_sites: float = float("inf"), policy: str = "fcfs",
+                 preempt_ratio: float = 0.25, max_evictions: int = 4):
         self.backend, self.budget, self.out_every = backend, budget, out_every
         self.clock, self.sleep, self.max_quantum = clock, sleep, max_quantum
         # slots: residents' total sites; beyond what fills the device, more
         # residents only share it more thinly (longer latency, same throughput)
         self.max_sites = max_sites
+        # "srpt": admit the least remaining work first, and when a waiting
+        # job has under preempt_ratio of a resident's remaining work and no
+        # slot is free, evict that resident (checkpoint to host, resume later
+        # bit-exactly); at most max_evictions per admission pass
+        self.policy, self.preempt_ratio, self.max_evictions = policy, preempt_ratio, max_evictions
         self.used = 0
         self.sites = 0
+        self.evictions = 0
         self.active: list[Job] = []
-        self.waiting: list[Job] = []
+        self.waiting = _Queue(policy)
         self.done: list[Job] = []
         self.rejected: list[Job] = []
         self.site_updates = 0
         self.batch_calls = 0
 
     def _admit(self, now: float) -> None:
-        # first come, first admitted; a job that never fits is rejected
+        # in queue order; a job that never fits is rejected
+        evicted = 0
         while self.waiting:
-            job = self.waiting[0]
+            job = self.waiting.peek()
             need = lattice_bytes(job.model, job.W, job.H, job.geometry)
             if need > self.budget:
-                self.waiting.pop(0)
+                self.waiting.pop()
                 job.error = "larger than the memory budget"
                 self.rejected.append(job)
                 continue
-            if self.used + need > self.budget:
+            fits = self.used + need <= self.budget and not (
+                self.active and self.sites + job.sites > self.max_sites)
+            if not fits:
+                if self.policy == "srpt" and evicted < self.max_evictions and self.active:
+                    victim = max(self.active, key=lambda j: j.remaining)
+                    if victim.remaining * self.preempt_ratio > job.remaining:
+                        self._evict(victim)
+                        evicted += 1
+                        continue
                 return
-            if self.active and self.sites + job.sites > self.max_sites:
-                return
-            self.waiting.pop(0)
+            self.waiting.pop()
             try:
-                job.handle = self.backend.create(job)
+                if job.ckpt is not None:
+                    job.handle = self.backend.resume(job, job.ckpt)
+                else:
+                    job.handle = self.backend.create(job)
             except Exception as e:  # allocation failure: retry once memory frees
                 job.error = f"create failed: {e}"
                 if not self.active:
                     self.rejected.append(job)
                 else:
-                    self.waiting.insert(0, job)
+                    self.waiting.push_front(job)
                 return
+            job.ckpt = None
             job.error = None
             job.bytes = need
-            job.admitted = now
+            if job.admitted is None:
+                job.admitted = now
             self.used += need
             self.sites += job.sites
             self.active.append(job)
+
+    def _evict(self, job: Job) -> None:
+        job.ckpt = self.backend.evict(job.handle)
+        job.handle = None
+        job.evictions += 1
+        self.evictions += 1
+        self.used -= job.bytes
+        self.sites -= job.sites
+        self.active.remove(job)
+        self.waiting.push(job)
 
     def _finish(self, job: Job, now: float) -> None:
         job.finished = now
@@ -249,7 +341,7 @@ class Server:
         while k < len(pending) or self.waiting or self.active or inflight:
             now = self.clock() - t0
             while k < len(pending) and pending[k].arrival <= now:
-                self.waiting.append(pending[k])
+                self.waiting.push(pending[k])
                 k += 1
             self._admit(now)
             if now > last_arrival + drain_limit and inflight is None:
@@ -282,9 +374,10 @@ class Server:
                 if k < len(pending):  # idle until the next arrival
                     self.sleep(max(0.0, pending[k].arrival - now))
                 elif self.waiting:  # nothing resident and nothing admissible
-                    for j in self.waiting:
+                    left = self.waiting.jobs()
+                    for j in left:
                         j.error = j.error or "could not be admitted"
-                    self.rejected.extend(self.waiting)
+                    self.rejected.extend(left)
                     self.waiting.clear()
         elapsed = self.clock() - t0
         return self.report(jobs, elapsed)
@@ -298,7 +391,7 @@ class Server:
             "sustained_gsite_updates_s": self.site_updates / elapsed / 1e9 if elapsed else 0.0,
             "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
             "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
-            "batch_calls": self.batch_calls,
+            "batch_calls": self.batch_calls, "policy": self.policy, "evictions": self.evictions,
         }
 
 
@@ -389,10 +482,10 @@ SERVE_MAX_SITES = float(1 << 29)
 
 def serve(rate: float, duration: float, budget: float = 150e9, drain_limit: float = 60.0,
           verify: int = 8, fcfs: bool = True, max_sites: float = SERVE_MAX_SITES,
-          quantum: int = 100, **job_kw) -> dict:
+          quantum: int = 100, policy: str = "fcfs", **job_kw) -> dict:
     jobs = make_jobs(rate, duration, **job_kw)
     backend = GpuBackend()
-    srv = Server(backend, budget=budget, max_sites=max_sites, max_quantum=quantum)
+    srv = Server(backend, budget=budget, max_sites=max_sites, max_quantum=quantum, policy=policy)
     rep = srv.run(jobs, drain_limit=drain_limit)
     backend.close()
     rep.update(rate=rate, duration=duration, max_sites=max_sites, quantum=quantum)
@@ -419,13 +512,16 @@ def main(argv=None):
                     help="resident site caps to try (slots)")
     ap.add_argument("--quantum", type=int, default=100)
     ap.add_argument("--no-fcfs", action="store_true")
+    ap.add_argument("--policy", nargs="+", default=["fcfs"], choices=["fcfs", "srpt"],
+                    help="admission order (srpt: least remaining work first, with eviction)")
     a = ap.parse_args(argv)
     import lgca_gb300 as gpu
     gpu.build()
     for r in a.rate:
         for cap in a.max_sites:
-            print(json.dumps(serve(r, a.duration, a.budget_gb * 1e9, a.drain, a.verify,
-                                   not a.no_fcfs, cap, a.quantum)), flush=True)
+            for pol in a.policy:
+                print(json.dumps(serve(r, a.duration, a.budget_gb * 1e9, a.drain, a.verify,
+                                       not a.no_fcfs, cap, a.quantum, pol)), flush=True)
 
 
 if __name__ == "__main__":

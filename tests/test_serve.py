@@ -50,6 +50,15 @@ class FakeBackend:
     def destroy(self, h):
         self.live.discard(h["job"])
 
+    def evict(self, h):
+        self.destroy(h)
+        return dict(h)  # the "checkpoint": the handle's state
+
+    def resume(self, job, blob):
+        h = dict(blob)
+        self.live.add(job.index)
+        return h
+
 
 def jobs_small(n=40, rate=200.0, seed=1):
     return S.make_jobs(rate, 10.0, rng_seed=seed, w_range=(64, 512), h_range=(64, 512),
@@ -100,6 +109,32 @@ def test_site_slots_bound_the_resident_set():
     srv._admit = admit
     rep = srv.run(jobs)
     assert rep["completed"] == len(jobs) and seen[0] >= 2 and srv.sites == 0
+
+
+def test_srpt_evicts_and_resumes_without_losing_steps():
+    """Least-remaining-work admission with eviction: big residents are
+    checkpointed out when much smaller jobs wait, and come back later; every
+    job still does exactly its steps, and small jobs finish sooner."""
+    def run(policy):
+        clock = FakeClock()
+        jobs = S.make_jobs(400.0, 2.0, rng_seed=9, w_range=(64, 1024), h_range=(64, 512),
+                           steps_range=(10, 5000), max_jobs=120)
+        cap = 3 * max(j.sites for j in jobs)
+        srv = S.Server(FakeBackend(clock), budget=1e12, clock=clock, sleep=clock.sleep,
+                       max_sites=cap, policy=policy)
+        return srv.run(jobs), jobs, srv
+    rep_f, jobs_f, _ = run("fcfs")
+    rep_s, jobs_s, srv = run("srpt")
+    assert rep_s["completed"] == len(jobs_s) and srv.evictions > 0 and srv.sites == 0
+    for j in jobs_s:
+        assert j.done_steps == j.steps and j.last_fields == (j.steps,)
+        assert j.outputs >= -(-j.steps // 500) and j.ckpt is None
+    assert rep_s["p50_latency_s"] < rep_f["p50_latency_s"]
+
+
+def test_unknown_policy_is_rejected():
+    with pytest.raises(ValueError):
+        S.Server(FakeBackend(FakeClock()), policy="lifo")
 
 
 def test_job_larger_than_budget_is_rejected():
@@ -192,3 +227,19 @@ def test_short_served_stream_is_bit_exact(gpu):
     assert rep["completed"] == len(jobs)
     assert all(j.outputs == -(-j.steps // 500) for j in jobs)
     assert S.verify_sample(srv.done, n=len(srv.done))  # every job, rebuilt from a host map
+
+
+@pytest.mark.gpu
+def test_evicted_and_resumed_jobs_are_bit_exact(gpu):
+    """With least-remaining-work admission and a small site cap, residents
+    are checkpointed out and resumed; every job's final fields still equal
+    its lone run."""
+    jobs = S.make_jobs(200.0, 1.0, rng_seed=12, w_range=(256, 1024), h_range=(256, 512),
+                       steps_range=(100, 3000))
+    backend = S.GpuBackend()
+    srv = S.Server(backend, budget=20e9, max_sites=3 * 1024 * 512, policy="srpt",
+                   preempt_ratio=0.5)
+    rep = srv.run(jobs)
+    backend.close()
+    assert rep["completed"] == len(jobs) and srv.evictions > 0
+    assert S.verify_sample(srv.done, n=len(srv.done))
