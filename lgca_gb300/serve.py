@@ -371,6 +371,9 @@ class Server:
                         self._finish(j, now)
             inflight = launched
             if inflight is None and not self.active:
+                self._admit(now)  # the jobs just finished freed their slots
+                if self.active:
+                    continue
                 if k < len(pending):  # idle until the next arrival
                     self.sleep(max(0.0, pending[k].arrival - now))
                 elif self.waiting:  # nothing resident and nothing admissible

@@ -3,6 +3,7 @@ simulated clock: admission against the memory budget, rejection of jobs that
 can never fit, a failing allocation (host-side fault injection), output
 cadence, latency accounting and the FCFS baseline.  The GPU test runs a short
 served stream and checks that sampled jobs give the same fields alone."""
+import numpy as np
 import pytest
 
 from lgca_gb300 import serve as S
@@ -234,12 +235,35 @@ def test_evicted_and_resumed_jobs_are_bit_exact(gpu):
     """With least-remaining-work admission and a small site cap, residents
     are checkpointed out and resumed; every job's final fields still equal
     its lone run."""
-    jobs = S.make_jobs(200.0, 1.0, rng_seed=12, w_range=(256, 1024), h_range=(256, 512),
+    # arrivals far above capacity with room for one lattice at a time: small
+    # newcomers displace big residents while the stream arrives
+    jobs = S.make_jobs(2000.0, 0.15, rng_seed=12, w_range=(256, 1024), h_range=(256, 512),
                        steps_range=(100, 3000))
     backend = S.GpuBackend()
-    srv = S.Server(backend, budget=20e9, max_sites=3 * 1024 * 512, policy="srpt",
-                   preempt_ratio=0.5)
+    srv = S.Server(backend, budget=20e9, max_sites=1024 * 512, policy="srpt", preempt_ratio=0.5)
     rep = srv.run(jobs)
     backend.close()
     assert rep["completed"] == len(jobs) and srv.evictions > 0
     assert S.verify_sample(srv.done, n=len(srv.done))
+
+
+@pytest.mark.gpu
+def test_backend_evict_resume_round_trip(gpu):
+    """Evict mid-run (checkpoint to host, lattice freed), resume into a new
+    lattice, finish: the fields equal an uninterrupted run."""
+    job = S.Job(index=7, arrival=0.0, model=3, W=640, H=384, geometry="disc", p=0.3, steps=700,
+                seed=7)
+    backend = S.GpuBackend()
+    h = backend.create(job)
+    backend.step([h], [300])
+    blob = backend.evict(h)
+    h2 = backend.resume(job, blob)
+    backend.step([h2], [400])
+    got = backend.fields(h2)
+    backend.destroy(h2)
+    backend.close()
+    L = S.build_alone(job)
+    L.collide_and_propagate(700)
+    want = L.block_sums(16)
+    L.close()
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
