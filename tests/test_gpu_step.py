@@ -297,3 +297,21 @@ def test_steps_captured_in_a_cuda_graph(gpu, oracle, model):
         want = oracle.run(model, want, k, types=types, seed=5, t0=0, force_x=10, force_p=0.3)
     assert np.array_equal(L.download(), want)
     L.close()
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("p", [0.1, 0.5])
+def test_roofline_sweep_kernels_at_1024(gpu, oracle, model, p):
+    """Every kernel and depth of the roofline sweep (one-step; register
+    wavefront and shared-memory tiles at 2, 4 and 8 steps per pass) on the
+    sweep's 1024x1024 check lattice: periodic, Bernoulli p on every channel,
+    seed 3, 16 steps -- bit-exact with the oracle."""
+    W = H = 1024
+    st = oracle.init_bernoulli(model, W, H, None, seed=3, p_move=p, p_rest=p)
+    want = oracle.run(model, st, 16, seed=3)
+    got = run_gpu(gpu, model, st, 16, seed=3)
+    assert np.array_equal(got, want)
+    for variant in (2, 3):
+        for depth in (2, 4, 8):
+            got = run_gpu(gpu, model, st, 16, seed=3, depth=depth, variant=variant)
+            assert np.array_equal(got, want), (variant, depth)
