@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256, GMAX == GEOM_FULL ? 3 : 4)
         const int local = base + warp + 8 * i;
         if (local >= e.tasks) break;  // padding: warp-uniform
         int y, w;  // the lane's row and item (flattened same-parity mapping)
-        flat_site(local, lane, e.a.g.H, e.items, y, w);
+        flat_site(local, lane, e.a.g.H, e.items, e.a.fmagic, y, w);
 #define LGCA_BATCH_CASE(F, MODEL, GM)                                                          \
     case F * 6 + GM * 2:                                                                       \
         if (GM <= GMAX) step_word<MODEL, GM, true>(a, io, y, w, lane);                         \

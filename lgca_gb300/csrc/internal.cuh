@@ -90,6 +90,7 @@ struct StepArgs {
     int fx;             // forcing column (valid when force_thr > 0)
     int wpt;            // words per lane of the one-step kernel (1 or 2)
     int bw;             // warps per block of the one-step kernels (0: chosen per launch)
+    uint32_t fmagic;    // flat_magic of the kernel's lane items (set by the launcher)
 };
 
 // One lattice of a batch (batch.cu): its step arguments (src/dst unused),
@@ -214,15 +215,29 @@ __host__ __device__ __forceinline__ long long flat_tasks(int H, int items)
 {
     return class_tasks(H, items, 0) + class_tasks(H, items, 1);
 }
-// Row y and item of `lane` in warp task `task` (y >= H past a class's end).
-__host__ __device__ __forceinline__ void flat_site(long long task, int lane, int H, int items,
-                                                   int &y, int &item)
+// Multiplier for dividing lane numbers by `items` without a divide: with
+// m = ceil(2^32 / items), floor(l * m / 2^32) = l / items for every l with
+// l * items < 2^32 (the rounding error l * (m * items - 2^32) / 2^32 stays
+// below one step).  Lane numbers stay below rows-per-class * items + 32;
+// 0 when that bound fails or items < 2 (then a divide is used).
+__host__ __device__ __forceinline__ uint32_t flat_magic(int H, int items)
+{
+    if (items < 2) return 0u;
+    const unsigned long long lmax = (unsigned long long)((H + 1) / 2) * (unsigned)items + 32u;
+    if (lmax * (unsigned long long)items >= (1ull << 32)) return 0u;
+    return (uint32_t)(((1ull << 32) + (unsigned)items - 1) / (unsigned)items);
+}
+
+// Row y and item of `lane` in warp task `task` (y >= H past a class's end);
+// magic = flat_magic(H, items).
+__device__ __forceinline__ void flat_site(long long task, int lane, int H, int items,
+                                          uint32_t magic, int &y, int &item)
 {
     const long long even_tasks = class_tasks(H, items, 0);
     const int p = task >= even_tasks ? 1 : 0;
-    const long long l = (p ? task - even_tasks : task) * 32 + lane;
-    const long long r = l / items;
-    item = (int)(l - r * items);
+    const unsigned l = (unsigned)((p ? task - even_tasks : task) * 32 + lane);
+    const unsigned r = magic ? __umulhi(l, magic) : l / (unsigned)items;
+    item = (int)(l - r * (unsigned)items);
     y = (int)(2 * r + p);
 }
 

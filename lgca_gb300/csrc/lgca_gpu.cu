@@ -1107,6 +1107,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         const int fam = h->model == LGCA_HPP ? 0 : (h->model == LGCA_FHP_I ? 1 : 2);
         e.code = fam * 6 + e.gm * 2 + (pair ? 1 : 0);
         e.items = pair ? h->g.nw / 2 : h->g.nw;  // lane items per row
+        e.a.fmagic = flat_magic(h->g.H, e.items);
         e.buf0 = h->buf[h->cur];
         e.buf1 = h->buf[h->cur ^ 1];
         e.seed = h->seed;

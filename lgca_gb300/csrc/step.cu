@@ -20,7 +20,7 @@ __global__ void __launch_bounds__(32 * STEP_WARPS) k_step(const __grid_constant_
     const long long task = (long long)blockIdx.x * blockDim.y + threadIdx.y;
     if (task >= flat_tasks(a.g.H, a.g.nw)) return;  // whole warp
     int y, w;
-    flat_site(task, threadIdx.x, a.g.H, a.g.nw, y, w);
+    flat_site(task, threadIdx.x, a.g.H, a.g.nw, a.fmagic, y, w);
     // the chirality word does not depend on the previous step: draw it first
     uint64_t ch = 0;
     if (MODEL != M_HPP && a.chir == nullptr)
@@ -38,11 +38,13 @@ __global__ void __launch_bounds__(32 * STEP_WARPS) k_step2(const __grid_constant
     const long long task = (long long)blockIdx.x * blockDim.y + threadIdx.y;
     if (task >= flat_tasks(a.g.H, np)) return;
     int y, t;
-    flat_site(task, threadIdx.x, a.g.H, np, y, t);
+    flat_site(task, threadIdx.x, a.g.H, np, a.fmagic, y, t);
     uint64_t c0 = 0, c1 = 0;
     if (MODEL != M_HPP && a.chir == nullptr) {
-        c0 = lgca_rng_draw(a.chir_key, lgca_rng_index((uint32_t)y, (uint32_t)(2 * t)));
-        c1 = lgca_rng_draw(a.chir_key, lgca_rng_index((uint32_t)y, (uint32_t)(2 * t + 1)));
+        // draws of words 2t and 2t+1: mix(key + index * gamma), indices 1 apart
+        const uint64_t z = a.chir_key + lgca_rng_index((uint32_t)y, (uint32_t)(2 * t)) * LGCA_RNG_GAMMA;
+        c0 = lgca_mix64(z);
+        c1 = lgca_mix64(z + LGCA_RNG_GAMMA);
     }
     const StepIO io{a.src, a.dst, a.chir_key, a.force_key};
     pdl_wait();
@@ -86,8 +88,10 @@ static int pick_warps(int requested, long long chunks, long long warp_rows)
 }
 
 template <int MODEL>
-static cudaError_t launch_model2(int gm, const StepArgs &a, cudaStream_t st)
+static cudaError_t launch_model2(int gm, const StepArgs &args, cudaStream_t st)
 {
+    StepArgs a = args;
+    a.fmagic = flat_magic(a.g.H, a.g.nw / 2);
     const long long tasks = flat_tasks(a.g.H, a.g.nw / 2);
     const int bw = pick_warps(a.bw, 1, tasks);
     const long long blocks = (tasks + bw - 1) / bw;
@@ -101,9 +105,12 @@ static cudaError_t launch_model2(int gm, const StepArgs &a, cudaStream_t st)
 }
 
 template <int MODEL>
-static cudaError_t launch_model(int gm, const StepArgs &a, cudaStream_t st)
+static cudaError_t launch_model(int gm, const StepArgs &args, cudaStream_t st)
 {
-    if (a.wpt == 2 && (a.g.nw % 2) == 0 && (a.g.W % 64) == 0) return launch_model2<MODEL>(gm, a, st);
+    if (args.wpt == 2 && (args.g.nw % 2) == 0 && (args.g.W % 64) == 0)
+        return launch_model2<MODEL>(gm, args, st);
+    StepArgs a = args;
+    a.fmagic = flat_magic(a.g.H, a.g.nw);
     const long long tasks = flat_tasks(a.g.H, a.g.nw);
     const int bw = pick_warps(a.bw, 1, tasks);
     const long long blocks = (tasks + bw - 1) / bw;
