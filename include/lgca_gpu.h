@@ -265,7 +265,9 @@ int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes);
  *   lgca_batch_step_each: member i (in the order added) advances nsteps[i]
  *   steps (0 = not at all); members with fewer steps drop out of the
  *   work-list when done.  Work queued on a member's own stream before the
- *   call runs first; the member's later calls run after the batch. */
+ *   call runs first; the member's later calls run after the batch.
+ *   A lattice belongs to at most one batch; lgca_destroy removes it from
+ *   its batch first. */
 typedef struct lgca_batch *lgca_batch_handle;
 int lgca_batch_create(lgca_batch_handle *out);
 int lgca_batch_destroy(lgca_batch_handle b);

@@ -148,7 +148,10 @@ class GpuLattice:
     # lifetime
     def close(self) -> None:
         if getattr(self, "_h", None):
-            lib().lgca_destroy(self._h)
+            b = getattr(self, "_batch", None)
+            if b is not None and self in b.members:  # keep the batch's member order in step
+                b.members.remove(self)
+            lib().lgca_destroy(self._h)  # also leaves its batch on the device side
             self._h = None
 
     def __del__(self):
@@ -364,10 +367,12 @@ class GpuBatch:
     def add(self, lattice: "GpuLattice") -> None:
         self._chk(lib().lgca_batch_add(self._b, lattice.handle))
         self.members.append(lattice)
+        lattice._batch = self
 
     def remove(self, lattice: "GpuLattice") -> None:
         self._chk(lib().lgca_batch_remove(self._b, lattice.handle))
         self.members.remove(lattice)
+        lattice._batch = None
 
     def step(self, nsteps: int) -> None:
         self._chk(lib().lgca_batch_step(self._b, int(nsteps)))
@@ -389,6 +394,8 @@ class GpuBatch:
 
     def close(self) -> None:
         if getattr(self, "_b", None):
+            for m in self.members:
+                m._batch = None
             lib().lgca_batch_destroy(self._b)
             self._b = None
 

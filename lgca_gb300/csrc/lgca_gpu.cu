@@ -18,6 +18,8 @@
 
 using namespace lgca_gpu;
 
+struct lgca_batch;
+
 struct lgca_lattice {
     int model = 0, D = 0;
     PlaneGeom g{};
@@ -39,6 +41,7 @@ struct lgca_lattice {
     int *sync = nullptr;          // persistent kernel: error flag + one step flag per block
     int *sync_err_host = nullptr; // pinned copy of the error flag, checked at sync points
     size_t bytes = 0;
+    lgca_batch *batch = nullptr;  // the batch this lattice belongs to, if any
     std::string err;
 };
 
@@ -260,6 +263,7 @@ int lgca_destroy(lgca_handle h)
 {
     if (!h) return LGCA_OK;
     DeviceGuard dg(h->device);
+    if (h->batch) lgca_batch_remove(h->batch, h);  // the batch must not keep a dangling member
     // memory goes back to the pool in stream order, after the handle's queued
     // work (batch steps of a member are ordered before it); no host wait
     void *mem[] = {h->buf[0], h->buf[1], h->solid, h->slip, h->chir, h->scratch, h->sync};
@@ -979,6 +983,7 @@ int lgca_batch_destroy(lgca_batch_handle b)
     if (!b) return LGCA_OK;
     DeviceGuard dg(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
+    for (lgca_lattice *m : b->members) m->batch = nullptr;
     for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
     cudaFree(b->dE);
     cudaFree(b->dP);  // dB lives in the same allocation
@@ -999,13 +1004,14 @@ int lgca_batch_add(lgca_batch_handle b, lgca_handle h)
     if (!b) return bfail(nullptr, LGCA_ERR_INVALID, "invalid batch");
     if (!valid(h)) return bfail(b, LGCA_ERR_INVALID, "invalid lattice handle");
     if (h->device != b->device) return bfail(b, LGCA_ERR_INVALID, "lattice on another device");
-    for (lgca_lattice *m : b->members)
-        if (m == h) return bfail(b, LGCA_ERR_INVALID, "lattice already in the batch");
+    if (h->batch == b) return bfail(b, LGCA_ERR_INVALID, "lattice already in the batch");
+    if (h->batch) return bfail(b, LGCA_ERR_INVALID, "lattice already in another batch");
     DeviceGuard dg(b->device);
     cudaEvent_t e;
     BCK(b, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     b->members.push_back(h);
     b->ev.push_back(e);
+    h->batch = b;
     return LGCA_OK;
 }
 
@@ -1017,6 +1023,7 @@ int lgca_batch_remove(lgca_batch_handle b, lgca_handle h)
         if (b->members[i] == h) {
             // the member's stream already waits for the batch's queued steps
             cudaEventDestroy(b->ev[i]);
+            h->batch = nullptr;
             b->members.erase(b->members.begin() + i);
             b->ev.erase(b->ev.begin() + i);
             return LGCA_OK;

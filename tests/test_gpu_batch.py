@@ -112,3 +112,30 @@ def test_autotuner_single_lattice_choice_keeps_results(gpu, oracle):
     want = oracle.run(0, st, 40, types=types, seed=2, force_x=8, force_p=0.2)
     assert np.array_equal(L.download(), want) and L.step_count == 40
     L.close()
+
+
+def test_membership_rules(gpu):
+    """A lattice joins at most one batch; closing a member removes it from
+    its batch, whose other members keep stepping correctly."""
+    a = gpu.GpuLattice(1, 128, 8, seed=1)
+    b = gpu.GpuLattice(1, 128, 8, seed=2)
+    for L in (a, b):
+        L.init_random(0.3, 0.3)
+    want = []
+    twin = gpu.GpuLattice(1, 128, 8, seed=2)
+    twin.restore(b.checkpoint())
+    twin.collide_and_propagate(5)
+    want = twin.download()
+    twin.close()
+    with gpu.GpuBatch() as B1, gpu.GpuBatch() as B2:
+        B1.add(a)
+        B1.add(b)
+        with pytest.raises(gpu.LgcaError):
+            B2.add(a)  # already in B1
+        with pytest.raises(gpu.LgcaError):
+            B1.add(a)  # twice
+        a.close()  # leaves B1
+        assert B1.members == [b]
+        B1.step(5)
+        assert np.array_equal(b.download(), want)
+    b.close()
