@@ -1071,7 +1071,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
     }
     // lane items per row of a member: word pairs where the width allows
     auto pair_of = [](const lgca_lattice *h) {
-        return h->variant != VARIANT_PLAIN && h->wpt == 2 && (h->g.nw % 2) == 0 && (h->g.W % 64) == 0;
+        return h->variant != VARIANT_PLAIN && h->wpt == 2 && (h->g.W % 64) == 0;
     };
     // warp tasks per warp: the caller's choice, else 4 / 2 / 1 as the call's
     // work keeps at least four waves of resident warps busy (4 blocks of 8
@@ -1082,7 +1082,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         for (size_t i = 0; i < nm; ++i)
             if (nsteps[i] > 0) {
                 const lgca_lattice *h = b->members[i];
-                all += flat_tasks(h->g.H, pair_of(h) ? h->g.nw / 2 : h->g.nw);
+                all += flat_tasks(h->g.H, pair_of(h) ? (h->g.nw + 1) / 2 : h->g.nw);
             }
         const long long wave = 32LL * sm_count();
         b->call_wt = all >= 16 * wave ? 4 : (all >= 8 * wave ? 2 : 1);
@@ -1113,7 +1113,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         e.gm = geom_mode(h);
         const int fam = h->model == LGCA_HPP ? 0 : (h->model == LGCA_FHP_I ? 1 : 2);
         e.code = fam * 6 + e.gm * 2 + (pair ? 1 : 0);
-        e.items = pair ? h->g.nw / 2 : h->g.nw;  // lane items per row
+        e.items = pair ? (h->g.nw + 1) / 2 : h->g.nw;  // lane items per row (last pair may be half)
         e.a.fmagic = flat_magic(h->g.H, e.items);
         e.buf0 = h->buf[h->cur];
         e.buf1 = h->buf[h->cur ^ 1];

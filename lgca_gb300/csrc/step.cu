@@ -34,7 +34,7 @@ template <int MODEL, int GM>
 __global__ void __launch_bounds__(32 * STEP_WARPS) k_step2(const __grid_constant__ StepArgs a)
 {
     pdl_launch_dependents();
-    const int np = a.g.nw >> 1;
+    const int np = (a.g.nw + 1) >> 1;
     const long long task = (long long)blockIdx.x * blockDim.y + threadIdx.y;
     if (task >= flat_tasks(a.g.H, np)) return;
     int y, t;
@@ -91,8 +91,9 @@ template <int MODEL>
 static cudaError_t launch_model2(int gm, const StepArgs &args, cudaStream_t st)
 {
     StepArgs a = args;
-    a.fmagic = flat_magic(a.g.H, a.g.nw / 2);
-    const long long tasks = flat_tasks(a.g.H, a.g.nw / 2);
+    const int np = (a.g.nw + 1) / 2;  // word pairs per row (the last may be half)
+    a.fmagic = flat_magic(a.g.H, np);
+    const long long tasks = flat_tasks(a.g.H, np);
     const int bw = pick_warps(a.bw, 1, tasks);
     const long long blocks = (tasks + bw - 1) / bw;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
@@ -107,7 +108,7 @@ static cudaError_t launch_model2(int gm, const StepArgs &args, cudaStream_t st)
 template <int MODEL>
 static cudaError_t launch_model(int gm, const StepArgs &args, cudaStream_t st)
 {
-    if (args.wpt == 2 && (args.g.nw % 2) == 0 && (args.g.W % 64) == 0)
+    if (args.wpt == 2 && (args.g.W % 64) == 0)
         return launch_model2<MODEL>(gm, args, st);
     StepArgs a = args;
     a.fmagic = flat_magic(a.g.H, a.g.nw);
@@ -151,7 +152,7 @@ __global__ void k_band(const __grid_constant__ StepArgs a, uint64_t *buf0, uint6
     const int nb = gridDim.x, b = blockIdx.x;
     const int bl = (b + nb - 1) % nb, br = (b + 1) % nb;
     const int y0 = (int)((long long)a.g.H * b / nb), y1 = (int)((long long)a.g.H * (b + 1) / nb);
-    const int per_row = WPT == 2 ? (a.g.nw / 2 + 31) / 32 : (a.g.nw + 31) / 32;
+    const int per_row = WPT == 2 ? ((a.g.nw + 1) / 2 + 31) / 32 : (a.g.nw + 31) / 32;
     const int tasks = (y1 - y0) * per_row;
     const int lane = threadIdx.x, warp = threadIdx.y, nwarps = blockDim.y;
     const bool leader = lane == 0 && warp == 0;
@@ -224,7 +225,7 @@ template <int MODEL, int GM>
 static cudaError_t band_wpt(const StepArgs &a, uint64_t *b0, uint64_t *b1, uint64_t seed,
                             uint64_t t0, int n, int *flags, int *err, int maxb, cudaStream_t st)
 {
-    if (a.wpt == 2 && (a.g.nw % 2) == 0 && (a.g.W % 64) == 0)
+    if (a.wpt == 2 && (a.g.W % 64) == 0)
         return band_launch<MODEL, GM, 2>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
     return band_launch<MODEL, GM, 1>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
 }

@@ -223,9 +223,12 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
 }
 
 // Two words per lane (lattices with an even number of words per row, i.e.
-// W a multiple of 128): 16-byte loads and stores, one shuffle per shifted
+// W a multiple of 64): 16-byte loads and stores, one shuffle per shifted
 // plane for 128 sites, and half as many warps, so that an L2-resident lattice
-// fits in one wave of resident warps.  Same arithmetic as step_word.
+// fits in one wave of resident warps.  Same arithmetic as step_word.  With an
+// odd number of words per row the last pair holds the last word and the
+// row's padding word (the pitch is even): that word's east neighbour is the
+// seam word, and the padding word is written back as zero.
 template <int MODEL, int GM, bool CG = false, bool PRE = false>
 __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, const int y,
                                           const int t, const int lane, const int width = 32,
@@ -233,8 +236,9 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
 {
     constexpr int D = ModelTraits<MODEL>::D;
     const PlaneGeom &g = a.g;
-    const int np = g.nw >> 1;
+    const int np = (g.nw + 1) >> 1;
     const bool active = t < np && y < g.H;
+    const bool half = (g.nw & 1) && t == np - 1;  // the pair's second word is padding
     const int seg = lane & (width - 1);  // lane within its row segment
     const int ym = (y == 0) ? g.H - 1 : y - 1;
     const int yp = (y == g.H - 1) ? 0 : y + 1;
@@ -320,7 +324,7 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
             if (d == WEST && row == row0 && forcing && ex == a.fx)
                 in &= ~force_flip_at<MODEL, GM, CG>(a, io, y);
         }
-        return k ? ((v1 >> 1) | (in << 63)) : ((v0 >> 1) | (v1 << 63));
+        return k ? ((v1 >> 1) | (in << 63)) : ((v0 >> 1) | ((half ? in : v1) << 63));
     };
     // pulled values of word k of the pair
     uint64_t q[2][7];
@@ -384,7 +388,8 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
     uint64_t *__restrict__ dp = io.dst + row0 + w0;
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        *reinterpret_cast<ulonglong2 *>(dp + d * ps) = make_ulonglong2(out[0][d], out[1][d]);
+        *reinterpret_cast<ulonglong2 *>(dp + d * ps) =
+            make_ulonglong2(out[0][d], half ? 0ull : out[1][d]);
 }
 
 }  // namespace lgca_gpu

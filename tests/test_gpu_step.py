@@ -233,10 +233,12 @@ def test_temporal_blocking_karman_config(gpu, depth, variant):
 @pytest.mark.parametrize("model", MODELS)
 @pytest.mark.parametrize("geom", sorted(GEOMS))
 def test_one_step_kernels_one_and_two_words_per_lane(gpu, oracle, model, geom):
-    """Widths that are multiples of 128 run the two-words-per-lane kernel;
-    forcing columns sit on pair, word and chunk edges."""
+    """Widths that are multiples of 64 run the two-words-per-lane kernel,
+    including odd word counts (the last pair holds one word and the row's
+    padding); forcing columns sit on pair, word and chunk edges."""
     rng = np.random.default_rng(3 * model + len(geom))
-    for W, H in [(128, 6), (256, 10), (384, 8), (1152, 12), (4096, 4)]:
+    for W, H in [(64, 6), (128, 6), (192, 8), (256, 10), (320, 6), (384, 8), (1088, 10),
+                 (1152, 12), (2112, 4), (4096, 4)]:
         types = GEOMS[geom](W, H)
         seed = int(rng.integers(1 << 40))
         st = oracle.init_bernoulli(model, W, H, types, seed=seed, p_move=0.35, p_rest=0.3)
