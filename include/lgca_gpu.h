@@ -278,12 +278,12 @@ int lgca_batch_step(lgca_batch_handle b, int nsteps);
 int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps);
 int lgca_batch_set_graph_steps(lgca_batch_handle b, int steps_per_graph); /* 0: no graphs */
 /* Warp tasks (32 lane items of one member) each warp of the batched kernel
- * takes per step: 1, 2, 4 or 8, or 0 (default) to choose per call: 4 when
- * the call's work fills at least four waves of resident warps at 4 tasks per
- * warp, else 2 or 1.  More tasks per warp pay the member lookup less often
- * (4 ran 10 % faster than 1 on 512 lattices of 1 G sites); fewer give more
- * parallelism to small calls.  A tuning knob: results do not depend on it.
- * (No reference counterpart.) */
+ * takes per step: 1, 2, 4 or 8, or 0 (default) to choose per call: 2 when
+ * the call's work fills at least four waves of resident warps at 2 tasks per
+ * warp, 4 for calls 16 times larger, else 1.  More tasks per warp pay the
+ * member lookup less often (2 ran 18 % faster than 1 on 512 lattices of
+ * 1 G sites); fewer give more parallelism to small calls.  A tuning knob:
+ * results do not depend on it.  (No reference counterpart.) */
 int lgca_batch_set_warp_tasks(lgca_batch_handle b, int n);
 int lgca_batch_sync(lgca_batch_handle b);
 const char *lgca_batch_last_error(lgca_batch_handle b);

@@ -47,11 +47,14 @@ __global__ void __launch_bounds__(256, GMAX == GEOM_FULL ? 3 : 4)
         int y, w;  // the lane's row and item (flattened same-parity mapping)
         flat_site(local, lane, e.a.g.H, e.items, e.a.fmagic, y, w);
 #define LGCA_BATCH_CASE(F, MODEL, GM)                                                          \
-    case F * 6 + GM * 2:                                                                       \
+    case F * 9 + GM * 3:                                                                       \
         if (GM <= GMAX) step_word<MODEL, GM, true>(a, io, y, w, lane);                         \
         break;                                                                                 \
-    case F * 6 + GM * 2 + 1:                                                                   \
-        if (GM <= GMAX) step_pair<MODEL, GM, true>(a, io, y, w, lane);                         \
+    case F * 9 + GM * 3 + 1:                                                                   \
+        if (GM <= GMAX) step_pair<MODEL, GM, true, false, false>(a, io, y, w, lane);           \
+        break;                                                                                 \
+    case F * 9 + GM * 3 + 2:                                                                   \
+        if (GM <= GMAX) step_pair<MODEL, GM, true, false, true>(a, io, y, w, lane);            \
         break;
 #define LGCA_BATCH_CASES(F, MODEL)                                                             \
     LGCA_BATCH_CASE(F, MODEL, GEOM_NONE)                                                       \

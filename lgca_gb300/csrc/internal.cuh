@@ -107,7 +107,7 @@ struct BatchEntry {
     int task0;    // first warp task (a multiple of the block's tasks) and real tasks
     int tasks;
     int gm, wpt;  // geometry mode, words per lane
-    int code;     // model family * 6 + geometry mode * 2 + (wpt == 2)
+    int code;     // model family * 9 + geometry mode * 3 + path (0 word, 1 pair, 2 pair, odd words)
 };
 // total_tasks: warp tasks of the active members (each member's tasks padded
 // to whole blocks of 8 * warp_tasks); block_lat[b] = member of block b;

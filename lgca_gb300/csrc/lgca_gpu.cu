@@ -1073,9 +1073,10 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
     auto pair_of = [](const lgca_lattice *h) {
         return h->variant != VARIANT_PLAIN && h->wpt == 2 && (h->g.W % 64) == 0;
     };
-    // warp tasks per warp: the caller's choice, else 4 / 2 / 1 as the call's
-    // work keeps at least four waves of resident warps busy (4 blocks of 8
-    // warps per SM); small calls keep one task per warp for parallelism
+    // warp tasks per warp: the caller's choice, else 2 once the call's work
+    // fills at least four waves of resident warps at 2 tasks per warp (4
+    // blocks of 8 warps per SM), 4 for calls 16 times larger; small calls keep
+    // one task per warp for parallelism
     b->call_wt = b->warp_tasks;
     if (b->call_wt == 0) {
         long long all = 0;
@@ -1085,7 +1086,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
                 all += flat_tasks(h->g.H, pair_of(h) ? (h->g.nw + 1) / 2 : h->g.nw);
             }
         const long long wave = 32LL * sm_count();
-        b->call_wt = all >= 16 * wave ? 4 : (all >= 8 * wave ? 2 : 1);
+        b->call_wt = all >= 128 * wave ? 4 : (all >= 8 * wave ? 2 : 1);
     }
     // one work-list, lattices sorted by steps (descending)
     std::vector<int> order(nm);
@@ -1112,7 +1113,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         e.wpt = e.a.wpt;
         e.gm = geom_mode(h);
         const int fam = h->model == LGCA_HPP ? 0 : (h->model == LGCA_FHP_I ? 1 : 2);
-        e.code = fam * 6 + e.gm * 2 + (pair ? 1 : 0);
+        e.code = fam * 9 + e.gm * 3 + (pair ? ((h->g.nw & 1) ? 2 : 1) : 0);
         e.items = pair ? (h->g.nw + 1) / 2 : h->g.nw;  // lane items per row (last pair may be half)
         e.a.fmagic = flat_magic(h->g.H, e.items);
         e.buf0 = h->buf[h->cur];

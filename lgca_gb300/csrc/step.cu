@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(32 * STEP_WARPS) k_step(const __grid_constant_
     step_word<MODEL, GM, true, true>(a, io, y, w, threadIdx.x, 32, ch);
 }
 
-template <int MODEL, int GM>
+template <int MODEL, int GM, bool ODD>
 __global__ void __launch_bounds__(32 * STEP_WARPS) k_step2(const __grid_constant__ StepArgs a)
 {
     pdl_launch_dependents();
@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(32 * STEP_WARPS) k_step2(const __grid_constant
     }
     const StepIO io{a.src, a.dst, a.chir_key, a.force_key};
     pdl_wait();
-    step_pair<MODEL, GM, true, true>(a, io, y, t, threadIdx.x, 32, c0, c1);
+    step_pair<MODEL, GM, true, true, ODD>(a, io, y, t, threadIdx.x, 32, c0, c1);
 }
 
 int sm_count()
@@ -98,10 +98,17 @@ static cudaError_t launch_model2(int gm, const StepArgs &args, cudaStream_t st)
     const long long blocks = (tasks + bw - 1) / bw;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     const dim3 grid((unsigned)blocks), block(32, bw);
+    if (a.g.nw & 1) {
+        switch (gm) {
+        case GEOM_NONE: return launch_pdl(k_step2<MODEL, GEOM_NONE, true>, grid, block, 0, st, a);
+        case GEOM_NOSLIP: return launch_pdl(k_step2<MODEL, GEOM_NOSLIP, true>, grid, block, 0, st, a);
+        default: return launch_pdl(k_step2<MODEL, GEOM_FULL, true>, grid, block, 0, st, a);
+        }
+    }
     switch (gm) {
-    case GEOM_NONE: return launch_pdl(k_step2<MODEL, GEOM_NONE>, grid, block, 0, st, a);
-    case GEOM_NOSLIP: return launch_pdl(k_step2<MODEL, GEOM_NOSLIP>, grid, block, 0, st, a);
-    default: return launch_pdl(k_step2<MODEL, GEOM_FULL>, grid, block, 0, st, a);
+    case GEOM_NONE: return launch_pdl(k_step2<MODEL, GEOM_NONE, false>, grid, block, 0, st, a);
+    case GEOM_NOSLIP: return launch_pdl(k_step2<MODEL, GEOM_NOSLIP, false>, grid, block, 0, st, a);
+    default: return launch_pdl(k_step2<MODEL, GEOM_FULL, false>, grid, block, 0, st, a);
     }
 }
 
@@ -225,7 +232,7 @@ template <int MODEL, int GM>
 static cudaError_t band_wpt(const StepArgs &a, uint64_t *b0, uint64_t *b1, uint64_t seed,
                             uint64_t t0, int n, int *flags, int *err, int maxb, cudaStream_t st)
 {
-    if (a.wpt == 2 && (a.g.W % 64) == 0)
+    if (a.wpt == 2 && (a.g.nw % 2) == 0 && (a.g.W % 64) == 0)  // band form: whole pairs
         return band_launch<MODEL, GM, 2>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
     return band_launch<MODEL, GM, 1>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
 }

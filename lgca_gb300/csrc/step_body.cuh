@@ -226,10 +226,10 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
 // W a multiple of 64): 16-byte loads and stores, one shuffle per shifted
 // plane for 128 sites, and half as many warps, so that an L2-resident lattice
 // fits in one wave of resident warps.  Same arithmetic as step_word.  With an
-// odd number of words per row the last pair holds the last word and the
+// odd number of words per row (ODD) the last pair holds the last word and the
 // row's padding word (the pitch is even): that word's east neighbour is the
 // seam word, and the padding word is written back as zero.
-template <int MODEL, int GM, bool CG = false, bool PRE = false>
+template <int MODEL, int GM, bool CG = false, bool PRE = false, bool ODD = false>
 __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, const int y,
                                           const int t, const int lane, const int width = 32,
                                           const uint64_t pre0 = 0, const uint64_t pre1 = 0)
@@ -238,7 +238,7 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
     const PlaneGeom &g = a.g;
     const int np = (g.nw + 1) >> 1;
     const bool active = t < np && y < g.H;
-    const bool half = (g.nw & 1) && t == np - 1;  // the pair's second word is padding
+    const bool half = ODD && t == np - 1;  // (ODD: odd words per row) the second word is padding
     const int seg = lane & (width - 1);  // lane within its row segment
     const int ym = (y == 0) ? g.H - 1 : y - 1;
     const int yp = (y == g.H - 1) ? 0 : y + 1;
