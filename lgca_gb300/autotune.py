@@ -87,10 +87,13 @@ class Autotuner:
         return variant, depth, bw
 
     # ------------------------------------------------------------ batch members
-    def tune_batch_members(self, lattices, steps: int = 8, sample: int = 6) -> dict[str, int]:
+    def tune_batch_members(self, lattices, steps: int = 24, sample: int = 6,
+                           margin: float = 0.05) -> dict[str, int]:
         """Choose words per lane per (model family, size class) by timing a
         batch of up to `sample` twins of the class's members with each
-        candidate; apply the choice (as the members' kernel variant)."""
+        candidate; two words per lane stay unless one word is faster by more
+        than `margin` (the timings of small samples are noisy); apply the
+        choice (as the members' kernel variant)."""
         groups: dict[str, list] = {}
         for L in lattices:
             groups.setdefault(f"{family(L.model)}:{size_class(L.dim_x, L.dim_y)}", []).append(L)
@@ -101,7 +104,7 @@ class Autotuner:
                     T = gpu.GpuLattice(L.model, L.dim_x, L.dim_y)
                     T.restore(L.checkpoint())
                     twins.append(T)
-                best, best_t = 2, float("inf")
+                times = {}
                 for wpt, variant in WPT_CANDIDATES.items():
                     with gpu.GpuBatch() as B:
                         for T in twins:
@@ -112,12 +115,10 @@ class Autotuner:
                         t0 = time.perf_counter()
                         B.step(steps)
                         B.sync()
-                        t = time.perf_counter() - t0
-                    if t < best_t:
-                        best, best_t = wpt, t
+                        times[wpt] = time.perf_counter() - t0
                 for T in twins:
                     T.close()
-                self.batch[key] = best
+                self.batch[key] = 1 if times[1] < (1.0 - margin) * times[2] else 2
             for L in members:
                 L.set_kernel_variant(WPT_CANDIDATES[self.batch[key]])
         return dict(self.batch)
