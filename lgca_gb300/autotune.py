@@ -87,45 +87,54 @@ class Autotuner:
         return variant, depth, bw
 
     # ------------------------------------------------------------ batch members
-    def tune_batch_members(self, lattices, steps: int = 32, sample: int = 6,
-                           margin: float = 0.05, repeats: int = 3,
-                           min_sites: int = 1 << 22) -> dict[str, int]:
-        """Choose words per lane per (model family, size class) by timing a
-        batch of up to `sample` twins of the class's members with each
-        candidate (interleaved, best of `repeats`); two words per lane stay
-        unless one word is faster by more than `margin`, and classes whose
-        sample holds fewer than `min_sites` sites keep two words untimed
-        (their timings are launch noise); apply the choice (as the members'
-        kernel variant)."""
+    def tune_batch_members(self, lattices, steps: int = 24, sample: int = 6,
+                           margin: float = 0.03, repeats: int = 2) -> dict[str, int]:
+        """Choose words per lane per (model family, size class) where it
+        matters: inside a batch that holds twins of up to `sample` members of
+        every class (so the device is as loaded as in the real batch), each
+        untuned class is timed with each candidate while the others keep two
+        words per lane (best of `repeats`); two words stay unless one word
+        makes the whole batch faster by more than `margin`.  Apply the choice
+        (as the members' kernel variant)."""
         groups: dict[str, list] = {}
         for L in lattices:
             groups.setdefault(f"{family(L.model)}:{size_class(L.dim_x, L.dim_y)}", []).append(L)
-        for key, members in groups.items():
-            if key not in self.batch:
-                if sum(L.dim_x * L.dim_y for L in members[:sample]) < min_sites:
-                    self.batch[key] = 2
-                else:
-                    twins = []
-                    for L in members[:sample]:
-                        T = gpu.GpuLattice(L.model, L.dim_x, L.dim_y)
-                        T.restore(L.checkpoint())
-                        twins.append(T)
-                    times = {wpt: float("inf") for wpt in WPT_CANDIDATES}
-                    for _ in range(repeats):
-                        for wpt, variant in WPT_CANDIDATES.items():
-                            with gpu.GpuBatch() as B:
-                                for T in twins:
-                                    T.set_kernel_variant(variant)
-                                    B.add(T)
-                                B.step(2)
-                                B.sync()
-                                t0 = time.perf_counter()
-                                B.step(steps)
-                                B.sync()
-                                times[wpt] = min(times[wpt], time.perf_counter() - t0)
-                    for T in twins:
-                        T.close()
+        todo = [key for key in groups if key not in self.batch]
+        if todo:
+            twins: dict[str, list] = {}
+            for key, members in groups.items():
+                twins[key] = []
+                for L in members[:sample]:
+                    T = gpu.GpuLattice(L.model, L.dim_x, L.dim_y)
+                    T.restore(L.checkpoint())
+                    T.set_kernel_variant(WPT_CANDIDATES[2])
+                    twins[key].append(T)
+            with gpu.GpuBatch() as B:
+                for ts in twins.values():
+                    for T in ts:
+                        B.add(T)
+
+                def timed() -> float:
+                    B.step(2)
+                    B.sync()
+                    t0 = time.perf_counter()
+                    B.step(steps)
+                    B.sync()
+                    return time.perf_counter() - t0
+
+                for key in todo:
+                    times = {}
+                    for wpt, variant in WPT_CANDIDATES.items():
+                        for T in twins[key]:
+                            T.set_kernel_variant(variant)
+                        times[wpt] = min(timed() for _ in range(repeats))
+                    for T in twins[key]:
+                        T.set_kernel_variant(WPT_CANDIDATES[2])
                     self.batch[key] = 1 if times[1] < (1.0 - margin) * times[2] else 2
+            for ts in twins.values():
+                for T in ts:
+                    T.close()
+        for key, members in groups.items():
             for L in members:
                 L.set_kernel_variant(WPT_CANDIDATES[self.batch[key]])
         return dict(self.batch)
