@@ -41,12 +41,11 @@ template <> struct ModelTraits<M_FHP_II> { static constexpr int D = 7; };
 template <> struct ModelTraits<M_FHP_III> { static constexpr int D = 7; };
 
 // HPP: a head-on pair swaps to the perpendicular pair when the other pair is
-// empty.  The chirality is not used.
+// empty.  The chirality is not used.  The state is exactly {0, 2} or exactly
+// {1, 3} when n0 != n1, n0 == n2 and n1 == n3.
 LGCA_HDI void collide_hpp(uint64_t n[4])
 {
-    const uint64_t h02 = n[0] & n[2] & ~(n[1] | n[3]);
-    const uint64_t h13 = n[1] & n[3] & ~(n[0] | n[2]);
-    const uint64_t ch = h02 | h13;
+    const uint64_t ch = (n[0] ^ n[1]) & ~(n[0] ^ n[2]) & ~(n[1] ^ n[3]);
     n[0] ^= ch; n[1] ^= ch; n[2] ^= ch; n[3] ^= ch;
 }
 
@@ -59,12 +58,16 @@ LGCA_HDI void collide_hpp(uint64_t n[4])
 // matches.  The same boolean function, regrouped for few operations, indexing
 // the moving channels n0..n5 around the hexagon (the reference's a..f are
 // n1..n5, n0):
-//   * count the occupied moving channels once with a bit-sliced adder
-//     (c0 + 2 c1 + 4 c2) and form "exactly 1 / 2 / 3 moving" masks;
+//   * count the occupied moving channels of each half-hexagon with a full
+//     adder (s = parity, k = carry: the half's count is s + 2k) and form
+//     "exactly 1 / 2 / 3 moving" masks straight from the two halves:
+//       1: s1 != s2 and no carry;  3: s1 != s2 and exactly one carry;
+//       2: s1 == s2 == 1 and no carry, or s1 == s2 == 0 and exactly one carry;
 //   * head-on pair k = {n_k, n_k+3}: P_k = n_k & n_k+3 & is2; the pair turns by
 //     -60 deg (p = 1) or +60 deg (p = 0), so channel pair k flips when P_k or
 //     (p ? P_k+1 : P_k-1) holds (the reference's db1|(p&db2)|(~p&db3));
-//   * three-body: T = is3 & (n0&n2&n4 | n1&n3&n5) flips all six;
+//   * three-body: with exactly three moving, (n0 n2 n4) or (n1 n3 n5) is full
+//     exactly when n0 == n2 == n4; then T flips all six;
 //   * rest rules (FHP-II): a rest particle plus a single moving particle at x
 //     (R1 = r & is1) and two moving particles at x-1, x+1 without rest
 //     (R2 = ~r & is2) both have their "centre" at x:
@@ -76,23 +79,22 @@ LGCA_HDI void collide_fhp(uint64_t n[7], uint64_t p)
 {
     const uint64_t n0 = n[0], n1 = n[1], n2 = n[2], n3 = n[3], n4 = n[4], n5 = n[5];
 
-    // moving-particle count: two full adders and a 2-bit combine
+    // half-hexagon counts: s + 2k for (n0, n1, n2) and (n3, n4, n5)
     const uint64_t s1 = n0 ^ n1 ^ n2, k1 = (n0 & n1) | (n2 & (n0 ^ n1));
     const uint64_t s2 = n3 ^ n4 ^ n5, k2 = (n3 & n4) | (n5 & (n3 ^ n4));
-    const uint64_t c0 = s1 ^ s2, t = s1 & s2;
-    const uint64_t c1 = k1 ^ k2 ^ t, c2 = (k1 & k2) | (t & (k1 ^ k2));
-    const uint64_t is2 = ~c0 & c1 & ~c2;
-    const uint64_t is3 = c0 & c1 & ~c2;
+    const uint64_t sx = s1 ^ s2;
+    const uint64_t is3 = sx & (k1 ^ k2);
+    const uint64_t is2 = ~sx & ((s1 & ~(k1 | k2)) | (~s1 & (k1 ^ k2)));
 
     const uint64_t P0 = n0 & n3 & is2, P1 = n1 & n4 & is2, P2 = n2 & n5 & is2;
-    const uint64_t T = is3 & ((n0 & n2 & n4) | (n1 & n3 & n5));
+    const uint64_t T = is3 & ~((n0 ^ n2) | (n2 ^ n4));
     const uint64_t X0 = T | P0 | ((p & P1) | (~p & P2));
     const uint64_t X1 = T | P1 | ((p & P2) | (~p & P0));
     const uint64_t X2 = T | P2 | ((p & P0) | (~p & P1));
 
     if (REST) {
         const uint64_t r = n[6];
-        const uint64_t is1 = c0 & ~c1 & ~c2;
+        const uint64_t is1 = sx & ~(k1 | k2);
         const uint64_t R1 = r & is1, R2 = ~r & is2;
         const uint64_t K0 = (R1 & n0) | (R2 & n5 & n1);
         const uint64_t K1 = (R1 & n1) | (R2 & n0 & n2);
