@@ -7,8 +7,6 @@
 
 namespace lgca_gpu {
 
-// Grid: x = 32-item chunk of a row, y = group of blockDim.y warps; one warp
-// per (row, chunk), rows of <= 16 items sharing a warp.
 static constexpr int STEP_WARPS = 8;  // largest block: 8 warps
 
 // Grid: 1-D, blockDim.y warps per block; warp task = blockIdx.x * blockDim.y

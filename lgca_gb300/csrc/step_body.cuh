@@ -21,9 +21,12 @@
 // missing bit taken from the neighbouring word (a warp shuffle, or a load at
 // a warp edge / the periodic x seam).
 //
-// Mapping: one warp per (row, chunk of 32 words), one word (64 sites) per
-// lane.  Each lane loads D words and stores D words; the only other traffic
-// is one word per shifted plane at the two warp edges.
+// Mapping (set by the caller): each lane holds one word (step_word) or two
+// words (step_pair) of one row; consecutive lanes hold consecutive words of
+// a row, and a lane whose neighbour lane holds another row (or no row) loads
+// the neighbour word instead of shuffling.  Each lane loads D words (or
+// pairs) and stores as many; the only other traffic is one word per shifted
+// plane at row and warp edges.
 #pragma once
 #include "internal.cuh"
 #include "../../include/lgca/rng.h"
