@@ -282,6 +282,40 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
         slip[1] = v.y;
     }
 
+    // Edge words, loaded with the state so that their latency overlaps it:
+    // a lane whose left (right) neighbour lane holds another row, or none,
+    // takes the word west (east) of its pair from memory for every plane that
+    // shifts that way.  Which planes shift which way depends on the model
+    // and the row parity (warp-uniform):
+    //   FHP, even row: west 0 (row y), 1 (y-1), 5 (y+1); east 3 (row y)
+    //   FHP, odd row:  west 0 (row y); east 3 (row y), 2 (y-1), 4 (y+1)
+    //   HPP:           west 0 (row y); east 2 (row y)
+    const bool need_w = active && (seg == 0 || t == 0);
+    const bool need_e = active && (seg == width - 1 || t == np - 1);
+    const int widx = (t == 0) ? g.nw - 1 : w0 - 1;
+    const int eidx = (t == np - 1) ? 0 : w0 + 2;
+    auto ldw = [&](int d, unsigned row) -> uint64_t { return ld_state<CG>(s + (d * ps + row + widx)); };
+    auto lde = [&](int d, unsigned row) -> uint64_t { return ld_state<CG>(s + (d * ps + row + eidx)); };
+    uint64_t eg[4] = {0, 0, 0, 0};  // in the order the pulls below use them
+    if (MODEL == M_HPP) {
+        if (need_w) eg[0] = ldw(0, row0);
+        if (need_e) eg[1] = lde(2, row0);
+    } else if (even) {
+        if (need_w) {
+            eg[0] = ldw(0, row0);
+            eg[1] = ldw(1, rowm);
+            eg[2] = ldw(5, rowp);
+        }
+        if (need_e) eg[3] = lde(3, row0);
+    } else {
+        if (need_w) eg[0] = ldw(0, row0);
+        if (need_e) {
+            eg[1] = lde(3, row0);
+            eg[2] = lde(2, rowm);
+            eg[3] = lde(4, rowp);
+        }
+    }
+
     constexpr int WEST = (MODEL == M_HPP) ? 2 : 3;
     const bool forcing = a.force_thr != 0;
     const int fw = a.fx >> 6;
@@ -300,57 +334,54 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
         n[1][WEST] &= ~f1;
     }
 
-    const bool need_w = active && (seg == 0 || t == 0);
-    const bool need_e = active && (seg == width - 1 || t == np - 1);
-    const int widx = (t == 0) ? g.nw - 1 : w0 - 1;
-    const int eidx = (t == np - 1) ? 0 : w0 + 2;
     const int wx = (t == 0) ? g.W - 1 : 64 * w0 - 1;
     const int ex = (t == np - 1) ? 0 : 64 * w0 + 128;
 
-    // x-1 pull of the pair (v0, v1)
-    auto shl = [&](uint64_t v0, uint64_t v1, int d, unsigned row, int k) -> uint64_t {
+    // x-1 pull of the pair (v0, v1); `edge` is the word west of it, read by
+    // lanes with need_w (and forced there when it holds the forcing column)
+    auto shl = [&](uint64_t v0, uint64_t v1, uint64_t edge, bool fcol, int k) -> uint64_t {
         const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v1 >> 32), 1, width);
         uint64_t in = hi >> 31;
         if (need_w) {
-            in = ld_state<CG>(s + (d * ps + row + widx)) >> 63;
-            if (d == 0 && row == row0 && forcing && wx == a.fx)
-                in |= force_flip_at<MODEL, GM, CG>(a, io, y);
+            in = edge >> 63;
+            if (fcol && forcing && wx == a.fx) in |= force_flip_at<MODEL, GM, CG>(a, io, y);
         }
         return k ? ((v1 << 1) | (v0 >> 63)) : ((v0 << 1) | in);
     };
-    // x+1 pull of the pair
-    auto shr = [&](uint64_t v0, uint64_t v1, int d, unsigned row, int k) -> uint64_t {
+    // x+1 pull of the pair; `edge` is the word east of it
+    auto shr = [&](uint64_t v0, uint64_t v1, uint64_t edge, bool fcol, int k) -> uint64_t {
         const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v0, 1, width);
         uint64_t in = lo & 1u;
         if (need_e) {
-            in = ld_state<CG>(s + (d * ps + row + eidx)) & 1ull;
-            if (d == WEST && row == row0 && forcing && ex == a.fx)
-                in &= ~force_flip_at<MODEL, GM, CG>(a, io, y);
+            in = edge & 1ull;
+            if (fcol && forcing && ex == a.fx) in &= ~force_flip_at<MODEL, GM, CG>(a, io, y);
         }
         return k ? ((v1 >> 1) | (in << 63)) : ((v0 >> 1) | ((half ? in : v1) << 63));
     };
     // pulled values of word k of the pair
     uint64_t q[2][7];
     if (MODEL == M_HPP) {
-        const uint64_t a0 = shl(n[0][0], n[1][0], 0, row0, 0), a1 = shl(n[0][0], n[1][0], 0, row0, 1);
-        const uint64_t b0 = shr(n[0][2], n[1][2], 2, row0, 0), b1 = shr(n[0][2], n[1][2], 2, row0, 1);
+        const uint64_t a0 = shl(n[0][0], n[1][0], eg[0], true, 0), a1 = shl(n[0][0], n[1][0], eg[0], true, 1);
+        const uint64_t b0 = shr(n[0][2], n[1][2], eg[1], true, 0), b1 = shr(n[0][2], n[1][2], eg[1], true, 1);
         q[0][0] = a0; q[1][0] = a1; q[0][2] = b0; q[1][2] = b1;
         q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][3] = n[0][3]; q[1][3] = n[1][3];
-    } else {
-        const uint64_t a0 = shl(n[0][0], n[1][0], 0, row0, 0), a1 = shl(n[0][0], n[1][0], 0, row0, 1);
-        const uint64_t b0 = shr(n[0][3], n[1][3], 3, row0, 0), b1 = shr(n[0][3], n[1][3], 3, row0, 1);
+    } else if (even) {  // warp-uniform (row mapping contract)
+        const uint64_t a0 = shl(n[0][0], n[1][0], eg[0], true, 0), a1 = shl(n[0][0], n[1][0], eg[0], true, 1);
+        const uint64_t c0 = shl(n[0][1], n[1][1], eg[1], false, 0), c1 = shl(n[0][1], n[1][1], eg[1], false, 1);
+        const uint64_t e0 = shl(n[0][5], n[1][5], eg[2], false, 0), e1 = shl(n[0][5], n[1][5], eg[2], false, 1);
+        const uint64_t b0 = shr(n[0][3], n[1][3], eg[3], true, 0), b1 = shr(n[0][3], n[1][3], eg[3], true, 1);
         q[0][0] = a0; q[1][0] = a1; q[0][3] = b0; q[1][3] = b1;
-        if (even) {  // warp-uniform (row mapping contract)
-            const uint64_t c0 = shl(n[0][1], n[1][1], 1, rowm, 0), c1 = shl(n[0][1], n[1][1], 1, rowm, 1);
-            const uint64_t e0 = shl(n[0][5], n[1][5], 5, rowp, 0), e1 = shl(n[0][5], n[1][5], 5, rowp, 1);
-            q[0][1] = c0; q[1][1] = c1; q[0][5] = e0; q[1][5] = e1;
-            q[0][2] = n[0][2]; q[1][2] = n[1][2]; q[0][4] = n[0][4]; q[1][4] = n[1][4];
-        } else {
-            const uint64_t c0 = shr(n[0][2], n[1][2], 2, rowm, 0), c1 = shr(n[0][2], n[1][2], 2, rowm, 1);
-            const uint64_t e0 = shr(n[0][4], n[1][4], 4, rowp, 0), e1 = shr(n[0][4], n[1][4], 4, rowp, 1);
-            q[0][2] = c0; q[1][2] = c1; q[0][4] = e0; q[1][4] = e1;
-            q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][5] = n[0][5]; q[1][5] = n[1][5];
-        }
+        q[0][1] = c0; q[1][1] = c1; q[0][5] = e0; q[1][5] = e1;
+        q[0][2] = n[0][2]; q[1][2] = n[1][2]; q[0][4] = n[0][4]; q[1][4] = n[1][4];
+        if (D == 7) { q[0][6] = n[0][6]; q[1][6] = n[1][6]; }
+    } else {
+        const uint64_t a0 = shl(n[0][0], n[1][0], eg[0], true, 0), a1 = shl(n[0][0], n[1][0], eg[0], true, 1);
+        const uint64_t b0 = shr(n[0][3], n[1][3], eg[1], true, 0), b1 = shr(n[0][3], n[1][3], eg[1], true, 1);
+        const uint64_t c0 = shr(n[0][2], n[1][2], eg[2], false, 0), c1 = shr(n[0][2], n[1][2], eg[2], false, 1);
+        const uint64_t e0 = shr(n[0][4], n[1][4], eg[3], false, 0), e1 = shr(n[0][4], n[1][4], eg[3], false, 1);
+        q[0][0] = a0; q[1][0] = a1; q[0][3] = b0; q[1][3] = b1;
+        q[0][2] = c0; q[1][2] = c1; q[0][4] = e0; q[1][4] = e1;
+        q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][5] = n[0][5]; q[1][5] = n[1][5];
         if (D == 7) { q[0][6] = n[0][6]; q[1][6] = n[1][6]; }
     }
     if (!active) return;
