@@ -126,7 +126,8 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
         n[WEST] &= ~(fl << fb);
     }
 
-    // neighbour words at the warp edges and the periodic x seam
+    // neighbour words at row and warp edges and the periodic x seam, one per
+    // shifted plane (see step_pair for the planes per model and parity)
     const bool need_w = active && (seg == 0 || w == 0);
     const bool need_e = active && (seg == width - 1 || w == g.nw - 1);
     const int widx = (w == 0) ? g.nw - 1 : w - 1;
@@ -135,50 +136,70 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
     const int epos = (w == g.nw - 1) ? g.L : 63;
     const int wx = (w == 0) ? g.W - 1 : 64 * w - 1;  // site of the fetched west bit
     const int ex = (w == g.nw - 1) ? 0 : 64 * w + 64; // site of the fetched east bit
+    auto ldw = [&](int d, unsigned row) -> uint64_t { return ld_state<CG>(s + (d * ps + row + widx)); };
+    auto lde = [&](int d, unsigned row) -> uint64_t { return ld_state<CG>(s + (d * ps + row + eidx)); };
+    uint64_t eg[4] = {0, 0, 0, 0};
+    if (MODEL == M_HPP) {
+        if (need_w) eg[0] = ldw(0, row0);
+        if (need_e) eg[1] = lde(2, row0);
+    } else if (even) {
+        if (need_w) {
+            eg[0] = ldw(0, row0);
+            eg[1] = ldw(1, rowm);
+            eg[2] = ldw(5, rowp);
+        }
+        if (need_e) eg[3] = lde(3, row0);
+    } else {
+        if (need_w) eg[0] = ldw(0, row0);
+        if (need_e) {
+            eg[1] = lde(3, row0);
+            eg[2] = lde(2, rowm);
+            eg[3] = lde(4, rowp);
+        }
+    }
 
-    // x-1 pull: (v << 1) | bit of site x-1
-    auto shl = [&](uint64_t v, int d, unsigned row) -> uint64_t {
+    // x-1 pull: (v << 1) | bit of site x-1 (from `edge` in lanes with need_w)
+    auto shl = [&](uint64_t v, uint64_t edge, bool fcol) -> uint64_t {
         const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v >> 32), 1, width);
         uint64_t in = hi >> 31;
         if (need_w) {
-            in = (ld_state<CG>(s + (d * ps + row + widx)) >> wbit) & 1ull;
-            if (d == 0 && row == row0 && forcing && wx == a.fx)
-                in |= force_flip_at<MODEL, GM, CG>(a, io, y);
+            in = (edge >> wbit) & 1ull;
+            if (fcol && forcing && wx == a.fx) in |= force_flip_at<MODEL, GM, CG>(a, io, y);
         }
         return (v << 1) | in;
     };
     // x+1 pull: (v >> 1) | bit of site x+1 placed at the last valid bit
-    auto shr = [&](uint64_t v, int d, unsigned row) -> uint64_t {
+    auto shr = [&](uint64_t v, uint64_t edge, bool fcol) -> uint64_t {
         const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v, 1, width);
         uint64_t in = lo & 1u;
         if (need_e) {
-            in = ld_state<CG>(s + (d * ps + row + eidx)) & 1ull;
-            if (d == WEST && row == row0 && forcing && ex == a.fx)
-                in &= ~force_flip_at<MODEL, GM, CG>(a, io, y);
+            in = edge & 1ull;
+            if (fcol && forcing && ex == a.fx) in &= ~force_flip_at<MODEL, GM, CG>(a, io, y);
         }
         return (v >> 1) | (in << epos);
     };
 
     uint64_t p[7];
     if (MODEL == M_HPP) {
-        p[0] = shl(n[0], 0, row0);
+        p[0] = shl(n[0], eg[0], true);
         p[1] = n[1];
-        p[2] = shr(n[2], 2, row0);
+        p[2] = shr(n[2], eg[1], true);
         p[3] = n[3];
+    } else if (even) {  // warp-uniform (row mapping contract)
+        p[0] = shl(n[0], eg[0], true);
+        p[1] = shl(n[1], eg[1], false);
+        p[5] = shl(n[5], eg[2], false);
+        p[3] = shr(n[3], eg[3], true);
+        p[2] = n[2];
+        p[4] = n[4];
+        if (D == 7) p[6] = n[6];
     } else {
-        p[0] = shl(n[0], 0, row0);
-        p[3] = shr(n[3], 3, row0);
-        if (even) {  // warp-uniform (row mapping contract)
-            p[1] = shl(n[1], 1, rowm);
-            p[5] = shl(n[5], 5, rowp);
-            p[2] = n[2];
-            p[4] = n[4];
-        } else {
-            p[2] = shr(n[2], 2, rowm);
-            p[4] = shr(n[4], 4, rowp);
-            p[1] = n[1];
-            p[5] = n[5];
-        }
+        p[0] = shl(n[0], eg[0], true);
+        p[3] = shr(n[3], eg[1], true);
+        p[2] = shr(n[2], eg[2], false);
+        p[4] = shr(n[4], eg[3], false);
+        p[1] = n[1];
+        p[5] = n[5];
         if (D == 7) p[6] = n[6];
     }
     if (!active) return;

@@ -428,7 +428,7 @@ class StepTimeTable:
                 W, H = s, max(256, s // 2)
                 L = gpu.GpuLattice(m, W, H, seed=1)
                 L.init_random(0.25, 0.25)
-                L.set_kernel_variant(1)
+                L.set_kernel_variant(0)  # the plain kernel: one step per pass, its fastest form
                 L.collide_and_propagate(5)
                 L.sync()
                 t0 = time.perf_counter()
@@ -470,7 +470,7 @@ def verify_sample(jobs, n: int = 8, block: int = 16, seed: int = 0) -> bool:
     ok = True
     for j in pick:
         L = build_alone(j)
-        L.set_kernel_variant(1)
+        L.set_kernel_variant(1)  # one word per lane: another code path than the batch's
         L.collide_and_propagate(j.steps)
         f = L.block_sums(block)
         ok &= all(np.array_equal(a, b) for a, b in zip(f, j.last_fields))
