@@ -33,7 +33,11 @@ __global__ void __launch_bounds__(256, GMAX == GEOM_FULL ? 3 : 4)
             const int *__restrict__ s_base)
 {
     pdl_launch_dependents();
-    pdl_wait();  // keys, step counter and states come from earlier kernels
+    // The work-list, the key table and the step counter were written before
+    // the chain of batch steps began (copies and plain kernels, which
+    // complete before the chain's first kernel starts) and stay unchanged
+    // along it, so they are read before the wait; only the states come from
+    // the previous step.
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const BatchEntry &e = E[block_lat[blockIdx.x]];
     const int base = blockIdx.x * 8 * T - e.task0;  // the block's first task of its lattice
@@ -41,6 +45,7 @@ __global__ void __launch_bounds__(256, GMAX == GEOM_FULL ? 3 : 4)
     const ulonglong2 k = __ldg(reinterpret_cast<const ulonglong2 *>(e.keys) + s);
     const StepIO io{(s & 1) ? e.buf1 : e.buf0, (s & 1) ? e.buf0 : e.buf1, k.x, k.y};
     const StepArgs &a = e.a;
+    pdl_wait();
     for (int i = 0; i < T; ++i) {
         const int local = base + warp + 8 * i;
         if (local >= e.tasks) break;  // padding: warp-uniform
