@@ -232,6 +232,10 @@ int lgca_sync(lgca_handle h);
 
 /* The cudaStream_t the handle enqueues on (as void*), and a way to replace
  * it by a caller-owned stream (NULL restores the handle's own stream).
+ * lgca_stream also orders the stream after the lattice's queued batch steps
+ * and marks it used, so that the lattice's next batch step runs after what
+ * the caller queues on it: call it again after each batch call, rather than
+ * keeping the pointer across batch calls.
  * Steps queued on a stream under CUDA graph capture are recorded with their
  * buffers and random keys fixed at capture time: a replay repeats steps
  * t .. t+k-1 of the capturing call, so capture an even number of steps to
@@ -265,7 +269,10 @@ int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes);
  *   lgca_batch_step_each: member i (in the order added) advances nsteps[i]
  *   steps (0 = not at all); members with fewer steps drop out of the
  *   work-list when done.  Work queued on a member's own stream before the
- *   call runs first; the member's later calls run after the batch.
+ *   call runs first; the member's later calls run after the batch.  Both
+ *   orders are set up lazily: a call costs one stream wait per member whose
+ *   stream was used since it last stepped, and none for the others; the
+ *   member's stream waits for the batch at the member's next call.
  *   A lattice belongs to at most one batch; lgca_destroy removes it from
  *   its batch first. */
 typedef struct lgca_batch *lgca_batch_handle;

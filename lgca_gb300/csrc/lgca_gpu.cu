@@ -42,6 +42,15 @@ struct lgca_lattice {
     int *sync_err_host = nullptr; // pinned copy of the error flag, checked at sync points
     size_t bytes = 0;
     lgca_batch *batch = nullptr;  // the batch this lattice belongs to, if any
+    // Ordering against batch calls without stream calls per member and call:
+    // `after_batch` -- batch steps of this lattice are queued on the batch's
+    // stream and the handle's stream has not yet been made to wait for them
+    // (done at the handle's next use, on `batch_done`); `used` -- work was
+    // queued on the handle's stream since the last batch call that stepped it,
+    // so the next such call orders its steps after that work.
+    cudaEvent_t batch_done = nullptr;
+    bool after_batch = false;
+    bool used = true;
     std::string err;
 };
 
@@ -174,7 +183,28 @@ int geom_mode(const lgca_lattice *h)
 
 bool valid(lgca_handle h) { return h != nullptr && h->buf[0] != nullptr; }
 
+// Called before the handle's stream is used: the stream waits for the batch
+// steps queued for the lattice (once per batch call), and is marked used.
+int enter(lgca_lattice *h)
+{
+    if (h->after_batch) {
+        const cudaError_t e = cudaStreamWaitEvent(h->stream, h->batch_done, 0);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamWaitEvent (batch)");
+        h->after_batch = false;
+    }
+    h->used = true;
+    return LGCA_OK;
+}
+
+// Entry points that queue work on, or wait for, the handle's stream.
 #define CHECK_HANDLE(h)                                                          \
+    do {                                                                         \
+        if (!valid(h)) return fail(nullptr, LGCA_ERR_INVALID, "invalid handle"); \
+        if (const int st_ = enter(h)) return st_;                                \
+    } while (0)
+
+// Entry points that only read or set host-side fields.
+#define CHECK_VALID(h)                                                           \
     do {                                                                         \
         if (!valid(h)) return fail(nullptr, LGCA_ERR_INVALID, "invalid handle"); \
     } while (0)
@@ -263,7 +293,10 @@ int lgca_destroy(lgca_handle h)
 {
     if (!h) return LGCA_OK;
     DeviceGuard dg(h->device);
-    if (h->batch) lgca_batch_remove(h->batch, h);  // the batch must not keep a dangling member
+    // the batch must not keep a dangling member; leaving orders the frees
+    // below after the lattice's queued batch steps (a failed wait: a full
+    // device sync instead)
+    if (h->batch && lgca_batch_remove(h->batch, h) != LGCA_OK) cudaDeviceSynchronize();
     // memory goes back to the pool in stream order, after the handle's queued
     // work (batch steps of a member are ordered before it); no host wait
     void *mem[] = {h->buf[0], h->buf[1], h->solid, h->slip, h->chir, h->scratch, h->sync};
@@ -287,7 +320,7 @@ int lgca_trim_memory(int device, uint64_t keep_bytes)
 
 int lgca_info(lgca_handle h, int *model, int *W, int *H, uint64_t *seed, uint64_t *step)
 {
-    CHECK_HANDLE(h);
+    CHECK_VALID(h);
     if (model) *model = h->model;
     if (W) *W = h->g.W;
     if (H) *H = h->g.H;
@@ -298,7 +331,7 @@ int lgca_info(lgca_handle h, int *model, int *W, int *H, uint64_t *seed, uint64_
 
 int lgca_set_step(lgca_handle h, uint64_t t)
 {
-    CHECK_HANDLE(h);
+    CHECK_VALID(h);
     h->t = t;
     return LGCA_OK;
 }
@@ -443,7 +476,7 @@ int lgca_init_zero(lgca_handle h)
 
 int lgca_set_forcing_column(lgca_handle h, int x, double p)
 {
-    CHECK_HANDLE(h);
+    CHECK_VALID(h);
     if (x >= h->g.W) return fail(h, LGCA_ERR_INVALID, "forcing column %d outside 0..%d", x, h->g.W - 1);
     if (!(p >= 0.0 && p <= 1.0)) return fail(h, LGCA_ERR_INVALID, "probability must lie in [0, 1]");
     if (x < 0 || p <= 0.0) {
@@ -480,7 +513,7 @@ int lgca_set_chirality(lgca_handle h, const uint8_t *field)
 
 int lgca_set_temporal_depth(lgca_handle h, int depth)
 {
-    CHECK_HANDLE(h);
+    CHECK_VALID(h);
     if (depth < 1 || depth > 8) return fail(h, LGCA_ERR_INVALID, "depth %d outside 1..8", depth);
     h->depth = depth;
     return LGCA_OK;
@@ -488,7 +521,7 @@ int lgca_set_temporal_depth(lgca_handle h, int depth)
 
 int lgca_set_kernel_variant(lgca_handle h, int variant)
 {
-    CHECK_HANDLE(h);
+    CHECK_VALID(h);
     if (variant < VARIANT_AUTO || variant > VARIANT_PLAIN2)
         return fail(h, LGCA_ERR_INVALID, "unknown kernel variant %d", variant);
     h->variant = variant;
@@ -497,7 +530,7 @@ int lgca_set_kernel_variant(lgca_handle h, int variant)
 
 int lgca_set_block_warps(lgca_handle h, int warps)
 {
-    CHECK_HANDLE(h);
+    CHECK_VALID(h);
     if (!(warps == 0 || warps == 1 || warps == 2 || warps == 4 || warps == 8))
         return fail(h, LGCA_ERR_INVALID, "warps per block must be 0, 1, 2, 4 or 8");
     h->bw = warps;
@@ -724,7 +757,13 @@ int lgca_sync(lgca_handle h)
     return LGCA_OK;
 }
 
-void *lgca_stream(lgca_handle h) { return valid(h) ? (void *)h->stream : nullptr; }
+void *lgca_stream(lgca_handle h)
+{
+    // the caller queues work on the stream: order it after the lattice's
+    // batch steps and before its next ones
+    if (!valid(h) || enter(h) != LGCA_OK) return nullptr;
+    return (void *)h->stream;
+}
 
 int lgca_set_stream(lgca_handle h, void *stream)
 {
@@ -765,7 +804,7 @@ size_t ckpt_planes(const lgca_lattice *h)
 
 int lgca_checkpoint_size(lgca_handle h, size_t *bytes)
 {
-    CHECK_HANDLE(h);
+    CHECK_VALID(h);
     if (!bytes) return fail(h, LGCA_ERR_INVALID, "bytes is NULL");
     const size_t plane = (size_t)h->g.H * h->g.nw * sizeof(uint64_t);
     *bytes = sizeof(CkptHeader) + ckpt_planes(h) * plane;
@@ -870,7 +909,7 @@ int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes)
 
 int lgca_device_bytes(lgca_handle h, size_t *bytes)
 {
-    CHECK_HANDLE(h);
+    CHECK_VALID(h);
     if (bytes) *bytes = h->bytes;
     return LGCA_OK;
 }
@@ -983,7 +1022,12 @@ int lgca_batch_destroy(lgca_batch_handle b)
     if (!b) return LGCA_OK;
     DeviceGuard dg(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
-    for (lgca_lattice *m : b->members) m->batch = nullptr;
+    for (lgca_lattice *m : b->members) {
+        // the batch's steps are complete (synchronised above)
+        m->batch = nullptr;
+        m->batch_done = nullptr;
+        m->after_batch = false;
+    }
     for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
     cudaFree(b->dE);
     cudaFree(b->dP);  // dB lives in the same allocation
@@ -1012,6 +1056,9 @@ int lgca_batch_add(lgca_batch_handle b, lgca_handle h)
     b->members.push_back(h);
     b->ev.push_back(e);
     h->batch = b;
+    h->batch_done = b->done;
+    h->after_batch = false;
+    h->used = true;  // the first batch call waits for the lattice's queued work
     return LGCA_OK;
 }
 
@@ -1021,11 +1068,17 @@ int lgca_batch_remove(lgca_batch_handle b, lgca_handle h)
     DeviceGuard dg(b->device);
     for (size_t i = 0; i < b->members.size(); ++i) {
         if (b->members[i] == h) {
-            // the member's stream already waits for the batch's queued steps
+            // the lattice's stream waits for its queued batch steps before it
+            // leaves (its next work, or the frees of lgca_destroy, follow them)
+            const cudaError_t e = h->after_batch ? cudaStreamWaitEvent(h->stream, b->done, 0)
+                                                 : cudaSuccess;
+            h->after_batch = false;
+            h->batch_done = nullptr;
             cudaEventDestroy(b->ev[i]);
             h->batch = nullptr;
             b->members.erase(b->members.begin() + i);
             b->ev.erase(b->ev.begin() + i);
+            if (e != cudaSuccess) return bcuda(b, e, "cudaStreamWaitEvent (leaving the batch)");
             return LGCA_OK;
         }
     }
@@ -1062,12 +1115,15 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
     const size_t nm = b->members.size();
     for (size_t i = 0; i < nm; ++i)
         if (nsteps[i] < 0) return bfail(b, LGCA_ERR_INVALID, "negative step count");
-    // order after each member's own pending work (no host wait: the work-list
-    // copies below are queued behind the previous call's steps)
+    // order after the work queued on a member's own stream since the last
+    // call that stepped it; members with none cost no stream call (no host
+    // wait either: the work-list copies below queue behind the previous call)
     for (size_t i = 0; i < nm; ++i) {
-        if (nsteps[i] == 0) continue;
-        BCK(b, cudaEventRecord(b->ev[i], b->members[i]->stream));
+        lgca_lattice *h = b->members[i];
+        if (nsteps[i] == 0 || !h->used) continue;
+        BCK(b, cudaEventRecord(b->ev[i], h->stream));
         BCK(b, cudaStreamWaitEvent(b->stream, b->ev[i], 0));
+        h->used = false;
     }
     // lane items per row of a member: word pairs where the width allows
     auto pair_of = [](const lgca_lattice *h) {
@@ -1209,12 +1265,14 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         }
         s0 = s1;
     }
-    // members continue after the batch
+    // members continue after the batch: each member's stream waits on `done`
+    // at its next use (enter); `done` is recorded again by later calls, which
+    // finish later on this stream, so a wait issued then still covers this call
     BCK(b, cudaEventRecord(b->done, b->stream));
     for (size_t i = 0; i < nm; ++i) {
         if (nsteps[i] == 0) continue;
         lgca_lattice *h = b->members[i];
-        BCK(b, cudaStreamWaitEvent(h->stream, b->done, 0));
+        h->after_batch = true;
         if (nsteps[i] & 1) h->cur ^= 1;
         h->t += (uint64_t)nsteps[i];
     }

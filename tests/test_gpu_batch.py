@@ -87,6 +87,46 @@ def test_batch_calls_interleave_with_member_calls(gpu, oracle):
     Bl.close()
 
 
+def test_batch_ordering_with_long_queues(gpu):
+    """Ordering between a member's own stream and batch calls with enough
+    queued work on both sides that a missing dependency would show: a long
+    run queued on a member before the batch call, block sums queued on it
+    right after (they must see the batch's steps), more own steps, another
+    batch call, and a stream fetched by the caller after a batch call."""
+    import torch
+    W, H = 4096, 2048
+    A = gpu.GpuLattice(3, W, H, seed=21)
+    S = gpu.GpuLattice(0, 512, 64, seed=22)
+    A.init_random(0.3, 0.3)
+    S.init_random(0.2)
+    twin = gpu.GpuLattice(3, W, H, seed=21)
+    twin.init_random(0.3, 0.3)
+    A.collide_and_propagate(60)  # queued on A's stream, not synchronised
+    n = np.zeros((3, H // 32, W // 32), dtype=np.int32)
+    with gpu.GpuBatch(graph_steps=0) as B:
+        B.add(A)
+        B.add(S)
+        B.step_each([40, 40])
+        A.block_sums_async(32, n[0], n[1], n[2])  # after the batch's 40 steps
+        A.collide_and_propagate(7)
+        B.step(3)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.ExternalStream(A.stream_ptr()))  # after the second call
+        ev.synchronize()
+        # the fetched stream waited for the whole second call
+        assert torch.cuda.ExternalStream(B.stream_ptr()).query()
+        got = A.download()
+    twin.collide_and_propagate(100)
+    n_want = twin.block_sums(32)
+    twin.collide_and_propagate(10)
+    assert np.array_equal(got, twin.download())
+    for a, b in zip(n, n_want):
+        assert np.array_equal(a, b)
+    assert A.step_count == 110 and S.step_count == 43
+    for L in (A, S, twin):
+        L.close()
+
+
 def test_batched_config_small_is_bit_exact_and_faster(gpu):
     """The batched workload generator at reduced scale: batched and
     one-at-a-time runs agree bit for bit (the full 512 x 1000 run is in the
