@@ -1144,10 +1144,23 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         const long long wave = 32LL * sm_count();
         b->call_wt = all >= 128 * wave ? 4 : (all >= 8 * wave ? 2 : 1);
     }
-    // one work-list, lattices sorted by steps (descending)
-    std::vector<int> order(nm);
-    for (size_t i = 0; i < nm; ++i) order[i] = (int)i;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return nsteps[x] > nsteps[y]; });
+    // kernel code of a member: family x geometry mode x lane path
+    auto code_of = [&](const lgca_lattice *h) {
+        const int fam = h->model == LGCA_HPP ? 0 : (h->model == LGCA_FHP_I ? 1 : 2);
+        const int path = pair_of(h) ? ((h->g.nw & 1) ? 2 : 1) : 0;
+        return fam * 9 + geom_mode(h) * 3 + path;
+    };
+    // one work-list, lattices sorted by steps (descending: a segment's active
+    // members are a prefix), then by kernel code, so that the blocks resident
+    // at one time mostly run one code path (fewer instruction-cache misses)
+    std::vector<int> order(nm), code(nm);
+    for (size_t i = 0; i < nm; ++i) {
+        order[i] = (int)i;
+        code[i] = code_of(b->members[i]);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return nsteps[x] != nsteps[y] ? nsteps[x] > nsteps[y] : code[x] < code[y];
+    });
     b->E.clear();
     b->P.assign(1, 0);
     b->nsteps.clear();
@@ -1168,8 +1181,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         e.a.wpt = pair ? 2 : 1;
         e.wpt = e.a.wpt;
         e.gm = geom_mode(h);
-        const int fam = h->model == LGCA_HPP ? 0 : (h->model == LGCA_FHP_I ? 1 : 2);
-        e.code = fam * 9 + e.gm * 3 + (pair ? ((h->g.nw & 1) ? 2 : 1) : 0);
+        e.code = code[i];
         e.items = pair ? (h->g.nw + 1) / 2 : h->g.nw;  // lane items per row (last pair may be half)
         e.a.fmagic = flat_magic(h->g.H, e.items);
         e.buf0 = h->buf[h->cur];

@@ -164,6 +164,19 @@ def test_fcfs_baseline_queueing():
     assert base["p50_latency_s"] == pytest.approx(3.0)
 
 
+def test_step_time_table_statistics():
+    """Median and fastest repeat of each sample, interpolated log-log by site
+    count (the table's samples are set by hand; measuring them needs a GPU)."""
+    t = object.__new__(S.StepTimeTable)
+    t.stat = "median"
+    t.samples = {m: [(1000, [3e-6, 1e-6, 2e-6]), (100000, [4e-4, 1e-4, 2e-4])] for m in range(4)}
+    job = S.Job(index=0, arrival=0.0, model=2, W=100, H=100, geometry="periodic", p=0.2,
+                steps=10, seed=0)  # 10^4 sites: halfway in log between the samples
+    assert t(job) == pytest.approx((2e-6 * 2e-4) ** 0.5)
+    assert t.with_stat("best")(job) == pytest.approx((1e-6 * 1e-4) ** 0.5)
+    assert t.stat == "median"
+
+
 def test_job_stream_shapes():
     jobs = S.make_jobs(100.0, 5.0, rng_seed=3)
     assert all(j.W % 64 == 0 and j.H % 64 == 0 and 256 <= j.W <= 8192 and 256 <= j.H <= 4096
