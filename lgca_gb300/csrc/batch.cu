@@ -56,10 +56,10 @@ __global__ void __launch_bounds__(256, GMAX == GEOM_FULL ? 3 : 4)
         if (GM <= GMAX) step_word<MODEL, GM, true>(a, io, y, w, lane);                         \
         break;                                                                                 \
     case F * 9 + GM * 3 + 1:                                                                   \
-        if (GM <= GMAX) step_pair<MODEL, GM, true, false, false>(a, io, y, w, lane);           \
+        if (GM <= GMAX) step_pair<MODEL, GM, true, false, false, true>(a, io, y, w, lane);     \
         break;                                                                                 \
     case F * 9 + GM * 3 + 2:                                                                   \
-        if (GM <= GMAX) step_pair<MODEL, GM, true, false, true>(a, io, y, w, lane);            \
+        if (GM <= GMAX) step_pair<MODEL, GM, true, false, true, true>(a, io, y, w, lane);      \
         break;
 #define LGCA_BATCH_CASES(F, MODEL)                                                             \
     LGCA_BATCH_CASE(F, MODEL, GEOM_NONE)                                                       \

@@ -252,8 +252,13 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
 // fits in one wave of resident warps.  Same arithmetic as step_word.  With an
 // odd number of words per row (ODD) the last pair holds the last word and the
 // row's padding word (the pitch is even): that word's east neighbour is the
-// seam word, and the padding word is written back as zero.
-template <int MODEL, int GM, bool CG = false, bool PRE = false, bool ODD = false>
+// seam word, and the padding word is written back as zero.  With WRAP the
+// periodic seam words of a row that lies inside the lane segment come from
+// the row's own first and last lanes by shuffle, so that narrow rows (a few
+// lane items each) load no edge words at all; only words held by another
+// segment are loaded.
+template <int MODEL, int GM, bool CG = false, bool PRE = false, bool ODD = false,
+          bool WRAP = false>
 __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, const int y,
                                           const int t, const int lane, const int width = 32,
                                           const uint64_t pre0 = 0, const uint64_t pre1 = 0)
@@ -311,8 +316,15 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
     //   FHP, even row: west 0 (row y), 1 (y-1), 5 (y+1); east 3 (row y)
     //   FHP, odd row:  west 0 (row y); east 3 (row y), 2 (y-1), 4 (y+1)
     //   HPP:           west 0 (row y); east 2 (row y)
-    const bool need_w = active && (seg == 0 || t == 0);
-    const bool need_e = active && (seg == width - 1 || t == np - 1);
+    // source lanes, within the segment, of the words west and east of the
+    // pair: the neighbouring items of the row, or across the seam (WRAP) the
+    // row's last / first item; a source outside the segment means a load
+    const int srcw = WRAP ? seg + (t == 0 ? np - 1 : -1) : seg - 1;
+    const int srce = WRAP ? seg + (t == np - 1 ? 1 - np : 1) : seg + 1;
+    const bool need_w =
+        active && (WRAP ? (unsigned)srcw >= (unsigned)width : (seg == 0 || t == 0));
+    const bool need_e =
+        active && (WRAP ? (unsigned)srce >= (unsigned)width : (seg == width - 1 || t == np - 1));
     const int widx = (t == 0) ? g.nw - 1 : w0 - 1;
     const int eidx = (t == np - 1) ? 0 : w0 + 2;
     auto ldw = [&](int d, unsigned row) -> uint64_t { return ld_state<CG>(s + (d * ps + row + widx)); };
@@ -361,7 +373,10 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
     // x-1 pull of the pair (v0, v1); `edge` is the word west of it, read by
     // lanes with need_w (and forced there when it holds the forcing column)
     auto shl = [&](uint64_t v0, uint64_t v1, uint64_t edge, bool fcol, int k) -> uint64_t {
-        const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v1 >> 32), 1, width);
+        // a lane offers the high half of its last real word (v0 in a half pair)
+        const uint32_t hi =
+            WRAP ? __shfl_sync(FULL, (uint32_t)((half ? v0 : v1) >> 32), srcw, width)
+                 : __shfl_up_sync(FULL, (uint32_t)(v1 >> 32), 1, width);
         uint64_t in = hi >> 31;
         if (need_w) {
             in = edge >> 63;
@@ -371,7 +386,8 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
     };
     // x+1 pull of the pair; `edge` is the word east of it
     auto shr = [&](uint64_t v0, uint64_t v1, uint64_t edge, bool fcol, int k) -> uint64_t {
-        const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v0, 1, width);
+        const uint32_t lo = WRAP ? __shfl_sync(FULL, (uint32_t)v0, srce, width)
+                                 : __shfl_down_sync(FULL, (uint32_t)v0, 1, width);
         uint64_t in = lo & 1u;
         if (need_e) {
             in = edge & 1ull;
