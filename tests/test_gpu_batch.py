@@ -18,7 +18,7 @@ def make_jobs(gpu, n, rng, max_side=700):
     jobs = []
     for i in range(n):
         model = int(rng.integers(4))
-        W = int(rng.choice([64, 100, 128, 256, 300, 512, 640, max_side]))
+        W = int(rng.choice([64, 100, 128, 192, 256, 300, 320, 512, 640, max_side]))
         H = 2 * int(rng.integers(2, max_side // 2))
         types = GEOMS[int(rng.integers(len(GEOMS)))](W, H)
         L = gpu.GpuLattice(model, W, H, seed=1000 + i)
