@@ -1125,6 +1125,21 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         BCK(b, cudaStreamWaitEvent(b->stream, b->ev[i], 0));
         h->used = false;
     }
+    // From here on steps may be queued.  If the call fails part way, the
+    // members it covers still order their next use after what it queued
+    // (their states are then unspecified, as after any failed call).
+    struct OnFailure {
+        lgca_batch *b;
+        const int *nsteps;
+        bool armed = true;
+        ~OnFailure()
+        {
+            if (!armed) return;
+            if (cudaEventRecord(b->done, b->stream) != cudaSuccess) cudaStreamSynchronize(b->stream);
+            for (size_t i = 0; i < b->members.size(); ++i)
+                if (nsteps[i] > 0) b->members[i]->after_batch = true;
+        }
+    } on_failure{b, nsteps};
     // lane items per row of a member: word pairs where the width allows
     auto pair_of = [](const lgca_lattice *h) {
         return h->variant != VARIANT_PLAIN && h->wpt == 2 && (h->g.W % 64) == 0;
@@ -1288,6 +1303,7 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         if (nsteps[i] & 1) h->cur ^= 1;
         h->t += (uint64_t)nsteps[i];
     }
+    on_failure.armed = false;
     return LGCA_OK;
 }
 
