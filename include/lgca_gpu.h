@@ -6,8 +6,9 @@
  * its geometry planes, its step counter and the CUDA stream it runs on.
  * Plain C types only; every call returns an lgca_status (0 = success) and
  * records a message retrievable with lgca_last_error().  Calls on one handle
- * must not overlap from several host threads.  Host buffers are owned by the
- * caller and may be freed when the call returns.
+ * must not overlap from several host threads, and a call on a batch counts
+ * as a call on each of its members.  Host buffers are owned by the caller
+ * and may be freed when the call returns.
  *
  * The entry points replace the backend half of the reference's Lattice<Model>
  * interface (keva92/lgca src/lattice.h:32-238, implemented by OMP_Lattice in
