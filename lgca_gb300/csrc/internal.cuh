@@ -229,14 +229,18 @@ __host__ __device__ __forceinline__ uint32_t flat_magic(int H, int items)
 }
 
 // Row y and item of `lane` in warp task `task` (y >= H past a class's end);
-// magic = flat_magic(H, items).
-__device__ __forceinline__ void flat_site(long long task, int lane, int H, int items,
-                                          uint32_t magic, int &y, int &item)
+// magic = flat_magic(H, items).  Host-callable for the mapping checks.
+__host__ __device__ __forceinline__ void flat_site(long long task, int lane, int H, int items,
+                                                   uint32_t magic, int &y, int &item)
 {
     const long long even_tasks = class_tasks(H, items, 0);
     const int p = task >= even_tasks ? 1 : 0;
     const unsigned l = (unsigned)((p ? task - even_tasks : task) * 32 + lane);
+#ifdef __CUDA_ARCH__
     const unsigned r = magic ? __umulhi(l, magic) : l / (unsigned)items;
+#else
+    const unsigned r = magic ? (unsigned)(((unsigned long long)l * magic) >> 32) : l / (unsigned)items;
+#endif
     item = (int)(l - r * (unsigned)items);
     y = (int)(2 * r + p);
 }
