@@ -1,0 +1,76 @@
+"""CPU parity of the CUDA step bodies themselves: tests/step_emu.cpp compiles
+lgca_gb300/csrc/step_body.cuh with g++, runs every warp as 32 host threads
+in lockstep (shuffles through a shared array), and the states it reaches are
+compared bit for bit with the oracle.  Covers the one-word body, the
+two-words-per-lane body with and without the batch kernel's seam shuffles
+(WRAP), odd word counts (a half last pair), narrow rows that share a warp,
+every model and geometry mode, and forcing columns on word edges and at the
+x seam.  No GPU is needed."""
+import os
+import shutil
+import struct
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from lgca_gb300 import geometry as G
+
+
+@pytest.fixture(scope="module")
+def emu(tmp_path_factory):
+    gxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if gxx is None or not os.path.isdir(cuda_inc):
+        pytest.skip("g++ or the CUDA headers not available")
+    exe = tmp_path_factory.mktemp("emu") / "step_emu"
+    subprocess.run([gxx, "-O2", "-std=c++20", "-Wno-attributes", "-I", cuda_inc,
+                    os.path.join(ROOT, "tests", "step_emu.cpp"), "-o", str(exe), "-pthread"],
+                   check=True, capture_output=True)
+    return exe
+
+
+def run_emu(exe, tmp, model, cells, types, steps, seed, t0, force_x, force_thr, path):
+    H, W = cells.shape
+    inp, out = tmp / "in.bin", tmp / "out.bin"
+    with open(inp, "wb") as f:
+        f.write(struct.pack("<6i3Q", model, W, H, steps, force_x, path, seed, t0, force_thr))
+        f.write(np.ascontiguousarray(cells, np.uint8).tobytes())
+        f.write(np.ascontiguousarray(types, np.uint8).tobytes())
+    r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True)
+    assert r.returncode == 0, (r.returncode, r.stderr[-500:])
+    return np.frombuffer(out.read_bytes(), np.uint8).reshape(H, W)
+
+
+GEOMS = {
+    "periodic": lambda w, h: G.periodic(w, h),
+    "pipe": G.pipe,
+    "disc": lambda w, h: G.disc(w, h, w // 3, h // 2, max(2, h // 5)),
+    "slip": lambda w, h: G.reflecting(w, h, "forward"),
+}
+
+# (width, height): pair widths with even and odd word counts, rows narrower
+# than a warp (several rows per warp) and wider; one-word widths
+PAIR = [(64, 12), (128, 10), (192, 14), (256, 8), (320, 12), (640, 6), (2112, 4)]
+WORD = [(100, 10), (300, 8)]
+
+
+@pytest.mark.parametrize("model", [0, 1, 3])
+@pytest.mark.parametrize("geom", list(GEOMS))
+def test_emulated_step_bodies_equal_oracle(emu, tmp_path, oracle, model, geom):
+    rng = np.random.default_rng(model * 31 + len(geom))
+    for W, H in PAIR + WORD:
+        types = GEOMS[geom](W, H).astype(np.uint8)
+        st = oracle.init_bernoulli(model, W, H, GEOMS[geom](W, H), seed=7, p_move=0.35,
+                                   p_rest=0.3)
+        # forcing on both seam words and at a random column
+        for fx in sorted({0, W - 1, int(rng.integers(W))}):
+            p = 0.4
+            thr = oracle.prob_threshold(p)
+            want = oracle.run(model, st, 5, types=GEOMS[geom](W, H), seed=11, t0=3,
+                              force_x=fx, force_p=p)
+            paths = (1, 2) if W % 64 == 0 else (0,)
+            for path in paths:
+                got = run_emu(emu, tmp_path, model, st, types, 5, 11, 3, fx, thr, path)
+                assert np.array_equal(got, want), (model, geom, W, H, fx, path)
