@@ -74,3 +74,33 @@ def test_emulated_step_bodies_equal_oracle(emu, tmp_path, oracle, model, geom):
             for path in paths:
                 got = run_emu(emu, tmp_path, model, st, types, 5, 11, 3, fx, thr, path)
                 assert np.array_equal(got, want), (model, geom, W, H, fx, path)
+
+
+def test_emulated_step_bodies_stay_in_bounds(tmp_path, oracle):
+    """The step bodies' loads and stores stay inside the state, geometry and
+    output buffers: the emulator built with the address and undefined-
+    behaviour sanitizers, on the widths where rows share or straddle warps."""
+    gxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if gxx is None or not os.path.isdir(cuda_inc):
+        pytest.skip("g++ or the CUDA headers not available")
+    exe = tmp_path / "step_emu_asan"
+    r = subprocess.run([gxx, "-O1", "-g", "-std=c++20", "-Wno-attributes",
+                        "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
+                        "-fno-omit-frame-pointer", "-I", cuda_inc,
+                        os.path.join(ROOT, "tests", "step_emu.cpp"), "-o", str(exe), "-pthread"],
+                       capture_output=True)
+    if r.returncode != 0:
+        pytest.skip("sanitizer runtime not available")
+    for model in (0, 3):
+        for W, H in [(64, 12), (320, 12), (640, 6), (2112, 4), (100, 10)]:
+            for geom in ("periodic", "slip"):
+                types = GEOMS[geom](W, H).astype(np.uint8)
+                st = oracle.init_bernoulli(model, W, H, GEOMS[geom](W, H), seed=7, p_move=0.35,
+                                           p_rest=0.3)
+                thr = oracle.prob_threshold(0.4)
+                want = oracle.run(model, st, 3, types=GEOMS[geom](W, H), seed=11, t0=3,
+                                  force_x=W - 1, force_p=0.4)
+                for path in ((1, 2) if W % 64 == 0 else (0,)):
+                    got = run_emu(exe, tmp_path, model, st, types, 3, 11, 3, W - 1, thr, path)
+                    assert np.array_equal(got, want), (model, geom, W, H, path)
