@@ -29,10 +29,19 @@ namespace lgca_gpu {
 // the non-coherent L1/texture path: grids of consecutive steps share SMs, so
 // an SM's L1 can still hold lines of a buffer that an older step read and the
 // step in between has since rewritten.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// (Host builds of the kernel bodies -- the CPU emulation in the tests -- see
+// no-ops.)
+__device__ __forceinline__ void pdl_wait()
+{
+#ifdef __CUDA_ARCH__
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
 __device__ __forceinline__ void pdl_launch_dependents()
 {
+#ifdef __CUDA_ARCH__
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
 }
 
 //

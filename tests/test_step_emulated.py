@@ -104,3 +104,46 @@ def test_emulated_step_bodies_stay_in_bounds(tmp_path, oracle):
                 for path in ((1, 2) if W % 64 == 0 else (0,)):
                     got = run_emu(exe, tmp_path, model, st, types, 3, 11, 3, W - 1, thr, path)
                     assert np.array_equal(got, want), (model, geom, W, H, path)
+
+
+@pytest.fixture(scope="module")
+def multistep_emu(tmp_path_factory):
+    gxx = shutil.which("g++")
+    cuda = "/usr/local/cuda"
+    if gxx is None or not os.path.isdir(os.path.join(cuda, "include")):
+        pytest.skip("g++ or the CUDA headers not available")
+    exe = tmp_path_factory.mktemp("emu") / "multistep_emu"
+    lib = os.path.join(cuda, "lib64")
+    subprocess.run([gxx, "-O2", "-std=c++20", "-Wno-attributes", "-I", os.path.join(cuda, "include"),
+                    os.path.join(ROOT, "tests", "multistep_emu.cpp"), "-o", str(exe), "-pthread",
+                    "-L", lib, "-lcudart", f"-Wl,-rpath,{lib}"], check=True, capture_output=True)
+    return exe
+
+
+@pytest.mark.parametrize("model", [0, 1, 3])
+def test_emulated_temporal_blocking_kernels_equal_oracle(multistep_emu, tmp_path, oracle, model):
+    """k_wave (register wavefront) and k_multistep (shared-memory tiles) run
+    as host threads: K = 2, 4, 8 steps per pass (the FHP wavefront up to 4),
+    strips and tiles that wrap around narrow lattices, slabs that do not
+    divide the height, every geometry mode and a forcing column on the seam."""
+    for W, H in [(640, 40), (2112, 24), (128, 20)]:
+        for geom in ("periodic", "pipe", "slip"):
+            types = GEOMS[geom](W, H)
+            st = oracle.init_bernoulli(model, W, H, types, seed=7, p_move=0.35, p_rest=0.3)
+            thr = oracle.prob_threshold(0.4)
+            for kernel in (0, 1):
+                for depth in (2, 4, 8):
+                    if kernel == 0 and depth == 8 and model != 0:
+                        continue  # the FHP wavefront holds at most 4 time levels
+                    want = oracle.run(model, st, depth, types=types, seed=11, t0=3,
+                                      force_x=W - 1, force_p=0.4)
+                    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+                    with open(inp, "wb") as f:
+                        f.write(struct.pack("<7i3Q", model, W, H, depth, W - 1, kernel, depth,
+                                            11, 3, thr))
+                        f.write(st.tobytes())
+                        f.write(types.astype(np.uint8).tobytes())
+                    r = subprocess.run([str(multistep_emu), str(inp), str(out)], capture_output=True)
+                    assert r.returncode == 0, (model, W, H, geom, kernel, depth, r.returncode)
+                    got = np.frombuffer(out.read_bytes(), np.uint8).reshape(H, W)
+                    assert np.array_equal(got, want), (model, W, H, geom, kernel, depth)
