@@ -147,3 +147,35 @@ def test_emulated_temporal_blocking_kernels_equal_oracle(multistep_emu, tmp_path
                     assert r.returncode == 0, (model, W, H, geom, kernel, depth, r.returncode)
                     got = np.frombuffer(out.read_bytes(), np.uint8).reshape(H, W)
                     assert np.array_equal(got, want), (model, W, H, geom, kernel, depth)
+
+
+def test_emulated_step_bodies_random_configurations(emu, tmp_path, oracle):
+    """Seeded random small lattices: any width (pair paths for multiples of
+    64), random cell-type noise including slip cells, forcing anywhere with
+    any probability, random seeds and start steps."""
+    rng = np.random.default_rng(2024)
+    for _ in range(40):
+        model = int(rng.integers(4))
+        W = 64 * int(rng.integers(1, 12)) if rng.random() < 0.6 else int(rng.integers(1, 700))
+        H = 2 * int(rng.integers(1, 20))
+        kind = int(rng.integers(3))
+        if kind == 0:
+            types = G.pipe(W, H)
+        elif kind == 1:
+            types = G.disc(W, H, int(rng.integers(W)), int(rng.integers(H)), int(rng.integers(1, 6)))
+        else:
+            types = rng.choice([0, 0, 0, 1, 2], size=(H, W)).astype(np.int32)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        st = oracle.init_bernoulli(model, W, H, types, seed=int(rng.integers(1000)),
+                                   p_move=float(rng.uniform(0.1, 0.6)),
+                                   p_rest=float(rng.uniform(0.1, 0.6)))
+        fx = int(rng.integers(W)) if rng.random() < 0.7 else -1
+        p = float(rng.uniform(0.05, 1.0))
+        seed, t0, steps = int(rng.integers(1 << 40)), int(rng.integers(1 << 20)), int(rng.integers(1, 5))
+        want = oracle.run(model, st, steps, types=types, seed=seed, t0=t0, force_x=fx,
+                          force_p=p if fx >= 0 else 0.0)
+        thr = oracle.prob_threshold(p) if fx >= 0 else 0
+        for path in ((1, 2) if W % 64 == 0 else (0,)):
+            got = run_emu(emu, tmp_path, model, st, types.astype(np.uint8), steps, seed, t0, fx,
+                          thr, path)
+            assert np.array_equal(got, want), (model, W, H, kind, fx, p, seed, t0, steps, path)
