@@ -920,10 +920,12 @@ int lgca_device_bytes(lgca_handle h, size_t *bytes)
 
 struct lgca_batch {
     std::vector<lgca_lattice *> members;
-    std::vector<cudaEvent_t> ev;  // one per member: its stream's work before the batch
+    // one per member: its stream's work before a call, recorded only when the
+    // member's stream was used since it last stepped
+    std::vector<cudaEvent_t> ev;
     int device = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr;
+    cudaEvent_t done = nullptr;  // end of the latest call; members' streams wait on it lazily
     int *s_base = nullptr;       // device: first batch-local step of a graph replay
     int graph_steps = 32;        // steps captured per CUDA graph (0: no graphs)
     int warp_tasks = 0;          // warp tasks per warp of the batched kernel (0: per call)
