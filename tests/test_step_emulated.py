@@ -114,7 +114,7 @@ def multistep_emu(tmp_path_factory):
         pytest.skip("g++ or the CUDA headers not available")
     exe = tmp_path_factory.mktemp("emu") / "multistep_emu"
     lib = os.path.join(cuda, "lib64")
-    subprocess.run([gxx, "-O2", "-std=c++20", "-Wno-attributes", "-I", os.path.join(cuda, "include"),
+    subprocess.run([gxx, "-O1", "-std=c++20", "-Wno-attributes", "-I", os.path.join(cuda, "include"),
                     os.path.join(ROOT, "tests", "multistep_emu.cpp"), "-o", str(exe), "-pthread",
                     "-L", lib, "-lcudart", f"-Wl,-rpath,{lib}"], check=True, capture_output=True)
     return exe
@@ -179,3 +179,61 @@ def test_emulated_step_bodies_random_configurations(emu, tmp_path, oracle):
             got = run_emu(emu, tmp_path, model, st, types.astype(np.uint8), steps, seed, t0, fx,
                           thr, path)
             assert np.array_equal(got, want), (model, W, H, kind, fx, p, seed, t0, steps, path)
+
+
+@pytest.fixture(scope="module")
+def batch_emu(tmp_path_factory):
+    gxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if gxx is None or not os.path.isdir(cuda_inc):
+        pytest.skip("g++ or the CUDA headers not available")
+    exe = tmp_path_factory.mktemp("emu") / "batch_emu"
+    # -O0: the kernel's many instantiations build in seconds; the small
+    # lattices here run as fast either way
+    subprocess.run([gxx, "-O0", "-std=c++20", "-Wno-attributes", "-I", cuda_inc,
+                    os.path.join(ROOT, "tests", "batch_emu.cpp"), "-o", str(exe), "-pthread"],
+                   check=True, capture_output=True)
+    return exe
+
+
+def test_emulated_batch_kernel_equals_oracle(batch_emu, tmp_path, oracle):
+    """k_batch_keys and k_batch on their grids, with the call's work-list:
+    random mixed batches (models, pair / odd / one-word widths, geometries
+    with cell-type noise, forcing, start steps, 0 to 6 steps per member so
+    members leave the work-list part way) at 1, 2, 4 and 8 tasks per warp;
+    every member equals its lone oracle run."""
+    rng = np.random.default_rng(77)
+    for trial in range(16):
+        wt = (1, 2, 4, 8)[trial % 4]
+        mem = []
+        for _ in range(int(rng.integers(1, 10))):
+            model = int(rng.integers(4))
+            W = 64 * int(rng.integers(1, 10)) if rng.random() < 0.7 else int(rng.integers(1, 400))
+            H = 2 * int(rng.integers(1, 24))
+            kind = int(rng.integers(4))
+            types = [G.periodic(W, H), G.pipe(W, H), G.reflecting(W, H, "forward"),
+                     rng.choice([0, 0, 0, 1, 2], size=(H, W))][kind]
+            types = np.ascontiguousarray(types, dtype=np.int32)
+            st = oracle.init_bernoulli(model, W, H, types, seed=int(rng.integers(1000)),
+                                       p_move=0.3, p_rest=0.3)
+            fx = int(rng.integers(W)) if rng.random() < 0.6 else -1
+            p = float(rng.uniform(0.05, 1.0))
+            mem.append((model, W, H, int(rng.integers(0, 7)), fx, int(rng.integers(1 << 40)),
+                        int(rng.integers(1 << 20)), p, st, types))
+        inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+        with open(inp, "wb") as f:
+            f.write(struct.pack("<2i", len(mem), wt))
+            for model, W, H, n, fx, seed, t0, p, st, types in mem:
+                thr = oracle.prob_threshold(p) if fx >= 0 else 0
+                f.write(struct.pack("<5i3Q", model, W, H, n, fx, seed, t0, thr))
+                f.write(st.tobytes())
+                f.write(types.astype(np.uint8).tobytes())
+        r = subprocess.run([str(batch_emu), str(inp), str(out)], capture_output=True)
+        assert r.returncode == 0, r.returncode
+        data, off = out.read_bytes(), 0
+        for model, W, H, n, fx, seed, t0, p, st, types in mem:
+            got = np.frombuffer(data[off:off + W * H], np.uint8).reshape(H, W)
+            off += W * H
+            want = oracle.run(model, st, n, types=types, seed=seed, t0=t0, force_x=fx,
+                              force_p=p if fx >= 0 else 0.0)
+            assert np.array_equal(got, want), (trial, wt, model, W, H, n, fx)
