@@ -141,8 +141,10 @@ static cudaError_t launch_model(int gm, const StepArgs &args, cudaStream_t st)
 
 __device__ __forceinline__ uint64_t globaltimer_ns()
 {
-    uint64_t t;
+    uint64_t t = 0;
+#ifdef __CUDA_ARCH__  // (host builds of the kernel bodies for the CPU emulation read 0)
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+#endif
     return t;
 }
 

@@ -1,21 +1,23 @@
-// Host emulation of the CUDA step bodies (lgca_gb300/csrc/step_body.cuh) for
-// CPU parity checks of the kernel code itself.  The step bodies are compiled
-// here as plain C++ by g++; each warp is 32 host threads running in lockstep,
-// and a warp shuffle is an exchange through a shared array between two
-// barrier waits.  The lane mapping is the one-step kernels' (flat_site), with
-// the two-words-per-lane body where the width is a multiple of 64 (WRAP as
-// in the batch kernel, or plain as in k_step2) and the one-word body
-// elsewhere.  tests/test_step_emulated.py compares the result with the
-// oracle.
+// Host emulation of the CUDA one-step kernels for CPU parity checks of the
+// kernel code itself.  lgca_gb300/csrc/step.cu (with the step bodies of
+// step_body.cuh) is compiled here as plain C++ by g++; each warp is 32 host
+// threads running in lockstep, and a warp shuffle is an exchange through a
+// shared array between two barrier waits.  Paths: the step bodies under the
+// one-step kernels' lane mapping (flat_site) -- the one-word body, the
+// two-words-per-lane body, and that body with the batch kernel's seam
+// shuffles (WRAP) -- and the kernels k_step2 and k_step themselves on their
+// grids (blocks of 4 warps).  tests/test_step_emulated.py compares the
+// result with the oracle.
 //
 //   step_emu IN OUT
-//   IN:  int32 model, W, H, steps, force_x, path (0 one word, 1 pair,
-//        2 pair with WRAP); uint64 seed, t0, force_thr; H*W uint8 cells
-//        (bit d = channel d); H*W uint8 cell types (0 fluid, 1 no-slip,
-//        2 slip)
+//   IN:  int32 model, W, H, steps, force_x, path (0 one-word body, 1 pair
+//        body, 2 pair body with WRAP, 3 kernel k_step2, 4 kernel k_step);
+//        uint64 seed, t0, force_thr; H*W uint8 cells (bit d = channel d);
+//        H*W uint8 cell types (0 fluid, 1 no-slip, 2 slip)
 //   OUT: H*W uint8 cells after `steps` steps
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include <barrier>
@@ -64,8 +66,26 @@ inline uint32_t __shfl_down_sync(unsigned, uint32_t v, unsigned delta, int width
 }
 template <class T> inline T __ldcg(const T *p) { return *p; }
 template <class T> inline T __ldg(const T *p) { return *p; }
+// grid coordinates of the emulated thread
+thread_local uint3 threadIdx;
+thread_local uint3 blockIdx;
+thread_local dim3 blockDim;
+thread_local dim3 gridDim;
+// used only by the persistent band kernel of step.cu, which is compiled here
+// but not run
+inline void __syncthreads() { std::abort(); }
+inline void __nanosleep(unsigned) { std::abort(); }
+inline void __threadfence() { std::abort(); }
+inline int atomicExch(int *, int) { std::abort(); }
+// kernel qualifiers with no host meaning
+#ifndef __launch_bounds__
+#define __launch_bounds__(...)
+#endif
+#ifndef __grid_constant__
+#define __grid_constant__
+#endif
 
-#include "../lgca_gb300/csrc/step_body.cuh"
+#include "../lgca_gb300/csrc/step.cu"
 
 using namespace lgca_gpu;
 
@@ -101,11 +121,51 @@ static void run_steps(StepArgs a, uint64_t *buf0, uint64_t *buf1, uint64_t seed,
     for (auto &x : th) x.join();
 }
 
+// the kernels k_step2 (PATH 3) and k_step (PATH 4) on grids of 4-warp blocks
+template <int MODEL, int GM, int PATH, bool ODD>
+static void run_kernel(StepArgs a, uint64_t *buf0, uint64_t *buf1, uint64_t seed, uint64_t t0,
+                       int steps)
+{
+    constexpr int WARPS = 4;
+    const int items = PATH == 4 ? a.g.nw : (a.g.nw + 1) / 2;
+    const long long tasks = flat_tasks(a.g.H, items);
+    const long long blocks = (tasks + WARPS - 1) / WARPS;
+    a.fmagic = flat_magic(a.g.H, items);
+    std::vector<emu::Warp> warps(WARPS);
+    std::barrier<> done(32 * WARPS);
+    std::vector<std::thread> th;
+    for (int i = 0; i < 32 * WARPS; ++i)
+        th.emplace_back([&, i] {
+            threadIdx = make_uint3((unsigned)(i & 31), (unsigned)(i >> 5), 0);
+            blockDim = dim3(32, WARPS, 1);
+            emu::lane = i & 31;
+            emu::warp = &warps[i >> 5];
+            for (int s = 0; s < steps; ++s) {
+                StepArgs as = a;
+                const uint64_t t = t0 + (uint64_t)s;
+                as.src = (s & 1) ? buf1 : buf0;
+                as.dst = (s & 1) ? buf0 : buf1;
+                as.chir_key = lgca_rng_key(seed, LGCA_STREAM_CHIR, t);
+                as.force_key = lgca_rng_key(seed, LGCA_STREAM_FORCE, t);
+                for (long long b = 0; b < blocks; ++b) {
+                    blockIdx = make_uint3((unsigned)b, 0, 0);
+                    if (PATH == 3) k_step2<MODEL, GM, ODD>(as);
+                    else k_step<MODEL, GM>(as);
+                    done.arrive_and_wait();  // blocks in turn, steps in order
+                }
+            }
+        });
+    for (auto &x : th) x.join();
+}
+
 template <int MODEL, int GM>
 static bool dispatch_path(int path, bool odd, StepArgs a, uint64_t *b0, uint64_t *b1,
                           uint64_t seed, uint64_t t0, int steps)
 {
-    if (path == 0) run_steps<MODEL, GM, 0, false>(a, b0, b1, seed, t0, steps);
+    if (path == 3 && odd) run_kernel<MODEL, GM, 3, true>(a, b0, b1, seed, t0, steps);
+    else if (path == 3) run_kernel<MODEL, GM, 3, false>(a, b0, b1, seed, t0, steps);
+    else if (path == 4) run_kernel<MODEL, GM, 4, false>(a, b0, b1, seed, t0, steps);
+    else if (path == 0) run_steps<MODEL, GM, 0, false>(a, b0, b1, seed, t0, steps);
     else if (path == 1 && odd) run_steps<MODEL, GM, 1, true>(a, b0, b1, seed, t0, steps);
     else if (path == 1) run_steps<MODEL, GM, 1, false>(a, b0, b1, seed, t0, steps);
     else if (odd) run_steps<MODEL, GM, 2, true>(a, b0, b1, seed, t0, steps);
@@ -141,7 +201,7 @@ int main(int argc, char **argv)
         std::fread(types.data(), 1, types.size(), f) != types.size())
         return 2;
     std::fclose(f);
-    if (path != 0 && W % 64 != 0) return 3;
+    if ((path == 1 || path == 2 || path == 3) && W % 64 != 0) return 3;
 
     const int D = num_dir(model);
     PlaneGeom g{};
@@ -174,7 +234,7 @@ int main(int argc, char **argv)
     a.chunks = (g.nw + 31) / 32;
     a.force_thr = fx >= 0 ? thr : 0;
     a.fx = fx;
-    a.wpt = path == 0 ? 1 : 2;
+    a.wpt = (path == 0 || path == 4) ? 1 : 2;
     const bool odd = (g.nw & 1) != 0;
     if (model == 0) dispatch_geom<M_HPP>(gm, path, odd, a, b0.data(), b1.data(), seed, t0, steps);
     else if (model == 1) dispatch_geom<M_FHP_I>(gm, path, odd, a, b0.data(), b1.data(), seed, t0, steps);
