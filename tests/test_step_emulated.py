@@ -263,3 +263,33 @@ def test_emulated_batch_kernel_equals_oracle(batch_emu, tmp_path, oracle):
             want = oracle.run(model, st, n, types=types, seed=seed, t0=t0, force_x=fx,
                               force_p=p if fx >= 0 else 0.0)
             assert np.array_equal(got, want), (trial, wt, model, W, H, n, fx)
+
+
+def test_emulated_block_sums_equal_oracle(tmp_path, oracle):
+    """The integer block-sum kernels (block_sums.cuh) on their grids: B
+    dividing 64 (one thread per block row and word), B = 64·2^k (shuffle
+    reduction) and any other B (one thread per block), ragged edges."""
+    gxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if gxx is None or not os.path.isdir(cuda_inc):
+        pytest.skip("g++ or the CUDA headers not available")
+    exe = tmp_path / "block_sums_emu"
+    subprocess.run([gxx, "-O1", "-std=c++20", "-Wno-attributes", "-I", cuda_inc,
+                    os.path.join(ROOT, "tests", "block_sums_emu.cpp"), "-o", str(exe), "-pthread"],
+                   check=True, capture_output=True)
+    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+    for model in (0, 1, 3):
+        for W, H in [(64, 16), (100, 30), (640, 40), (4160, 6)]:
+            st = oracle.init_bernoulli(model, W, H, G.periodic(W, H), seed=5, p_move=0.4,
+                                       p_rest=0.3)
+            for B in (8, 16, 32, 64, 128, 2048, 7, 48):
+                with open(inp, "wb") as f:
+                    f.write(struct.pack("<4i", model, W, H, B))
+                    f.write(st.tobytes())
+                r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True)
+                assert r.returncode == 0, (model, W, H, B)
+                Hb, Wb = -(-H // B), -(-W // B)
+                got = np.frombuffer(out.read_bytes(), np.int32).reshape(3, Hb, Wb)
+                want = oracle.block_sums(model, st, B)
+                for i in range(3):
+                    assert np.array_equal(got[i], want[i]), (model, W, H, B, i)
