@@ -148,7 +148,7 @@ int lgca_set_temporal_depth(lgca_handle h, int depth);
  * memory tiles (several steps per pass), 4 = persistent (all steps of a call
  * in one cooperative launch; each block owns a band of rows and waits, with a
  * bounded wait, only for its two neighbour bands between steps; a wait that
- * times out makes lgca_sync return LGCA_ERR_TIMEOUT),
+ * times out marks the handle failed: see lgca_clear_error),
  * 5 = one step per pass with two words per lane where dim_x is a multiple of
  * 128 (variant 1 keeps one word per lane).  Results do not depend on it.
  * No reference counterpart (a scheduling choice of this engine). */
@@ -228,8 +228,26 @@ int lgca_apply_body_force_noalloc(int model, int dim_x, int dim_y, uint64_t *pla
                                   const uint64_t *slip, uint64_t seed, uint64_t call, int forcing,
                                   int bf_dir, unsigned long long *reverted, void *stream);
 
-/* Wait for all work of the handle. */
+/* Wait for all work of the handle.  Returns LGCA_ERR_TIMEOUT while the
+ * handle is marked failed (below). */
 int lgca_sync(lgca_handle h);
+
+/* Bounded waits of the persistent kernel (variant 4).  A neighbour wait that
+ * runs past the handle's wait limit (lgca_set_wait_limit, 1 us .. 60 s,
+ * default 2 s) makes the kernel stop early and marks the handle failed: its
+ * step counter has advanced but its state is partly stepped.  From then on
+ * every call that waits for the handle's stream (lgca_sync, downloads,
+ * counts, sums, post-processing, checkpoints) returns LGCA_ERR_TIMEOUT, and
+ * later persistent launches return at once without stepping, until
+ * lgca_clear_error(h).  After clearing, load a state (lgca_upload_state or
+ * lgca_checkpoint_load) before stepping on.
+ * lgca_test_withhold_progress(h, b) is a test hook: block b (-1: none) of
+ * the handle's persistent launches never publishes its progress, so its
+ * neighbours' waits run out after the wait limit (every wait still ends).
+ * No reference counterpart (the reference has no device-side waits). */
+int lgca_clear_error(lgca_handle h);
+int lgca_set_wait_limit(lgca_handle h, uint64_t wait_ns);
+int lgca_test_withhold_progress(lgca_handle h, int block);
 
 /* The cudaStream_t the handle enqueues on (as void*), and a way to replace
  * it by a caller-owned stream (NULL restores the handle's own stream).

@@ -83,6 +83,9 @@ def lib() -> C.CDLL:
             "lgca_block_sums_async": (C.c_int, [vp, C.c_int, vp, vp, vp]),
             "lgca_post_process": (C.c_int, [vp, C.c_int, vp, vp, vp, vp]),
             "lgca_sync": (C.c_int, [vp]),
+            "lgca_clear_error": (C.c_int, [vp]),
+            "lgca_set_wait_limit": (C.c_int, [vp, u64]),
+            "lgca_test_withhold_progress": (C.c_int, [vp, C.c_int]),
             "lgca_stream": (vp, [vp]),
             "lgca_set_stream": (C.c_int, [vp, vp]),
             "lgca_state_device": (C.c_int, [vp, C.POINTER(vp), C.POINTER(C.c_size_t),
@@ -317,6 +320,18 @@ class GpuLattice:
 
     def sync(self) -> None:
         _check(self._h, lib().lgca_sync(self._h))
+
+    def clear_error(self) -> None:
+        """Acknowledge a persistent-kernel timeout (the state must then be reloaded)."""
+        _check(self._h, lib().lgca_clear_error(self._h))
+
+    def set_wait_limit(self, wait_ns: int) -> None:
+        """Limit of one neighbour wait of the persistent kernel, in nanoseconds."""
+        _check(self._h, lib().lgca_set_wait_limit(self._h, int(wait_ns)))
+
+    def test_withhold_progress(self, block: int) -> None:
+        """Test hook: block `block` of persistent launches never publishes its step."""
+        _check(self._h, lib().lgca_test_withhold_progress(self._h, int(block)))
 
     def stream_ptr(self) -> int:
         return lib().lgca_stream(self._h) or 0

@@ -148,13 +148,20 @@ bool wave_supported(int model, const PlaneGeom &g, int depth);
 
 // Persistent band form (step.cu): nsteps steps in one cooperative launch,
 // buf0 holding the input; the result is in buf0 if nsteps is even, else in
-// buf1.  `flags` holds one int per block (at most max_blocks) and, like
-// *err, must be zero before the launch; *err != 0 afterwards means a bounded
-// neighbour wait gave up.
+// buf1.  `flags` holds one int per block (at most max_blocks) and must be
+// zero before the launch.  *err != 0 afterwards means a bounded neighbour
+// wait gave up; it is never cleared by the kernel, and a launch that finds it
+// set returns at once.  Each neighbour wait gives up after w.wait_ns (> 0)
+// nanoseconds; block w.withhold (-1: none) never publishes its progress (a
+// test hook that makes its neighbours' waits run out).
 static constexpr int PERSIST_MAX_BLOCKS = 1024;
+struct PersistWait {
+    uint64_t wait_ns;
+    int withhold;
+};
 cudaError_t launch_persistent(int model, int geom_mode, const StepArgs &a, uint64_t *buf0,
                               uint64_t *buf1, uint64_t seed, uint64_t t0, int nsteps, int *flags,
-                              int *err, int max_blocks, cudaStream_t stream);
+                              int *err, int max_blocks, const PersistWait &w, cudaStream_t stream);
 
 // Kernel families selectable per handle.
 enum : int {

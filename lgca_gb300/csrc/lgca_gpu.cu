@@ -38,8 +38,14 @@ struct lgca_lattice {
     cudaStream_t own_stream = nullptr, stream = nullptr;
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
-    int *sync = nullptr;          // persistent kernel: error flag + one step flag per block
-    int *sync_err_host = nullptr; // pinned copy of the error flag, checked at sync points
+    // persistent kernel: sync[0] = error flag (sticky: set when a bounded
+    // neighbour wait gave up, cleared only by lgca_clear_error), then one step
+    // flag per block; sync_err_host is its pinned copy, refreshed after each
+    // persistent call and checked by every call that waits for the stream
+    int *sync = nullptr;
+    int *sync_err_host = nullptr;
+    uint64_t wait_ns = 2000000000ull;  // limit of one neighbour wait
+    int withhold = -1;                 // test hook: block that never publishes its step
     size_t bytes = 0;
     lgca_batch *batch = nullptr;  // the batch this lattice belongs to, if any
     // Ordering against batch calls without stream calls per member and call:
@@ -182,6 +188,25 @@ int geom_mode(const lgca_lattice *h)
 }
 
 bool valid(lgca_handle h) { return h != nullptr && h->buf[0] != nullptr; }
+
+// Wait for the handle's stream, then report a persistent-kernel timeout that
+// has not been cleared: the state the stream produced is then not the state
+// of the handle's step counter.
+int synced(lgca_lattice *h)
+{
+    const cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamSynchronize");
+    if (h->sync_err_host && *h->sync_err_host)
+        return fail(h, LGCA_ERR_TIMEOUT,
+                    "a neighbour wait of the persistent kernel timed out; the state is partly "
+                    "stepped until lgca_clear_error and a new state");
+    return LGCA_OK;
+}
+
+#define SYNC(h)                                        \
+    do {                                               \
+        if (const int s_ = synced(h)) return s_;       \
+    } while (0)
 
 // Called before the handle's stream is used: the stream waits for the batch
 // steps queued for the lattice (once per batch call), and is marked used.
@@ -363,7 +388,7 @@ int lgca_set_cell_types(lgca_handle h, const int32_t *types)
     CK(h, cudaMemsetAsync(bad, 0, sizeof(int), h->stream));
     CK(h, launch_types_to_planes(g, static_cast<const int32_t *>(h->scratch), h->solid, h->slip, bad,
                                  h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
+    SYNC(h);
     h->has_noslip = any_noslip;
     h->has_slip = any_slip;
     return LGCA_OK;
@@ -407,7 +432,7 @@ int lgca_get_cell_types(lgca_handle h, int32_t *types)
     if (st) return st;
     CK(h, launch_planes_to_types(h->g, h->solid, h->slip, static_cast<int32_t *>(h->scratch), h->stream));
     CK(h, cudaMemcpyAsync(types, h->scratch, n * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
+    SYNC(h);
     return LGCA_OK;
 }
 
@@ -436,7 +461,7 @@ int lgca_download_state(lgca_handle h, uint8_t *cells)
     CK(h, launch_planes_to_aos(h->D, h->g, h->buf[h->cur], static_cast<uint8_t *>(h->scratch),
                                h->stream));
     CK(h, cudaMemcpyAsync(cells, h->scratch, n, cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
+    SYNC(h);
     return LGCA_OK;
 }
 
@@ -556,14 +581,16 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     if (h->variant == VARIANT_PERSIST && nsteps > 1) {
         const size_t sync_bytes = (size_t)(PERSIST_MAX_BLOCKS + 1) * sizeof(int);
         if (!h->sync) {
-            int sst = dalloc(h, reinterpret_cast<void **>(&h->sync), sync_bytes, false, "flags");
+            int sst = dalloc(h, reinterpret_cast<void **>(&h->sync), sync_bytes, true, "flags");
             if (sst) return sst;
             CK(h, cudaHostAlloc(&h->sync_err_host, sizeof(int), cudaHostAllocDefault));
             *h->sync_err_host = 0;
         }
-        CK(h, cudaMemsetAsync(h->sync, 0, sync_bytes, h->stream));
+        // step flags start at zero; the error flag keeps an earlier timeout
+        CK(h, cudaMemsetAsync(h->sync + 1, 0, sync_bytes - sizeof(int), h->stream));
+        const PersistWait w{h->wait_ns, h->withhold};
         CK(h, launch_persistent(h->model, gm, a, h->buf[h->cur], h->buf[h->cur ^ 1], h->seed, h->t,
-                                nsteps, h->sync + 1, h->sync, PERSIST_MAX_BLOCKS, h->stream));
+                                nsteps, h->sync + 1, h->sync, PERSIST_MAX_BLOCKS, w, h->stream));
         CK(h, cudaMemcpyAsync(h->sync_err_host, h->sync, sizeof(int), cudaMemcpyDeviceToHost,
                               h->stream));
         if (nsteps & 1) h->cur ^= 1;
@@ -628,7 +655,7 @@ int lgca_apply_body_force(lgca_handle h, int forcing, int bf_dir, uint64_t *reve
     if (reverted) {
         unsigned long long v = 0;
         CK(h, cudaMemcpyAsync(&v, rev, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
-        CK(h, cudaStreamSynchronize(h->stream));
+        SYNC(h);
         *reverted = v;
     }
     return LGCA_OK;
@@ -646,7 +673,7 @@ int lgca_count_particles(lgca_handle h, uint64_t *n)
     CK(h, launch_count(h->D, h->g, h->buf[h->cur], d, h->stream));
     unsigned long long v = 0;
     CK(h, cudaMemcpyAsync(&v, d, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
+    SYNC(h);
     *n = v;
     return LGCA_OK;
 }
@@ -665,7 +692,7 @@ int lgca_mean_velocity(lgca_handle h, float *ux, float *uy)
                                h->has_slip ? h->slip : nullptr, ds, nf, h->stream));
     struct { double s[2]; unsigned long long n; } v;
     CK(h, cudaMemcpyAsync(&v, ds, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
+    SYNC(h);
     *ux = (float)(v.s[0] / (double)v.n);
     *uy = (float)(v.s[1] / (double)v.n);
     return LGCA_OK;
@@ -693,7 +720,7 @@ int lgca_block_sums(lgca_handle h, int B, int32_t *N, int32_t *Jx2, int32_t *Jy)
     CK(h, cudaMemcpyAsync(N, d, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaMemcpyAsync(Jx2, d + nb, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaMemcpyAsync(Jy, d + 2 * nb, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
+    SYNC(h);
     return LGCA_OK;
 }
 
@@ -741,7 +768,7 @@ int lgca_post_process(lgca_handle h, int r, float *cell_density, float *cell_mom
     if (dcm) CK(h, cudaMemcpyAsync(cell_momentum, dcm, 2 * n * 4, cudaMemcpyDeviceToHost, h->stream));
     if (dmd && nc) CK(h, cudaMemcpyAsync(mean_density, dmd, nc * 4, cudaMemcpyDeviceToHost, h->stream));
     if (dmm && nc) CK(h, cudaMemcpyAsync(mean_momentum, dmm, 2 * nc * 4, cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
+    SYNC(h);
     return LGCA_OK;
 }
 
@@ -749,11 +776,40 @@ int lgca_sync(lgca_handle h)
 {
     CHECK_HANDLE(h);
     DeviceGuard dg(h->device);
+    SYNC(h);
+    return LGCA_OK;
+}
+
+int lgca_clear_error(lgca_handle h)
+{
+    CHECK_HANDLE(h);
+    DeviceGuard dg(h->device);
     CK(h, cudaStreamSynchronize(h->stream));
-    if (h->sync_err_host && *h->sync_err_host) {
-        *h->sync_err_host = 0;
-        return fail(h, LGCA_ERR_TIMEOUT, "a neighbour wait of the persistent kernel timed out");
+    if (h->sync) {
+        CK(h, cudaMemsetAsync(h->sync, 0, sizeof(int), h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
     }
+    if (h->sync_err_host) *h->sync_err_host = 0;
+    h->err.clear();
+    return LGCA_OK;
+}
+
+int lgca_set_wait_limit(lgca_handle h, uint64_t wait_ns)
+{
+    CHECK_VALID(h);
+    if (wait_ns < 1000ull || wait_ns > 60000000000ull)
+        return fail(h, LGCA_ERR_INVALID, "wait limit %llu ns outside 1 us .. 60 s",
+                    (unsigned long long)wait_ns);
+    h->wait_ns = wait_ns;
+    return LGCA_OK;
+}
+
+int lgca_test_withhold_progress(lgca_handle h, int block)
+{
+    CHECK_VALID(h);
+    if (block < -1 || block >= PERSIST_MAX_BLOCKS)
+        return fail(h, LGCA_ERR_INVALID, "block %d outside -1 .. %d", block, PERSIST_MAX_BLOCKS - 1);
+    h->withhold = block;
     return LGCA_OK;
 }
 
@@ -769,7 +825,7 @@ int lgca_set_stream(lgca_handle h, void *stream)
 {
     CHECK_HANDLE(h);
     DeviceGuard dg(h->device);
-    CK(h, cudaStreamSynchronize(h->stream));
+    SYNC(h);
     h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
     return LGCA_OK;
 }
@@ -850,7 +906,7 @@ int lgca_checkpoint_save(lgca_handle h, void *buf, size_t bytes)
         CK(h, copy_plane(h->slip));
     }
     if (h->frozen) CK(h, copy_plane(h->chir));
-    CK(h, cudaStreamSynchronize(h->stream));
+    SYNC(h);
     return LGCA_OK;
 }
 
@@ -864,7 +920,23 @@ int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes)
     if (hd.model != h->model || hd.dim_x != h->g.W || hd.dim_y != h->g.H)
         return fail(h, LGCA_ERR_INVALID, "checkpoint of model %d, %d x %d does not match the lattice",
                     hd.model, hd.dim_x, hd.dim_y);
+    // the settings pass the same checks as their setters before anything changes
+    if ((hd.flags & ~15) != 0) return fail(h, LGCA_ERR_INVALID, "checkpoint flags 0x%x invalid", hd.flags);
+    if (hd.variant < VARIANT_AUTO || hd.variant > VARIANT_PLAIN2)
+        return fail(h, LGCA_ERR_INVALID, "checkpoint kernel variant %d invalid", hd.variant);
+    if (hd.wpt != 1 && hd.wpt != 2)
+        return fail(h, LGCA_ERR_INVALID, "checkpoint words per lane %d invalid", hd.wpt);
+    if (hd.depth < 1 || hd.depth > 8)
+        return fail(h, LGCA_ERR_INVALID, "checkpoint temporal depth %d invalid", hd.depth);
+    const bool no_force = hd.force_x == -1 && hd.force_thr == 0;
+    const bool force_ok = hd.force_x >= 0 && hd.force_x < h->g.W && hd.force_thr >= 1 &&
+                          hd.force_thr <= (1ull << 32);
+    if (!no_force && !force_ok)
+        return fail(h, LGCA_ERR_INVALID, "checkpoint forcing column %d / threshold %llu invalid",
+                    hd.force_x, (unsigned long long)hd.force_thr);
     const bool has_geom = (hd.flags & 8) != 0, frozen = (hd.flags & 4) != 0;
+    if (!has_geom && (hd.flags & 3))
+        return fail(h, LGCA_ERR_INVALID, "checkpoint cell types without geometry planes");
     const size_t row = (size_t)h->g.nw * sizeof(uint64_t), pitch = (size_t)h->g.pitch * sizeof(uint64_t);
     const size_t plane = row * h->g.H;
     const size_t need = sizeof(CkptHeader) + ((size_t)h->D + (has_geom ? 2 : 0) + (frozen ? 1 : 0)) * plane;
@@ -892,7 +964,7 @@ int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes)
         CK(h, copy_plane(h->slip));
     }
     if (frozen) CK(h, copy_plane(h->chir));
-    CK(h, cudaStreamSynchronize(h->stream));
+    SYNC(h);
     h->has_noslip = has_geom && (hd.flags & 1);
     h->has_slip = has_geom && (hd.flags & 2);
     h->frozen = frozen;

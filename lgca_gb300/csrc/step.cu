@@ -136,8 +136,12 @@ static cudaError_t launch_model(int gm, const StepArgs &args, cudaStream_t st)
 // must not overwrite the previous-step rows those bands still read.  So
 // after each step a block publishes its step count and waits for its two
 // neighbours to reach the same count -- no grid-wide barrier.  The waits are
-// bounded: past PERSIST_WAIT_NS, or when another block reported a timeout, a
-// block records the error and stops; the host reports LGCA_ERR_TIMEOUT.
+// bounded: past wait_ns nanoseconds, or when another block reported a
+// timeout, a block records the error in *err and stops; the host reports
+// LGCA_ERR_TIMEOUT.  *err is sticky: a launch that finds it set does nothing,
+// so the steps queued behind a failed call do not run on a partial state.
+// `withhold` names a block that never publishes its step (-1: none), so that
+// a test can make its neighbours' waits run out; every wait still ends.
 
 __device__ __forceinline__ uint64_t globaltimer_ns()
 {
@@ -148,11 +152,10 @@ __device__ __forceinline__ uint64_t globaltimer_ns()
     return t;
 }
 
-static constexpr uint64_t PERSIST_WAIT_NS = 2000000000ull;
-
 template <int MODEL, int GM, int WPT>
 __global__ void k_band(const __grid_constant__ StepArgs a, uint64_t *buf0, uint64_t *buf1,
-                       uint64_t seed, uint64_t t0, int nsteps, int *flags, int *err)
+                       uint64_t seed, uint64_t t0, int nsteps, int *flags, int *err,
+                       uint64_t wait_ns, int withhold)
 {
     __shared__ uint64_t keys[2];
     __shared__ int stop;
@@ -166,9 +169,10 @@ __global__ void k_band(const __grid_constant__ StepArgs a, uint64_t *buf0, uint6
     if (leader) {
         keys[0] = lgca_rng_key(seed, LGCA_STREAM_CHIR, t0);
         keys[1] = lgca_rng_key(seed, LGCA_STREAM_FORCE, t0);
-        stop = 0;
+        stop = *(volatile int *)err;  // an earlier call gave up: do not step a partial state
     }
     __syncthreads();
+    if (stop) return;  // (block-uniform)
     for (int s = 0; s < nsteps; ++s) {
         const StepIO io{(s & 1) ? buf1 : buf0, (s & 1) ? buf0 : buf1, keys[0], keys[1]};
         for (int task = warp; task < tasks; task += nwarps) {
@@ -180,12 +184,12 @@ __global__ void k_band(const __grid_constant__ StepArgs a, uint64_t *buf0, uint6
         __syncthreads();  // the band's step s is written; keys[] no longer read
         if (leader) {
             __threadfence();
-            atomicExch(flags + b, s + 1);
+            if (b != withhold) atomicExch(flags + b, s + 1);
             volatile int *vf = flags;
             volatile int *verr = err;
             const uint64_t tw = globaltimer_ns();
             while (vf[bl] < s + 1 || vf[br] < s + 1) {
-                if (*verr || globaltimer_ns() - tw > PERSIST_WAIT_NS) {
+                if (*verr || globaltimer_ns() - tw > wait_ns) {
                     atomicExch(err, 1);
                     stop = 1;
                     break;
@@ -204,7 +208,7 @@ __global__ void k_band(const __grid_constant__ StepArgs a, uint64_t *buf0, uint6
 template <int MODEL, int GM, int WPT>
 static cudaError_t band_launch(const StepArgs &a, uint64_t *buf0, uint64_t *buf1, uint64_t seed,
                                uint64_t t0, int nsteps, int *flags, int *err, int max_blocks,
-                               cudaStream_t st)
+                               const PersistWait &w, cudaStream_t st)
 {
     auto kern = k_band<MODEL, GM, WPT>;
     int dev = 0, nsm = 0;
@@ -223,40 +227,45 @@ static cudaError_t band_launch(const StepArgs &a, uint64_t *buf0, uint64_t *buf1
     int blocks = nsm < a.g.H ? nsm : a.g.H;
     if (blocks > max_blocks) blocks = max_blocks;
     StepArgs aa = a;
-    void *args[] = {(void *)&aa, (void *)&buf0, (void *)&buf1, (void *)&seed, (void *)&t0,
-                    (void *)&nsteps, (void *)&flags, (void *)&err};
+    uint64_t wait_ns = w.wait_ns;
+    int withhold = w.withhold;
+    void *args[] = {(void *)&aa,    (void *)&buf0,  (void *)&buf1, (void *)&seed,
+                    (void *)&t0,    (void *)&nsteps, (void *)&flags, (void *)&err,
+                    (void *)&wait_ns, (void *)&withhold};
     return cudaLaunchCooperativeKernel((void *)kern, dim3(blocks), dim3(32, warps), args, 0, st);
 }
 
 template <int MODEL, int GM>
 static cudaError_t band_wpt(const StepArgs &a, uint64_t *b0, uint64_t *b1, uint64_t seed,
-                            uint64_t t0, int n, int *flags, int *err, int maxb, cudaStream_t st)
+                            uint64_t t0, int n, int *flags, int *err, int maxb, const PersistWait &w,
+                            cudaStream_t st)
 {
     if (a.wpt == 2 && (a.g.nw % 2) == 0 && (a.g.W % 64) == 0)  // band form: whole pairs
-        return band_launch<MODEL, GM, 2>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
-    return band_launch<MODEL, GM, 1>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
+        return band_launch<MODEL, GM, 2>(a, b0, b1, seed, t0, n, flags, err, maxb, w, st);
+    return band_launch<MODEL, GM, 1>(a, b0, b1, seed, t0, n, flags, err, maxb, w, st);
 }
 
 template <int MODEL>
 static cudaError_t band_model(int gm, const StepArgs &a, uint64_t *b0, uint64_t *b1,
                               uint64_t seed, uint64_t t0, int n, int *flags, int *err, int maxb,
-                              cudaStream_t st)
+                              const PersistWait &w, cudaStream_t st)
 {
     switch (gm) {
-    case GEOM_NONE: return band_wpt<MODEL, GEOM_NONE>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
-    case GEOM_NOSLIP: return band_wpt<MODEL, GEOM_NOSLIP>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
-    default: return band_wpt<MODEL, GEOM_FULL>(a, b0, b1, seed, t0, n, flags, err, maxb, st);
+    case GEOM_NONE: return band_wpt<MODEL, GEOM_NONE>(a, b0, b1, seed, t0, n, flags, err, maxb, w, st);
+    case GEOM_NOSLIP: return band_wpt<MODEL, GEOM_NOSLIP>(a, b0, b1, seed, t0, n, flags, err, maxb, w, st);
+    default: return band_wpt<MODEL, GEOM_FULL>(a, b0, b1, seed, t0, n, flags, err, maxb, w, st);
     }
 }
 
 cudaError_t launch_persistent(int model, int gm, const StepArgs &a, uint64_t *buf0, uint64_t *buf1,
                               uint64_t seed, uint64_t t0, int nsteps, int *flags, int *err,
-                              int max_blocks, cudaStream_t st)
+                              int max_blocks, const PersistWait &w, cudaStream_t st)
 {
+    if (w.wait_ns == 0) return cudaErrorInvalidValue;
     switch (model) {
-    case M_HPP: return band_model<M_HPP>(gm, a, buf0, buf1, seed, t0, nsteps, flags, err, max_blocks, st);
-    case M_FHP_I: return band_model<M_FHP_I>(gm, a, buf0, buf1, seed, t0, nsteps, flags, err, max_blocks, st);
-    default: return band_model<M_FHP_II>(gm, a, buf0, buf1, seed, t0, nsteps, flags, err, max_blocks, st);
+    case M_HPP: return band_model<M_HPP>(gm, a, buf0, buf1, seed, t0, nsteps, flags, err, max_blocks, w, st);
+    case M_FHP_I: return band_model<M_FHP_I>(gm, a, buf0, buf1, seed, t0, nsteps, flags, err, max_blocks, w, st);
+    default: return band_model<M_FHP_II>(gm, a, buf0, buf1, seed, t0, nsteps, flags, err, max_blocks, w, st);
     }
 }
 

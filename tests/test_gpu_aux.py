@@ -272,3 +272,57 @@ def test_paint_rejects_bad_arguments(gpu):
                 L.paint_cells(*args)
         L.paint_cells(gpu.SHAPE_RECT, gpu.FLUID, 0, 0, 64, 8)  # no planes yet: nothing to do
         assert not L.get_cell_types().any()
+
+
+def test_persistent_wait_timeout_marks_handle_failed_until_cleared(gpu, oracle):
+    """One block of the persistent kernel withholds its progress (test hook),
+    so its neighbours' bounded waits run out after the 1 ms limit.  Every call
+    that waits for the handle then reports LGCA_ERR_TIMEOUT, and persistent
+    calls queued behind the failure do not step, until lgca_clear_error; after
+    a state is reloaded the handle steps correctly again."""
+    model, W, H = 3, 512, 256
+    st = oracle.init_bernoulli(model, W, H, None, seed=4, p_move=0.3, p_rest=0.3)
+    with gpu.GpuLattice(model, W, H, seed=4) as L:
+        L.upload(st)
+        L.set_kernel_variant(4)
+        L.set_wait_limit(1_000_000)
+        L.test_withhold_progress(1)
+        L.collide_and_propagate(10)
+        for call in (L.sync, L.download, L.count_particles, lambda: L.block_sums(16), L.checkpoint):
+            with pytest.raises(gpu.LgcaError) as e:
+                call()
+            assert e.value.status == 4  # LGCA_ERR_TIMEOUT
+        L.test_withhold_progress(-1)
+        L.collide_and_propagate(10)  # a launch behind the failure returns without stepping
+        with pytest.raises(gpu.LgcaError) as e:
+            L.sync()
+        assert e.value.status == 4
+        L.clear_error()
+        L.sync()
+        L.upload(st)
+        L.set_step(0)
+        L.collide_and_propagate(10)
+        assert np.array_equal(L.download(), oracle.run(model, st, 10, seed=4))
+        with pytest.raises(gpu.LgcaError):
+            L.set_wait_limit(10)  # below 1 us
+
+
+def test_checkpoint_load_rejects_invalid_settings(gpu):
+    """A damaged checkpoint header is refused before anything changes."""
+    import struct
+    with gpu.GpuLattice(1, 128, 16, seed=3) as L:
+        L.init_random(0.3)
+        blob = bytearray(L.checkpoint())
+        want = L.download()
+        # header: magic[8], model, dim_x, dim_y, flags (int32), seed, step,
+        # fcall (uint64), force_x, depth (int32), force_thr (uint64), variant, wpt
+        offsets = {"flags": 20, "force_x": 48, "depth": 52, "variant": 64, "wpt": 68}
+        for field, bad in [("flags", 16), ("variant", 9), ("wpt", 3), ("depth", 0), ("depth", 9),
+                           ("force_x", 128), ("force_x", 5)]:
+            b = bytearray(blob)
+            struct.pack_into("<i", b, offsets[field], bad)
+            with pytest.raises(gpu.LgcaError):
+                L.restore(bytes(b))
+        assert np.array_equal(L.download(), want)
+        L.restore(bytes(blob))
+        assert np.array_equal(L.download(), want)

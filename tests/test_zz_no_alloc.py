@@ -40,12 +40,33 @@ def to_state(planes, W):
     return s
 
 
-def test_noalloc_body_force_equals_handle_path_on_two_calls(gpu):
+# (model, W, H, geometry, [(forcing, bf_dir) per call], device counter?)
+CASES = [
+    (3, 1000, 700, "karman", [(7000, "x"), (3000, "y")], True),
+    (0, 640, 480, "pipe", [(5000, "x"), (2000, None)], False),
+    (2, 333, 222, "disc", [(400, None), (900, "y")], True),
+    # a lattice of exactly LGCA_NOALLOC_MAX_CELLS cells: the work arrays reach
+    # the end of the fixed array, next to the count of the no-counter case
+    (1, 2048, 1024, "pipe", [(20000, "x"), (20000, "y")], False),
+    (3, 2048, 1024, "karman", [(30000, "y"), (10000, "x")], True),
+]
+
+
+def geometry(name, W, H):
+    if name == "karman":
+        return G.karman_reference(W, H)
+    if name == "pipe":
+        return G.pipe(W, H)
+    return G.disc(W, H, W // 3, H // 2, H // 5)
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"m{c[0]}_{c[1]}x{c[2]}_{c[3]}_{'dev' if c[5] else 'null'}")
+def test_noalloc_body_force_equals_handle_path_on_two_calls(gpu, case):
     torch = pytest.importorskip("torch")
-    model, W, H, seed = gpu.FHP_III, 1000, 700, 6
+    model, W, H, geom, calls, counter = case
+    seed = 6
     D = gpu.NUM_DIR[model]
-    types = G.karman_reference(W, H)
-    calls = [(7000, "x"), (3000, "y")]
+    types = geometry(geom, W, H)
 
     # the existing entry point on a handle: two calls in a row
     with gpu.GpuLattice(model, W, H, seed=seed) as L:
@@ -68,13 +89,15 @@ def test_noalloc_body_force_equals_handle_path_on_two_calls(gpu):
     for call, ((forcing, d), (want_state, want_n)) in enumerate(zip(calls, want)):
         st = lib.lgca_apply_body_force_noalloc(model, W, H, planes.data_ptr(), H * pitch, pitch,
                                                solid.data_ptr(), slip.data_ptr(), seed, call,
-                                               forcing, ord(d), rev.data_ptr(),
+                                               forcing, ord(d) if d else 0,
+                                               rev.data_ptr() if counter else None,
                                                C.c_void_p(stream.cuda_stream))
         assert st == 0, lib.lgca_last_error(None)
         torch.cuda.synchronize()
         got = to_state(planes.cpu().numpy().view(np.uint64), W)
         assert np.array_equal(got, want_state), call
-        assert int(rev.item()) == want_n
+        if counter:
+            assert int(rev.item()) == want_n
 
 
 def test_noalloc_rejects_lattices_above_its_limit(gpu):
