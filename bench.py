@@ -215,6 +215,48 @@ def gate_measurement(gpu, torch, hbm_peak):
             "bytes_per_launch": bytes_step, "traffic": profiled_traffic("step_fhp3_32768x16384.md")}
 
 
+def oracle_check(final_sha):
+    """Compare the batched run's final states with the committed hashes of
+    the same 512 jobs stepped one by one by the CPU oracle."""
+    path = os.path.join(ROOT, "tests", "golden", "batched_512.json")
+    try:
+        with open(path) as f:
+            want = json.load(f)["final_sha"]
+    except OSError:
+        return {"oracle_checked": 0}
+    same = sum(a == b for a, b in zip(final_sha, want))
+    return {"oracle_checked": min(len(final_sha), len(want)), "oracle_bit_exact": same,
+            "oracle_all_equal": same == len(want) == len(final_sha)}
+
+
+def served_leg(rate, duration):
+    """The served workload, bounded: Poisson arrivals at `rate` jobs/s for
+    `duration` s (sizes 256x256..8192x4096, 100..20000 steps, 16x16 fields
+    every 500 steps, 150 GB budget), a 10 s drain; FCFS single-lattice
+    execution of the same jobs from measured per-step times, and of the first
+    200 jobs run back to back on the GPU; 8 sampled jobs rerun alone with
+    every streamed field compared."""
+    from lgca_gb300 import serve as SV
+    r = SV.serve(rate, duration, budget=150e9, drain_limit=10.0, verify=8, fcfs=True,
+                 fcfs_sample=200)
+    fm = r.get("fcfs_measured", {})
+    return {"rate_jobs_s": rate, "duration_s": duration, "jobs": r["jobs"],
+            "completed": r["completed"], "backlog": r["backlog"], "elapsed_s": r["elapsed_s"],
+            "p50_s": r["p50_latency_s"], "p99_s": r["p99_latency_s"],
+            "sustained_gsite_updates_s": r["sustained_gsite_updates_s"],
+            "fcfs_p50_s": r["fcfs"]["p50_latency_s"], "fcfs_p99_s": r["fcfs"]["p99_latency_s"],
+            "fcfs_gsite_updates_s": r["fcfs"]["sustained_gsite_updates_s"],
+            "x_fcfs": r["throughput_speedup_vs_fcfs"],
+            "x_fcfs_best_repeat": r["throughput_speedup_vs_fcfs_best"],
+            "fcfs_measured_gsite_updates_s": fm.get("gsite_updates_s"),
+            "fcfs_measured_jobs": fm.get("jobs"),
+            "fcfs_table_gsite_updates_s_same_jobs": fm.get("table_gsite_updates_s"),
+            "x_fcfs_measured": r.get("throughput_speedup_vs_fcfs_measured"),
+            "sample_verified": r.get("sample_verified"),
+            "sample_bit_exact": r.get("sample_bit_exact"),
+            "evictions": r["evictions"], "batch_calls": r["batch_calls"]}
+
+
 def run_ours(args):
     import torch
     import lgca_gb300 as gpu
@@ -352,6 +394,10 @@ def run_ours(args):
         from lgca_gb300 import batched as BT
         batched = BT.compare(512, 1000, tune=True)
         batched.pop("tuned_words_per_lane", None)
+        batched.update(oracle_check(batched.pop("final_sha")))
+    served = None
+    if rank == 0 and not args.no_served:
+        served = served_leg(args.served_rate, args.served_duration)
     if rank == 0:
         cpu = cpu_baseline() if ws == 1 else None
         line = {
@@ -363,7 +409,7 @@ def run_ours(args):
                        "l2": "flushed between timed steps (256 MiB write, outside the events)",
                        "parallelism": f"replicas x{ws}"},
             "wall_s": t_wall, "e2e": e2e, "roofline": roofline, "roofline_gate": gate,
-            "batched": batched,
+            "batched": batched, "served": served,
             "cpu_baseline": cpu, "clocks": clk.summary(),
             "gpu_launches": (STEPS_PER_CHUNK + 1) * args.steps,
         }
@@ -380,6 +426,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 512-lattice batched vs one-at-a-time comparison")
+    ap.add_argument("--no-served", action="store_true", help="skip the served-form leg")
+    ap.add_argument("--served-rate", type=float, default=800.0)
+    ap.add_argument("--served-duration", type=float, default=20.0)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

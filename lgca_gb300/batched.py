@@ -105,7 +105,7 @@ def compare(n_jobs: int = 512, steps: int = 1000, tune: bool = True) -> dict:
             "batched_gsite_updates_s": sites * steps / tb / 1e9,
             "one_by_one_gsite_updates_s": sites * steps / ts / 1e9,
             "speedup": ts / tb, "bit_exact": hb == hs,
-            "tuned_words_per_lane": tuned}
+            "tuned_words_per_lane": tuned, "final_sha": hb}
 
 
 def main(argv=None):
@@ -115,7 +115,9 @@ def main(argv=None):
     ap.add_argument("--no-tune", action="store_true")
     a = ap.parse_args(argv)
     gpu.build()
-    print(json.dumps(compare(a.jobs, a.steps, not a.no_tune)))
+    r = compare(a.jobs, a.steps, not a.no_tune)
+    r.pop("final_sha")
+    print(json.dumps(r))
 
 
 if __name__ == "__main__":

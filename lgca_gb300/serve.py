@@ -22,12 +22,13 @@ tests substitute a CPU fake to exercise admission, budgets and failures.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import heapq
 import json
 import math
 import time
 from collections import deque
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 
@@ -55,6 +56,9 @@ class Job:
     bytes: int = 0
     ckpt: bytes | None = None  # state of an evicted job, restored on resume
     evictions: int = 0
+    # sampled jobs keep (step, hash of the fields) of every output they stream
+    record: bool = False
+    field_log: list = field(default_factory=list)
 
     @property
     def sites(self) -> int:
@@ -69,6 +73,14 @@ class Job:
         """Steps to the next output or the end."""
         to_out = out_every - (self.done_steps % out_every)
         return min(to_out, self.steps - self.done_steps)
+
+
+def fields_sha(fields) -> str:
+    """Hash of one streamed output: the N, Jx2, Jy block-sum arrays in order."""
+    h = hashlib.sha256()
+    for a in fields:
+        h.update(np.ascontiguousarray(a, dtype=np.int32).tobytes())
+    return h.hexdigest()
 
 
 def _round64(v: float) -> int:
@@ -367,6 +379,8 @@ class Server:
                 for (j, at), f in zip(emit, got):
                     j.last_fields = f
                     j.outputs += 1
+                    if j.record:
+                        j.field_log.append((at, fields_sha(f)))
                     if at == j.steps:
                         self._finish(j, now)
             inflight = launched
@@ -477,21 +491,73 @@ def build_alone(job: Job):
     return L
 
 
-def verify_sample(jobs, n: int = 8, block: int = 16, seed: int = 0) -> bool:
-    """Rerun a sample of completed jobs alone with the plain kernel: their
-    final fields must equal the served ones."""
+def mark_sample(jobs, n: int = 16, seed: int = 0, horizon: float = 0.5):
+    """Choose n jobs to verify before the run (so that every field they stream
+    is logged): drawn without replacement from the jobs that arrive in the
+    first `horizon` of the stream, which are the ones most likely to be
+    served within the run."""
+    if not jobs or n <= 0:
+        return []
+    t_end = max(j.arrival for j in jobs)
+    pool = [j for j in jobs if j.arrival <= horizon * t_end] or list(jobs)
     rng = np.random.default_rng(seed)
-    done = [j for j in jobs if j.finished is not None]
-    pick = [done[i] for i in rng.choice(len(done), size=min(n, len(done)), replace=False)]
-    ok = True
+    pick = [pool[i] for i in rng.choice(len(pool), size=min(n, len(pool)), replace=False)]
     for j in pick:
+        j.record = True
+    return pick
+
+
+def verify_sample(jobs, n: int = 8, block: int = 16) -> dict:
+    """Rerun up to n sampled jobs (marked before the run) alone through the
+    plain kernel in another code path (host cell map, one word per lane),
+    stopping at every step where the served job streamed fields: each of
+    those outputs, not only the last, must have the same block sums."""
+    sample = [j for j in jobs if j.record and j.field_log][:n]
+    fields = 0
+    ok = True
+    for j in sample:
         L = build_alone(j)
         L.set_kernel_variant(1)  # one word per lane: another code path than the batch's
-        L.collide_and_propagate(j.steps)
-        f = L.block_sums(block)
-        ok &= all(np.array_equal(a, b) for a, b in zip(f, j.last_fields))
+        done = 0
+        for at, want in j.field_log:
+            L.collide_and_propagate(at - done)
+            done = at
+            ok &= fields_sha(L.block_sums(block)) == want
+            fields += 1
         L.close()
-    return ok
+    return {"jobs": len(sample), "fields": fields, "bit_exact": bool(ok and sample)}
+
+
+def fcfs_measured(jobs, n: int = 200, block: int = 16, out_every: int = 500) -> dict:
+    """The first n jobs of the stream run first come, first served, one at a
+    time through the plain kernel on the GPU: each is created as the served
+    form creates it (device-painted geometry), stepped with its block sums
+    copied to the host every out_every steps and at its end, and destroyed.
+    Measures the service rate of FCFS execution directly (wall clock)."""
+    import lgca_gb300 as gpu
+    sel = sorted(jobs, key=lambda j: j.arrival)[:n]
+    t0 = time.perf_counter()
+    work = 0
+    for j in sel:
+        L = gpu.GpuLattice(j.model, j.W, j.H, seed=j.seed)
+        if j.geometry == "pipe":
+            L.apply_bc_pipe()
+            L.set_forcing_column(8, 0.01)
+        elif j.geometry == "disc":
+            L.paint_cells(gpu.SHAPE_DISC, gpu.SOLID_NO_SLIP, j.W // 8, j.H // 2, max(1, j.H // 16))
+        L.init_random(j.p, j.p)
+        L.set_kernel_variant(0)  # the plain kernel: one step per pass, its fastest form
+        done = 0
+        while done < j.steps:
+            k = min(out_every - done % out_every, j.steps - done)
+            L.collide_and_propagate(k)
+            done += k
+            L.block_sums(block)
+        work += j.steps * j.sites
+        L.close()
+    dt = time.perf_counter() - t0
+    return {"jobs": len(sel), "site_updates": work, "seconds": dt,
+            "gsite_updates_s": work / dt / 1e9 if dt else 0.0}
 
 
 # resident-site slots of the served runs: 2^30 sites keep a 100-step batch
@@ -502,8 +568,10 @@ SERVE_MAX_SITES = float(1 << 30)
 
 def serve(rate: float, duration: float, budget: float = 150e9, drain_limit: float = 60.0,
           verify: int = 8, fcfs: bool = True, max_sites: float = SERVE_MAX_SITES,
-          quantum: int = 100, policy: str = "fcfs", **job_kw) -> dict:
+          quantum: int = 100, policy: str = "fcfs", fcfs_sample: int = 0, **job_kw) -> dict:
     jobs = make_jobs(rate, duration, **job_kw)
+    if verify:
+        mark_sample(jobs, 2 * verify)
     backend = GpuBackend()
     srv = Server(backend, budget=budget, max_sites=max_sites, max_quantum=quantum, policy=policy)
     rep = srv.run(jobs, drain_limit=drain_limit)
@@ -522,8 +590,21 @@ def serve(rate: float, duration: float, budget: float = 150e9, drain_limit: floa
         rep["fcfs_best"] = best
         rep["throughput_speedup_vs_fcfs_best"] = (rep["sustained_gsite_updates_s"] /
                                                   best["sustained_gsite_updates_s"])
+    if fcfs and fcfs_sample:
+        # FCFS measured on the GPU for the first jobs, beside the table's
+        # prediction for the same jobs
+        meas = fcfs_measured(jobs, fcfs_sample)
+        sel = sorted(jobs, key=lambda j: j.arrival)[:fcfs_sample]
+        pred = sum(j.steps * table(j) for j in sel)
+        meas["table_predicted_seconds"] = pred
+        meas["table_gsite_updates_s"] = meas["site_updates"] / pred / 1e9 if pred else 0.0
+        rep["fcfs_measured"] = meas
+        rep["throughput_speedup_vs_fcfs_measured"] = (rep["sustained_gsite_updates_s"] /
+                                                      meas["gsite_updates_s"])
     if verify:
-        rep["sample_bit_exact"] = verify_sample(srv.done, verify)
+        v = verify_sample(jobs, verify)
+        rep["sample_verified"] = v
+        rep["sample_bit_exact"] = v["bit_exact"]
     return rep
 
 
@@ -538,6 +619,8 @@ def main(argv=None):
                     help="resident site caps to try (slots)")
     ap.add_argument("--quantum", type=int, default=100)
     ap.add_argument("--no-fcfs", action="store_true")
+    ap.add_argument("--fcfs-sample", type=int, default=0,
+                    help="also run the first N jobs FCFS on the GPU (measured, not simulated)")
     ap.add_argument("--policy", nargs="+", default=["fcfs"], choices=["fcfs", "srpt"],
                     help="admission order (srpt: least remaining work first, with eviction)")
     a = ap.parse_args(argv)
@@ -547,7 +630,8 @@ def main(argv=None):
         for cap in a.max_sites:
             for pol in a.policy:
                 print(json.dumps(serve(r, a.duration, a.budget_gb * 1e9, a.drain, a.verify,
-                                       not a.no_fcfs, cap, a.quantum, pol)), flush=True)
+                                       not a.no_fcfs, cap, a.quantum, pol, a.fcfs_sample)),
+                      flush=True)
 
 
 if __name__ == "__main__":

@@ -133,6 +133,24 @@ def test_srpt_evicts_and_resumes_without_losing_steps():
     assert rep_s["p50_latency_s"] < rep_f["p50_latency_s"]
 
 
+def test_sampled_jobs_log_every_output():
+    """Jobs marked before the run keep the hash of every field they stream,
+    in step order; unmarked jobs keep none."""
+    jobs = jobs_small(20, seed=9)
+    pick = S.mark_sample(jobs, 6, seed=3)
+    assert len(pick) == 6 and all(j.record for j in pick)
+    assert all(j.arrival <= 0.5 * max(x.arrival for x in jobs) for j in pick)
+    clock = FakeClock()
+    S.Server(FakeBackend(clock), budget=1e12, clock=clock, sleep=clock.sleep).run(jobs)
+    for j in jobs:
+        if j.record:
+            steps = [at for at, _ in j.field_log]
+            assert steps == sorted(steps) and steps[-1] == j.steps and len(steps) == j.outputs
+            assert all(h == S.fields_sha((at,)) for at, h in j.field_log)
+        else:
+            assert j.field_log == []
+
+
 def test_unknown_policy_is_rejected():
     with pytest.raises(ValueError):
         S.Server(FakeBackend(FakeClock()), policy="lifo")
@@ -234,13 +252,18 @@ def test_pipelined_backend_overlaps_and_gives_same_results():
 def test_short_served_stream_is_bit_exact(gpu):
     jobs = S.make_jobs(40.0, 1.5, rng_seed=11, w_range=(256, 1024), h_range=(256, 512),
                        steps_range=(100, 1500))
+    for j in jobs:
+        j.record = True  # log every streamed field
     backend = S.GpuBackend()
     srv = S.Server(backend, budget=20e9)
     rep = srv.run(jobs)
     backend.close()
     assert rep["completed"] == len(jobs)
-    assert all(j.outputs == -(-j.steps // 500) for j in jobs)
-    assert S.verify_sample(srv.done, n=len(srv.done))  # every job, rebuilt from a host map
+    assert all(j.outputs == -(-j.steps // 500) == len(j.field_log) for j in jobs)
+    # every job rebuilt from a host map, every one of its outputs compared
+    v = S.verify_sample(srv.done, n=len(srv.done))
+    assert v["bit_exact"] and v["jobs"] == len(jobs)
+    assert v["fields"] == sum(j.outputs for j in jobs)
 
 
 @pytest.mark.gpu
@@ -252,12 +275,16 @@ def test_evicted_and_resumed_jobs_are_bit_exact(gpu):
     # newcomers displace big residents while the stream arrives
     jobs = S.make_jobs(2000.0, 0.15, rng_seed=12, w_range=(256, 1024), h_range=(256, 512),
                        steps_range=(100, 3000))
+    for j in jobs:
+        j.record = True
     backend = S.GpuBackend()
     srv = S.Server(backend, budget=20e9, max_sites=1024 * 512, policy="srpt", preempt_ratio=0.5)
     rep = srv.run(jobs)
     backend.close()
     assert rep["completed"] == len(jobs) and srv.evictions > 0
-    assert S.verify_sample(srv.done, n=len(srv.done))
+    # the outputs streamed before and after each eviction, all compared
+    v = S.verify_sample(srv.done, n=len(srv.done))
+    assert v["bit_exact"] and v["fields"] == sum(j.outputs for j in jobs)
 
 
 @pytest.mark.gpu
