@@ -188,14 +188,91 @@ def gen_configs():
         json.dump(pins, f, indent=1)
 
 
+def blocksum_sha(N, Jx2, Jy) -> str:
+    """One hash over the three int32 block-sum arrays, in the order N, Jx2, Jy."""
+    return sha(np.stack([np.asarray(N, np.int32), np.asarray(Jx2, np.int32),
+                         np.asarray(Jy, np.int32)]))
+
+
+def gen_karman_long(engine: str = "ref", steps: int = 10000):
+    """The Karman workload over its whole run: FHP-III 8192x2048, disc r=128 at
+    (1024,1024), forcing column x=16 p=0.02, Bernoulli 0.3 seed 2.  Records the
+    hash of the 32x32 block sums every 100 steps and of the state every 1000
+    steps.  engine "ref" steps the reference OMP_Lattice (about 50 minutes on 8
+    cores), "port" the restatement (about 8 minutes)."""
+    import time
+    W, H = 8192, 2048
+    types = G.disc(W, H, 1024, 1024, 128)
+    st = O.init_bernoulli(O.FHP_III, W, H, types, seed=2, p_move=0.3, p_rest=0.3)
+    run = O.ref_run if engine == "ref" else O.run
+    out = dict(engine=engine, W=W, H=H, steps=steps, block=32, init_sha=sha(st),
+               blocksum_sha={}, blocksum_total=[], state_sha={})
+    s = st
+    t_start = time.time()
+    for t in range(0, steps, 100):
+        s = run(O.FHP_III, s, 100, types=types, seed=2, t0=t, force_x=16, force_p=0.02)
+        N, Jx2, Jy = O.block_sums(O.FHP_III, s, 32)
+        out["blocksum_sha"][str(t + 100)] = blocksum_sha(N, Jx2, Jy)
+        out["blocksum_total"].append([int(N.sum()), int(Jx2.sum()), int(Jy.sum())])
+        if (t + 100) % 1000 == 0:
+            out["state_sha"][str(t + 100)] = sha(s)
+        print(f"step {t + 100}: {time.time() - t_start:.0f} s", flush=True)
+    name = "config_karman_long.json" if engine == "ref" else "config_karman_long_port.json"
+    with open(os.path.join(HERE, name), "w") as f:
+        json.dump(out, f, indent=1)
+    return out
+
+
+def batched_job_types(job):
+    """Cell map of a batched-workload job, as lgca_gb300.batched.build paints it."""
+    W, H = job["W"], job["H"]
+    if job["geometry"] == "pipe":
+        return G.pipe(W, H)
+    if job["geometry"] == "disc":
+        return G.disc(W, H, W // 8, H // 2, max(1, H // 16), walls=False)
+    return G.periodic(W, H)
+
+
+def gen_batched(n_jobs: int = 512, steps: int = 1000):
+    """Final-state hashes of every job of the batched workload (512 lattices,
+    1000 steps each), stepped one by one through the restatement (pinned to
+    the reference by the other fixtures).  About an hour on 8 cores."""
+    import time
+    from lgca_gb300.batched import make_jobs
+    jobs = make_jobs(n_jobs)
+    out = dict(engine="port", steps=steps, jobs=jobs, init_sha=[], final_sha=[])
+    t_start = time.time()
+    for j in jobs:
+        types = batched_job_types(j)
+        st = O.init_bernoulli(j["model"], j["W"], j["H"], types, seed=j["seed"], p_move=j["p"],
+                              p_rest=j["p"])
+        pipe = j["geometry"] == "pipe"
+        fin = O.run(j["model"], st, steps, types=types, seed=j["seed"],
+                    force_x=8 if pipe else -1, force_p=0.01 if pipe else 0.0)
+        out["init_sha"].append(sha(st))
+        out["final_sha"].append(sha(fin))
+        print(f"job {j['index']} ({j['W']}x{j['H']}): {time.time() - t_start:.0f} s", flush=True)
+    with open(os.path.join(HERE, "batched_512.json"), "w") as f:
+        json.dump(out, f, indent=0)
+    return out
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--configs", action="store_true")
+    ap.add_argument("--batched", action="store_true")
+    ap.add_argument("--karman-long", choices=["ref", "port"])
     ap.add_argument("--mean-velocity", action="store_true")
     args = ap.parse_args()
     O.build(ref=True)
     if args.mean_velocity:
         print(json.dumps(mean_velocity_cases()))
+        sys.exit(0)
+    if args.karman_long:
+        gen_karman_long(args.karman_long)
+        sys.exit(0)
+    if args.batched:
+        gen_batched()
         sys.exit(0)
     gen_small()
     if args.configs:
