@@ -202,6 +202,9 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
         p[5] = n[5];
         if (D == 7) p[6] = n[6];
     }
+    // warps without wall or obstacle cells skip the boundary multiplexer (a
+    // vote of all lanes, before the inactive ones leave)
+    const bool walls = GM != GEOM_NONE && __any_sync(FULL, (solid | slip) != 0ull);
     if (!active) return;
 
     uint64_t c[7];
@@ -217,7 +220,7 @@ __device__ __forceinline__ void step_word(const StepArgs &a, const StepIO &io, c
     }
 
     uint64_t out[7];
-    if (GM == GEOM_NONE) {
+    if (GM == GEOM_NONE || !walls) {
 #pragma unroll
         for (int d = 0; d < D; ++d) out[d] = c[d];
     } else {
@@ -370,9 +373,11 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
     const int wx = (t == 0) ? g.W - 1 : 64 * w0 - 1;
     const int ex = (t == np - 1) ? 0 : 64 * w0 + 128;
 
-    // x-1 pull of the pair (v0, v1); `edge` is the word west of it, read by
-    // lanes with need_w (and forced there when it holds the forcing column)
-    auto shl = [&](uint64_t v0, uint64_t v1, uint64_t edge, bool fcol, int k) -> uint64_t {
+    // x-1 pull of the pair (v0, v1) into (r0, r1); `edge` is the word west of
+    // it, read by lanes with need_w (and forced there when it holds the
+    // forcing column).  One shuffle per pair: only the first word takes a bit
+    // from outside the pair.
+    auto shl = [&](uint64_t v0, uint64_t v1, uint64_t edge, bool fcol, uint64_t &r0, uint64_t &r1) {
         // a lane offers the high half of its last real word (v0 in a half pair)
         const uint32_t hi =
             WRAP ? __shfl_sync(FULL, (uint32_t)((half ? v0 : v1) >> 32), srcw, width)
@@ -382,10 +387,11 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
             in = edge >> 63;
             if (fcol && forcing && wx == a.fx) in |= force_flip_at<MODEL, GM, CG>(a, io, y);
         }
-        return k ? ((v1 << 1) | (v0 >> 63)) : ((v0 << 1) | in);
+        r0 = (v0 << 1) | in;
+        r1 = (v1 << 1) | (v0 >> 63);
     };
-    // x+1 pull of the pair; `edge` is the word east of it
-    auto shr = [&](uint64_t v0, uint64_t v1, uint64_t edge, bool fcol, int k) -> uint64_t {
+    // x+1 pull of the pair into (r0, r1); `edge` is the word east of it
+    auto shr = [&](uint64_t v0, uint64_t v1, uint64_t edge, bool fcol, uint64_t &r0, uint64_t &r1) {
         const uint32_t lo = WRAP ? __shfl_sync(FULL, (uint32_t)v0, srce, width)
                                  : __shfl_down_sync(FULL, (uint32_t)v0, 1, width);
         uint64_t in = lo & 1u;
@@ -393,34 +399,35 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
             in = edge & 1ull;
             if (fcol && forcing && ex == a.fx) in &= ~force_flip_at<MODEL, GM, CG>(a, io, y);
         }
-        return k ? ((v1 >> 1) | (in << 63)) : ((v0 >> 1) | ((half ? in : v1) << 63));
+        r0 = (v0 >> 1) | ((half ? in : v1) << 63);
+        r1 = (v1 >> 1) | (in << 63);
     };
     // pulled values of word k of the pair
     uint64_t q[2][7];
     if (MODEL == M_HPP) {
-        const uint64_t a0 = shl(n[0][0], n[1][0], eg[0], true, 0), a1 = shl(n[0][0], n[1][0], eg[0], true, 1);
-        const uint64_t b0 = shr(n[0][2], n[1][2], eg[1], true, 0), b1 = shr(n[0][2], n[1][2], eg[1], true, 1);
-        q[0][0] = a0; q[1][0] = a1; q[0][2] = b0; q[1][2] = b1;
+        shl(n[0][0], n[1][0], eg[0], true, q[0][0], q[1][0]);
+        shr(n[0][2], n[1][2], eg[1], true, q[0][2], q[1][2]);
         q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][3] = n[0][3]; q[1][3] = n[1][3];
     } else if (even) {  // warp-uniform (row mapping contract)
-        const uint64_t a0 = shl(n[0][0], n[1][0], eg[0], true, 0), a1 = shl(n[0][0], n[1][0], eg[0], true, 1);
-        const uint64_t c0 = shl(n[0][1], n[1][1], eg[1], false, 0), c1 = shl(n[0][1], n[1][1], eg[1], false, 1);
-        const uint64_t e0 = shl(n[0][5], n[1][5], eg[2], false, 0), e1 = shl(n[0][5], n[1][5], eg[2], false, 1);
-        const uint64_t b0 = shr(n[0][3], n[1][3], eg[3], true, 0), b1 = shr(n[0][3], n[1][3], eg[3], true, 1);
-        q[0][0] = a0; q[1][0] = a1; q[0][3] = b0; q[1][3] = b1;
-        q[0][1] = c0; q[1][1] = c1; q[0][5] = e0; q[1][5] = e1;
+        shl(n[0][0], n[1][0], eg[0], true, q[0][0], q[1][0]);
+        shl(n[0][1], n[1][1], eg[1], false, q[0][1], q[1][1]);
+        shl(n[0][5], n[1][5], eg[2], false, q[0][5], q[1][5]);
+        shr(n[0][3], n[1][3], eg[3], true, q[0][3], q[1][3]);
         q[0][2] = n[0][2]; q[1][2] = n[1][2]; q[0][4] = n[0][4]; q[1][4] = n[1][4];
         if (D == 7) { q[0][6] = n[0][6]; q[1][6] = n[1][6]; }
     } else {
-        const uint64_t a0 = shl(n[0][0], n[1][0], eg[0], true, 0), a1 = shl(n[0][0], n[1][0], eg[0], true, 1);
-        const uint64_t b0 = shr(n[0][3], n[1][3], eg[1], true, 0), b1 = shr(n[0][3], n[1][3], eg[1], true, 1);
-        const uint64_t c0 = shr(n[0][2], n[1][2], eg[2], false, 0), c1 = shr(n[0][2], n[1][2], eg[2], false, 1);
-        const uint64_t e0 = shr(n[0][4], n[1][4], eg[3], false, 0), e1 = shr(n[0][4], n[1][4], eg[3], false, 1);
-        q[0][0] = a0; q[1][0] = a1; q[0][3] = b0; q[1][3] = b1;
-        q[0][2] = c0; q[1][2] = c1; q[0][4] = e0; q[1][4] = e1;
+        shl(n[0][0], n[1][0], eg[0], true, q[0][0], q[1][0]);
+        shr(n[0][3], n[1][3], eg[1], true, q[0][3], q[1][3]);
+        shr(n[0][2], n[1][2], eg[2], false, q[0][2], q[1][2]);
+        shr(n[0][4], n[1][4], eg[3], false, q[0][4], q[1][4]);
         q[0][1] = n[0][1]; q[1][1] = n[1][1]; q[0][5] = n[0][5]; q[1][5] = n[1][5];
         if (D == 7) { q[0][6] = n[0][6]; q[1][6] = n[1][6]; }
     }
+    // whether any lane of the warp holds a wall or obstacle cell (a vote of
+    // all lanes, before the inactive ones leave): warps without one skip the
+    // boundary multiplexer
+    const bool walls = GM != GEOM_NONE &&
+                       __any_sync(FULL, (solid[0] | solid[1] | slip[0] | slip[1]) != 0ull);
     if (!active) return;
 
     const bool nsrow = (y == 0) || (y == g.H - 1);
@@ -439,7 +446,7 @@ __device__ __forceinline__ void step_pair(const StepArgs &a, const StepIO &io, c
         } else {
             collide<MODEL>(c, 0ull);
         }
-        if (GM == GEOM_NONE) {
+        if (GM == GEOM_NONE || !walls) {
 #pragma unroll
             for (int d = 0; d < D; ++d) out[k][d] = c[d];
         } else {

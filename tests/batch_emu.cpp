@@ -65,6 +65,16 @@ inline uint32_t __shfl_down_sync(unsigned, uint32_t v, unsigned delta, int width
     const int s = emu::lane + (int)delta;
     return emu::exchange(v, s >= base + width ? emu::lane : s);
 }
+// warp vote: every lane offers its predicate, each gets the OR of all
+inline int __any_sync(unsigned, int pred)
+{
+    emu::warp->v[emu::lane] = pred != 0;
+    emu::warp->bar.arrive_and_wait();
+    int any = 0;
+    for (int i = 0; i < 32; ++i) any |= (int)emu::warp->v[i];
+    emu::warp->bar.arrive_and_wait();
+    return any;
+}
 template <class T> inline T __ldcg(const T *p) { return *p; }
 template <class T> inline T __ldg(const T *p) { return *p; }
 #ifndef __launch_bounds__

@@ -72,6 +72,16 @@ inline uint32_t __shfl_down_sync(unsigned, uint32_t v, unsigned delta, int width
 }
 inline void __syncthreads() { emu::block->bar.arrive_and_wait(); }
 inline int __ffsll(long long x) { return __builtin_ffsll(x); }
+// warp vote: every lane offers its predicate, each gets the OR of all
+inline int __any_sync(unsigned, int pred)
+{
+    emu::warp->v[emu::lane] = pred != 0;
+    emu::warp->bar.arrive_and_wait();
+    int any = 0;
+    for (int i = 0; i < 32; ++i) any |= (int)emu::warp->v[i];
+    emu::warp->bar.arrive_and_wait();
+    return any;
+}
 template <class T> inline T __ldcg(const T *p) { return *p; }
 template <class T> inline T __ldg(const T *p) { return *p; }
 // the launchers in the included files are compiled but never called here
