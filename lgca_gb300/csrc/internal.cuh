@@ -208,13 +208,20 @@ cudaError_t launch_mean_velocity(int model, const PlaneGeom &g, const uint64_t *
                                  const uint64_t *solid, const uint64_t *slip, double *dsum,
                                  unsigned long long *nfluid, cudaStream_t s);
 
-// Random-cell body force (reference semantics).  scratch must hold
-// body_force_scratch_bytes(num_cells) bytes.
+// Random-cell body force (reference semantics), one cooperative launch.
+// scratch holds body_force_scratch_bytes(num_cells) bytes (a first-occurrence
+// table of one word per cell, then per-call state); `sticky` points to
+// BODY_FORCE_STICKY_BYTES bytes at a place that stays the same from call to
+// call for the same scratch, zero before the first call: it records how much
+// of the table is known to be all ones, so that calls need not clear it.
+// *reverted_dev receives the reversals (all ones if a grid barrier gave up,
+// which also sets *err_out when err_out is not null).
 size_t body_force_scratch_bytes(size_t num_cells);
+static constexpr size_t BODY_FORCE_STICKY_BYTES = 64;
 cudaError_t launch_body_force(int model, const PlaneGeom &g, uint64_t *planes,
                               const uint64_t *solid, const uint64_t *slip, uint64_t key,
-                              long long forcing, int bf_dir, void *scratch,
-                              unsigned long long *reverted_dev, cudaStream_t s);
+                              long long forcing, int bf_dir, void *scratch, void *sticky,
+                              unsigned long long *reverted_dev, int *err_out, cudaStream_t s);
 
 // Lane mapping of the one-step kernels: the lane items (words, or pairs of
 // words) of all even rows, then of all odd rows, are numbered row by row, and

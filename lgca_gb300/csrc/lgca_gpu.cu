@@ -38,6 +38,9 @@ struct lgca_lattice {
     cudaStream_t own_stream = nullptr, stream = nullptr;
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    // random-cell body force: its first-occurrence table (kept all ones
+    // between calls), per-call state, the table's clean mark and the count
+    void *bf = nullptr;
     // persistent kernel: sync[0] = error flag (sticky: set when a bounded
     // neighbour wait gave up, cleared only by lgca_clear_error), then one step
     // flag per block; sync_err_host is its pinned copy, refreshed after each
@@ -189,6 +192,20 @@ int geom_mode(const lgca_lattice *h)
 
 bool valid(lgca_handle h) { return h != nullptr && h->buf[0] != nullptr; }
 
+// The device error flag of bounded device waits (persistent kernel, body
+// force) and its pinned host copy, allocated at first use.
+int error_flag(lgca_lattice *h)
+{
+    if (h->sync) return LGCA_OK;
+    const size_t sync_bytes = (size_t)(PERSIST_MAX_BLOCKS + 1) * sizeof(int);
+    int st = dalloc(h, reinterpret_cast<void **>(&h->sync), sync_bytes, true, "flags");
+    if (st) return st;
+    const cudaError_t e = cudaHostAlloc(&h->sync_err_host, sizeof(int), cudaHostAllocDefault);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaHostAlloc");
+    *h->sync_err_host = 0;
+    return LGCA_OK;
+}
+
 // Wait for the handle's stream, then report a persistent-kernel timeout that
 // has not been cleared: the state the stream produced is then not the state
 // of the handle's step counter.
@@ -324,7 +341,7 @@ int lgca_destroy(lgca_handle h)
     if (h->batch && lgca_batch_remove(h->batch, h) != LGCA_OK) cudaDeviceSynchronize();
     // memory goes back to the pool in stream order, after the handle's queued
     // work (batch steps of a member are ordered before it); no host wait
-    void *mem[] = {h->buf[0], h->buf[1], h->solid, h->slip, h->chir, h->scratch, h->sync};
+    void *mem[] = {h->buf[0], h->buf[1], h->solid, h->slip, h->chir, h->scratch, h->sync, h->bf};
     for (void *p : mem) dfree(h, p);
     if (h->sync_err_host) {
         cudaStreamSynchronize(h->stream);
@@ -580,12 +597,7 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     const int gm = geom_mode(h);
     if (h->variant == VARIANT_PERSIST && nsteps > 1) {
         const size_t sync_bytes = (size_t)(PERSIST_MAX_BLOCKS + 1) * sizeof(int);
-        if (!h->sync) {
-            int sst = dalloc(h, reinterpret_cast<void **>(&h->sync), sync_bytes, true, "flags");
-            if (sst) return sst;
-            CK(h, cudaHostAlloc(&h->sync_err_host, sizeof(int), cudaHostAllocDefault));
-            *h->sync_err_host = 0;
-        }
+        if (const int fst = error_flag(h)) return fst;
         // step flags start at zero; the error flag keeps an earlier timeout
         CK(h, cudaMemsetAsync(h->sync + 1, 0, sync_bytes - sizeof(int), h->stream));
         const PersistWait w{h->wait_ns, h->withhold};
@@ -642,15 +654,20 @@ int lgca_apply_body_force(lgca_handle h, int forcing, int bf_dir, uint64_t *reve
         return fail(h, LGCA_ERR_INVALID, "bf_dir must be 'x', 'y' or 0");
     DeviceGuard dg(h->device);
     const size_t n = (size_t)h->g.W * h->g.H;
-    const size_t need = body_force_scratch_bytes(n) + 64;
-    int st = scratch_reserve(h, need);
-    if (st) return st;
-    unsigned long long *rev = reinterpret_cast<unsigned long long *>(
-        static_cast<char *>(h->scratch) + need - 64);
+    const size_t work = body_force_scratch_bytes(n);
+    if (const int fst = error_flag(h)) return fst;
+    if (!h->bf) {  // zeroed: the table's clean mark says "not clean" until the first call
+        int st = dalloc(h, &h->bf, work + 2 * BODY_FORCE_STICKY_BYTES, true, "body-force table");
+        if (st) return st;
+    }
+    char *sticky = static_cast<char *>(h->bf) + work;
+    unsigned long long *rev =
+        reinterpret_cast<unsigned long long *>(sticky + BODY_FORCE_STICKY_BYTES);
     const uint64_t key = lgca_rng_key(h->seed, LGCA_STREAM_FSEQ, h->fcall);
     CK(h, launch_body_force(h->model, h->g, h->buf[h->cur], h->has_noslip ? h->solid : nullptr,
-                            h->has_slip ? h->slip : nullptr, key, forcing, bf_dir, h->scratch, rev,
-                            h->stream));
+                            h->has_slip ? h->slip : nullptr, key, forcing, bf_dir, h->bf, sticky,
+                            rev, h->sync, h->stream));
+    CK(h, cudaMemcpyAsync(h->sync_err_host, h->sync, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     h->fcall += 1;
     if (reverted) {
         unsigned long long v = 0;

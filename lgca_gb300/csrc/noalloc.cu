@@ -13,11 +13,17 @@
 // The work arrays (first-occurrence table, per-block gains, running total)
 // sit in g_bf_scratch below: LGCA_NOALLOC_MAX_CELLS * 4 bytes + 4 KiB, held
 // by every GPU that loads the library until the process exits.  All calls
-// share it and it keeps the last call's contents; the body-force launcher
-// clears what must start fresh (the table and the running total) at the
-// start of every call.  Calls whose work overlaps on the GPU (different
-// streams, or different host threads) race on it and must be ordered by the
-// caller.
+// share it and it keeps the last call's contents.  The running total starts
+// from zero in every call; the table is left all ones by each call that
+// completes, which a mark at the end of the array records, and a call that
+// finds the mark missing (the first call, a call on a larger lattice than the
+// last, or after a call that stopped early) clears the table first.  Calls
+// whose work overlaps on the GPU (different streams, or different host
+// threads) race on it and must be ordered by the caller.
+//
+// The device address of the array is looked up once per device and cached;
+// it stays valid for the life of that device's CUDA context (a
+// cudaDeviceReset ends it).
 #include "internal.cuh"
 #include "../../include/lgca_gpu.h"
 #include "../../include/lgca/rng.h"
@@ -101,7 +107,7 @@ extern "C" int lgca_apply_body_force_noalloc(int model, int dim_x, int dim_y, ui
         return fail(LGCA_ERR_INVALID, "plane_stride smaller than dim_y * row_pitch");
     if (!(bf_dir == 'x' || bf_dir == 'y' || bf_dir == 0))
         return fail(LGCA_ERR_INVALID, "bf_dir must be 'x', 'y' or 0");
-    if (body_force_scratch_bytes((size_t)ncells) + 64 > kScratchBytes)
+    if (body_force_scratch_bytes((size_t)ncells) + 2 * BODY_FORCE_STICKY_BYTES > kScratchBytes)
         return fail(LGCA_ERR_INVALID, "scratch too small for this lattice");
 
     void *scratch = nullptr;
@@ -116,15 +122,16 @@ extern "C" int lgca_apply_body_force_noalloc(int model, int dim_x, int dim_y, ui
     g.ps = plane_stride;
     g.L = (dim_x - 1) & 63;
     g.lastmask = (g.L == 63) ? ~0ull : ((1ull << (g.L + 1)) - 1ull);
-    // the last 64 bytes of the scratch receive the count when the caller
-    // does not want it
+    // the end of the array: the table's clean mark, then the count when the
+    // caller does not want it
+    unsigned char *tail = static_cast<unsigned char *>(scratch) + kScratchBytes -
+                          2 * BODY_FORCE_STICKY_BYTES;
     unsigned long long *rev =
         reverted ? reverted
-                 : reinterpret_cast<unsigned long long *>(static_cast<unsigned char *>(scratch) +
-                                                          kScratchBytes - 64);
+                 : reinterpret_cast<unsigned long long *>(tail + BODY_FORCE_STICKY_BYTES);
     const uint64_t key = lgca_rng_key(seed, LGCA_STREAM_FSEQ, call);
     cudaError_t e = launch_body_force(model, g, planes, solid, slip, key, forcing, bf_dir, scratch,
-                                      rev, static_cast<cudaStream_t>(stream));
+                                      tail, rev, nullptr, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(LGCA_ERR_CUDA, cudaGetErrorString(e));
     return LGCA_OK;
 }

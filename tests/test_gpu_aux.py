@@ -163,6 +163,28 @@ def test_body_force_matches_oracle_large(gpu, oracle, model):
 
 
 @pytest.mark.parametrize("model", MODELS)
+def test_body_force_consecutive_calls_match_oracle(gpu, oracle, model):
+    """Calls in a row on one handle: each call leaves the first-occurrence
+    table all ones for the next (only the drawn entries are reset), across
+    targets reached in the first chunk, in a later chunk, never, and the
+    minimal target of one draw."""
+    W, H = 1536, 1100
+    types = G.karman_reference(W, H)
+    st = oracle.init_bernoulli(model, W, H, types, seed=8, p_move=0.3, p_rest=0.3)
+    calls = [(500, "x"), (120000, "y"), (10 ** 9, "x"), (0, "x"), (30000, "y"), (1, "x"),
+             (400000, "x")]
+    with gpu.GpuLattice(model, W, H, seed=8) as L:
+        L.set_cell_types(types)
+        L.upload(st)
+        want = st
+        for call, (forcing, d) in enumerate(calls):
+            want, nrev = oracle.apply_body_force(model, want, forcing, types=types, seed=8, call=call,
+                                                 bf_dir=d)
+            assert L.apply_body_force(forcing, d) == nrev, call
+            assert np.array_equal(L.download(), want), call
+
+
+@pytest.mark.parametrize("model", MODELS)
 def test_checkpoint_resume_is_bit_exact(gpu, oracle, model):
     """Stop after 17 steps, save, restore into a fresh handle, run 23 more:
     identical to 40 uninterrupted steps (geometry, forcing, chirality,
