@@ -28,10 +28,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
 #include "../lgca_gpu.h"
+#include "gb_device.h"
 #include "rng.h"
 
 namespace lgca_gb300 {
@@ -116,11 +118,7 @@ public:
         init_storage(coarse_graining_radius);
     }
 
-    virtual ~GB_Lattice()
-    {
-        if (m_snap) lgca_destroy(m_snap);
-        lgca_destroy(m_h);
-    }
+    virtual ~GB_Lattice() = default;
 
     GB_Lattice(const GB_Lattice &) = delete;
     GB_Lattice &operator=(const GB_Lattice &) = delete;
@@ -129,27 +127,27 @@ public:
     void apply_cell_type_all(const CellType t)
     {
         for (size_t c = 0; c < m_num_cells; ++c) m_cell_type[c] = t;
-        m_types_dirty = true;
+        m_dev->mark_types_dirty();
     }
     void apply_boundary_cell_type_east(const CellType t)
     {
         for (size_t c = m_dim_x - 1; c < m_num_cells; c += m_dim_x) m_cell_type[c] = t;
-        m_types_dirty = true;
+        m_dev->mark_types_dirty();
     }
     void apply_boundary_cell_type_north(const CellType t)
     {
         for (size_t c = m_num_cells - m_dim_x; c < m_num_cells; ++c) m_cell_type[c] = t;
-        m_types_dirty = true;
+        m_dev->mark_types_dirty();
     }
     void apply_boundary_cell_type_west(const CellType t)
     {
         for (size_t c = 0; c < m_num_cells; c += m_dim_x) m_cell_type[c] = t;
-        m_types_dirty = true;
+        m_dev->mark_types_dirty();
     }
     void apply_boundary_cell_type_south(const CellType t)
     {
         for (size_t c = 0; c < m_dim_x; ++c) m_cell_type[c] = t;
-        m_types_dirty = true;
+        m_dev->mark_types_dirty();
     }
     void apply_bc_periodic() { apply_cell_type_all(CellType::FLUID); }
     void apply_bc_reflecting(const std::string bounce_type)
@@ -185,7 +183,7 @@ public:
             const Real dist = std::sqrt(std::pow((pos_x - center_x), 2.0) + std::pow((pos_y - center_y), 2.0));
             if (dist < (diameter / 2.0)) m_cell_type[cell] = CellType::SOLID_NO_SLIP;
         }
-        m_types_dirty = true;
+        m_dev->mark_types_dirty();
     }
 
     // ---- initialisers (host state), src/lattice.cpp:165-308,463-496
@@ -196,7 +194,7 @@ public:
         pull_state();
         init_zero();
         for (size_t n : occupied_nodes) m_node_state[n / 8] |= (uint8_t)(1u << (n % 8));
-        m_state_dirty = true;
+        m_dev->mark_state_dirty();
     }
     void init_single_collision()
     {
@@ -222,10 +220,8 @@ public:
     unsigned long get_n_particles()
     {
         push();
-        uint64_t n = 0;
-        check(lgca_count_particles(m_h, &n), "get_n_particles");
-        m_num_particles = n;
-        return (unsigned long)n;
+        m_num_particles = m_dev->count_particles();
+        return (unsigned long)m_num_particles;
     }
     // Bitset::print of the state (src/lgca_bitset.h:198-203)
     void print()
@@ -272,55 +268,35 @@ public:
     {
         (void)p;
         push();
-        check(lgca_collide_and_propagate(m_h, 1), "collide_and_propagate");
-        m_state_stale = true;
-        ++m_version;
+        m_dev->step(1);
     }
     // Extension: n steps in one call (the engine may fuse them).
     void collide_and_propagate_n(int nsteps)
     {
         push();
-        check(lgca_collide_and_propagate(m_h, nsteps), "collide_and_propagate");
-        m_state_stale = true;
-        ++m_version;
+        m_dev->step(nsteps);
     }
     std::vector<Real> get_mean_velocity()  // src/omp_lattice.cpp:508-557
     {
         push();
-        float ux = 0, uy = 0;
-        check(lgca_mean_velocity(m_h, &ux, &uy), "get_mean_velocity");
-        return std::vector<Real>{ux, uy};
+        return m_dev->mean_velocity();
     }
     void apply_body_force(const int forcing)  // src/omp_lattice.cpp:254-346
     {
         push();
-        uint64_t n = 0;
-        check(lgca_apply_body_force(m_h, forcing, m_bf_dir, &n), "apply_body_force");
-        m_last_reverted = n;
-        m_state_stale = true;
-        ++m_version;
+        m_dev->body_force(forcing, m_bf_dir);
     }
     // src/omp_lattice.cpp:349-454, on the output buffer
     void post_process()
     {
-        lgca_handle src = m_h;
-        if (m_out_version != m_version || m_state_dirty) {
-            // the device state moved on since the last copy_data_to_output_buffer():
-            // post-process the buffer's copy on a second lattice
-            if (!m_snap) {
-                check(lgca_create((int)model_, m_dim_x, m_dim_y, m_seed, &m_snap), "post_process");
-            }
-            check(lgca_upload_state(m_snap, m_node_state_out.data()), "post_process");
-            src = m_snap;
-        }
-        check(lgca_post_process(src, m_coarse_graining_radius, m_cell_density.data(),
-                                m_cell_momentum.data(), m_mean_density.data(),
-                                m_mean_momentum.data()),
-              "post_process");
+        m_dev->post_process(m_node_state_out.data(), (int)m_coarse_graining_radius,
+                            m_cell_density.data(), m_cell_momentum.data(), m_mean_density.data(),
+                            m_mean_momentum.data());
     }
     void copy_data_to_device()
     {
-        m_types_dirty = m_state_dirty = true;
+        m_dev->mark_types_dirty();
+        m_dev->mark_state_dirty();
         push();
     }
     void copy_data_from_device() { pull_state(); }
@@ -328,7 +304,7 @@ public:
     {
         pull_state();
         m_node_state_out = m_node_state;
-        m_out_version = m_version;
+        m_dev->output_taken();
     }
 
     // ---- getters (src/lattice.h:213-237)
@@ -353,17 +329,20 @@ public:
     Real mean_density(const int x, const int y) { return m_mean_density[y * m_dim_x + x]; }
 
     // ---- extensions of this engine
-    lgca_handle handle() { push(); return m_h; }
+    lgca_handle handle() { push(); return m_dev->handle(); }
     uint64_t seed() const { return m_seed; }
     char bf_dir() const { return m_bf_dir; }
-    uint64_t last_reverted() const { return m_last_reverted; }
+    uint64_t last_reverted() const { return m_dev->last_reverted(); }
     const uint8_t *node_state() { pull_state(); return m_node_state.data(); }
     const CellType *cell_types() const { return m_cell_type.data(); }
     void set_forcing_column(int x, double p)
     {
-        check(lgca_set_forcing_column(m_h, x, p), "set_forcing_column");
+        m_dev->check(lgca_set_forcing_column(m_dev->handle(), x, p), "set_forcing_column");
     }
-    void set_temporal_depth(int depth) { check(lgca_set_temporal_depth(m_h, depth), "set_temporal_depth"); }
+    void set_temporal_depth(int depth)
+    {
+        m_dev->check(lgca_set_temporal_depth(m_dev->handle(), depth), "set_temporal_depth");
+    }
     // Integer B x B block sums (N, Jx2, Jy), each ceil(H/B) x ceil(W/B).
     void block_sums(int B, std::vector<int32_t> &N, std::vector<int32_t> &Jx2, std::vector<int32_t> &Jy)
     {
@@ -372,7 +351,7 @@ public:
         N.resize(nb);
         Jx2.resize(nb);
         Jy.resize(nb);
-        check(lgca_block_sums(m_h, B, N.data(), Jx2.data(), Jy.data()), "block_sums");
+        m_dev->check(lgca_block_sums(m_dev->handle(), B, N.data(), Jx2.data(), Jy.data()), "block_sums");
     }
 
 protected:
@@ -395,10 +374,8 @@ protected:
         m_cell_momentum.assign(2 * m_num_cells, 0.0f);
         m_mean_density.assign(m_num_coarse_cells, 0.0f);
         m_mean_momentum.assign(2 * m_num_coarse_cells, 0.0f);
-        if (lgca_create((int)model_, (int)m_dim_x, (int)m_dim_y, m_seed, &m_h) != LGCA_OK) {
-            printf("ERROR in GB_Lattice(): %s\n", lgca_last_error(nullptr));
-            abort();
-        }
+        m_dev.reset(new DeviceLattice((int)model_, m_dim_x, m_dim_y, m_seed));
+        m_dev->handle();  // the GPU lattice exists from construction on
     }
     // Bernoulli(1/NUM_DIR) per channel of FLUID cells (src/lattice.cpp:198-217,
     // :465-496) from the INIT stream, as lgca_init_random draws it; other
@@ -419,39 +396,15 @@ protected:
             }
             m_node_state[cell] = s;
         }
-        m_state_dirty = true;
+        m_dev->mark_state_dirty();
     }
     // host -> device when the host arrays changed
-    void push()
-    {
-        if (m_types_dirty) {
-            std::vector<int32_t> t(m_num_cells);
-            for (size_t c = 0; c < m_num_cells; ++c) t[c] = (int32_t)m_cell_type[c];
-            check(lgca_set_cell_types(m_h, t.data()), "set_cell_types");
-            m_types_dirty = false;
-        }
-        if (m_state_dirty) {
-            check(lgca_upload_state(m_h, m_node_state.data()), "upload_state");
-            m_state_dirty = false;
-            m_state_stale = false;
-            ++m_version;
-        }
-    }
+    void push() { m_dev->push(m_cell_type.data(), m_node_state.data()); }
     // device -> host when the device state moved on
     void pull_state()
     {
         push();
-        if (m_state_stale) {
-            check(lgca_download_state(m_h, m_node_state.data()), "download_state");
-            m_state_stale = false;
-        }
-    }
-    void check(int status, const char *what)
-    {
-        if (status != LGCA_OK) {
-            printf("ERROR in GB_Lattice::%s(): %s\n", what, lgca_last_error(m_h));
-            abort();
-        }
+        m_dev->pull(m_node_state.data());
     }
     unsigned int m_dim_x = 0, m_dim_y = 0;
     size_t m_num_cells = 0, m_num_nodes = 0, m_num_particles = 0;
@@ -461,15 +414,13 @@ protected:
     const Real m_rho = 1.0, m_c = 1.0;
     Real m_Re = 0, m_Ma_s = 0, m_d = 0, m_nu = 0, m_g = 0, m_nu_s = 0, m_c_s = 0, m_u = 0;
     char m_bf_dir = 0;
-    uint64_t m_seed = 0, m_last_reverted = 0;
+    uint64_t m_seed = 0;
 
     std::vector<CellType> m_cell_type;
     std::vector<uint8_t> m_node_state, m_node_state_out;  // one byte per cell, bit d = channel d
     std::vector<Real> m_cell_density, m_mean_density, m_cell_momentum, m_mean_momentum;
 
-    lgca_handle m_h = nullptr, m_snap = nullptr;
-    bool m_types_dirty = true, m_state_dirty = true, m_state_stale = false;
-    uint64_t m_version = 0, m_out_version = ~0ull;
+    std::unique_ptr<DeviceLattice> m_dev;  // the GPU lattice and its upload state
 };
 
 }  // namespace lgca_gb300

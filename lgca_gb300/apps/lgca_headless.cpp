@@ -13,8 +13,12 @@
 //
 // Common options: --frames N (viewer cases) or --steps N (box/periodic),
 // --model HPP|FHP_I|FHP_II|FHP_III, --Re, --Ma, --r, --seed, --out DIR,
-// --format none|vti|png, --every N.  Prints the reference's messages and a
-// final JSON line with the run's summary.
+// --format none|vti|png, --every N, --dump FILE (the final state, one byte
+// per cell, bit d = channel d).  Prints the reference's messages and a final
+// JSON line with the run's summary; for the pipe and karman cases it carries
+// the forcing controller's trace, one entry per frame: the bits of the mean
+// x velocity (float), the forcing applied (-1: none) and the particles
+// reverted.
 #include "lgca/gb_lattice.h"
 #include "lgca/io.h"
 
@@ -31,6 +35,7 @@ struct Options {
     std::string model = "FHP_III";
     std::string out = "./";
     std::string format = "none";
+    std::string dump;
     float Re = -1, Ma = -1;
     int r = -1;
     int frames = 20;
@@ -47,7 +52,7 @@ static void usage()
                  "usage: lgca_headless --case pipe|karman|diffusion|single|box|periodic "
                  "[--frames N] [--steps N] [--model M] [--Re x] [--Ma x] [--r n] [--seed s] "
                  "[--out dir] [--format none|vti|png] [--every N] [--write-steps N] "
-                 "[--bf-steps N] [--bf-intensity x]\n");
+                 "[--bf-steps N] [--bf-intensity x] [--dump file]\n");
     std::exit(2);
 }
 
@@ -74,6 +79,7 @@ static Options parse(int argc, char **argv)
         else if (a == "--bf-steps") o.bf_steps = std::stoi(val());
         else if (a == "--bf-intensity") o.bf_intensity = std::stof(val());
         else if (a == "--seed") o.seed = std::stoull(val());
+        else if (a == "--dump") o.dump = val();
         else usage();
     }
     if (!o.out.empty() && o.out.back() != '/') o.out += '/';
@@ -106,6 +112,17 @@ template <class L> static void output(L &lat, const Options &o, size_t step)
     }
 }
 
+template <class L> static void dump_state(L &lat, const Options &o)
+{
+    if (o.dump.empty()) return;
+    FILE *f = std::fopen(o.dump.c_str(), "wb");
+    if (!f || std::fwrite(lat.node_state(), 1, lat.num_cells(), f) != lat.num_cells()) {
+        std::fprintf(stderr, "cannot write %s\n", o.dump.c_str());
+        std::exit(1);
+    }
+    std::fclose(f);
+}
+
 template <Model M> static int run_viewer(Options o)
 {
     int pp = 5;
@@ -128,13 +145,22 @@ template <Model M> static int run_viewer(Options o)
     size_t steps = 0;
     double sim_time = 0;
     std::vector<Real> u{0, 0};
+    std::string trace;
     for (int frame = 0; frame < o.frames; ++frame) {
         if (controller) {  // apps/pipe/pipe_viewer.cpp:107-125
             u = lat.get_mean_velocity();
+            int applied = -1;
             if (u[0] < lat.u()) {
                 if (u[0] > 0.9 * lat.u()) forcing = (int)lat.get_equilibrium_forcing();
                 lat.apply_body_force(forcing);
+                applied = forcing;
             }
+            uint32_t bits;
+            std::memcpy(&bits, &u[0], sizeof(bits));
+            char e[96];
+            std::snprintf(e, sizeof(e), "%s[%u, %d, %llu]", trace.empty() ? "" : ", ", bits, applied,
+                          applied >= 0 ? (unsigned long long)lat.last_reverted() : 0ull);
+            trace += e;
         }
         const auto t0 = std::chrono::steady_clock::now();
         for (int s = 0; s < pp; ++s) {
@@ -153,12 +179,13 @@ template <Model M> static int run_viewer(Options o)
         std::fprintf(stderr, "Error check FAILED: There is a difference in the number of particles of %lld.\n",
                      (long long)n1 - (long long)n0);
     u = lat.get_mean_velocity();
+    dump_state(lat, o);
     const double mnups = sim_time > 0 ? lat.num_cells() * (double)steps / (sim_time * 1e6) : 0.0;
     std::printf("{\"case\": \"%s\", \"dims\": [%u, %u], \"steps\": %zu, \"particles_start\": %zu, "
                 "\"particles_end\": %zu, \"mean_velocity\": [%.6g, %.6g], \"mnups\": %.1f, "
-                "\"forcing\": %d}\n",
+                "\"forcing\": %d, \"trace\": [%s]}\n",
                 o.test_case.c_str(), lat.dim_x(), lat.dim_y(), steps, n0, n1, u[0], u[1], mnups,
-                forcing);
+                forcing, trace.c_str());
     return n1 == n0 ? 0 : 1;
 }
 
@@ -200,6 +227,7 @@ template <Model M> static int run_cli(Options o)
         }
     }
     const size_t n1 = lat.get_n_particles();
+    dump_state(lat, o);
     const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_all).count();
     if (n1 == n0) std::printf("Error check PASSED: There is no difference in the number of particles.\n");
     else std::printf("Error check FAILED: There is a difference in the number of particles of %lld.\n",

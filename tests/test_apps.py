@@ -139,3 +139,91 @@ def test_app_loops_conserve_particles(gpu, tmp_path, case, extra):
         assert pngs
         w, h, _ = read_png(pngs[-1])
         assert (w, h) == (summary["dims"][0] // 20, summary["dims"][1] // 20)
+
+
+# ------------------------------------------------------------------ oracle app loops
+def oracle_viewer_loop(oracle, model, case, frames, seed, Re, Ma, r, pp=5):
+    """The pipe / karman viewer loop (apps/pipe/pipe_viewer.cpp:100-146,
+    apps/karman/karman_viewer.cpp: same loop) on the oracle: mean velocity,
+    the forcing controller with the reference's thresholds, the random-cell
+    body force (src/omp_lattice.cpp:254-346), then pp steps per frame.
+    Returns the final state and the controller's trace."""
+    p = P.lattice_parameters(model, case, Re, Ma, r)
+    W, H = p["dim_x"], p["dim_y"]
+    types = G.pipe(W, H) if case == "pipe" else G.karman_reference(W, H)
+    D = P.NUM_DIR[model]
+    st = oracle.init_bernoulli(model, W, H, types, seed=seed, p_move=1 / D, p_rest=1 / D)
+    u_ref = np.float32(p["u"])
+    forcing, call, steps, trace = p["initial_forcing"], 0, 0, []
+    for _ in range(frames):
+        ux, _ = oracle.mean_velocity(model, st, types)
+        ux = np.float32(ux)
+        applied, nrev = -1, 0
+        if ux < u_ref:  # float comparison, as Real < Real
+            if float(ux) > 0.9 * float(u_ref):  # double comparison, as Real > double
+                forcing = p["equilibrium_forcing"]
+            st, nrev = oracle.apply_body_force(model, st, forcing, types=types, seed=seed, call=call,
+                                               bf_dir="x")
+            call += 1
+            applied = forcing
+        trace.append((ux, applied, nrev))
+        st = oracle.run(model, st, pp, types=types, seed=seed, t0=steps)
+        steps += pp
+    return st, trace, (W, H)
+
+
+# (case, model, frames, Re, Ma, controller branches the run takes): at Ma 0.3
+# the flow passes 0.9 u and the controller switches from the initial to the
+# equilibrium forcing; at Ma 0.05 it overshoots u and stops forcing
+@pytest.mark.gpu
+@pytest.mark.parametrize("case,model,frames,Re,Ma,branches", [
+    ("pipe", "FHP_III", 20, 20.0, 0.3, ("initial", "equilibrium")),
+    ("pipe", "FHP_I", 18, 20.0, 0.3, ("initial", "equilibrium")),
+    ("pipe", "HPP", 16, 20.0, 0.3, ("initial", "equilibrium")),
+    ("pipe", "FHP_III", 14, 10.0, 0.05, ("initial", "none")),
+    ("karman", "FHP_III", 16, 20.0, 0.3, ("initial", "equilibrium"))])
+def test_viewer_loop_with_forcing_controller_matches_oracle(gpu, oracle, tmp_path, case, model,
+                                                             frames, Re, Ma, branches):
+    """The pipe and karman app loops on the GPU (C++ GB_Lattice over the
+    shared device half of include/lgca/gb_device.h): the mean velocity
+    feeding the controller, the body force it applies and the state after the
+    run equal the oracle running the same loop."""
+    mnum = {"HPP": 0, "FHP_I": 1, "FHP_III": 3}[model]
+    r = 10 if case == "pipe" else 20
+    dump = tmp_path / "state.bin"
+    summary, _ = run_app(gpu, "--case", case, "--model", model, "--frames", frames, "--Re", Re,
+                         "--Ma", Ma, "--r", r, "--seed", 5, "--dump", dump)
+    want, trace, (W, H) = oracle_viewer_loop(oracle, mnum, case, frames, 5, Re, Ma, r)
+    assert summary["dims"] == [W, H]
+    got_trace = summary["trace"]
+    assert len(got_trace) == frames
+    for (ux_bits, applied, nrev), (ux, w_applied, w_nrev) in zip(got_trace, trace):
+        gux = np.array([ux_bits], np.uint32).view(np.float32)[0]
+        assert gux == pytest.approx(float(ux), rel=1e-5, abs=1e-7)
+        assert (applied, nrev) == (w_applied, w_nrev)
+    applied = {a for _, a, _ in trace}
+    p = P.lattice_parameters(mnum, case, Re, Ma, r)
+    names = {"initial": p["initial_forcing"], "equilibrium": p["equilibrium_forcing"], "none": -1}
+    assert {names[b] for b in branches} <= applied
+    got = np.fromfile(dump, np.uint8).reshape(H, W)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case,model", [("box", "FHP_III"), ("periodic", "HPP"),
+                                        ("periodic", "FHP_II")])
+def test_cli_loop_matches_oracle(gpu, oracle, tmp_path, case, model):
+    """The box / periodic CLI loop (apps/box/main.cpp:230-312): steps 0..N,
+    no forcing (bf_dir is 0 for these test cases)."""
+    mnum = {"HPP": 0, "FHP_II": 2, "FHP_III": 3}[model]
+    dump = tmp_path / "state.bin"
+    summary, _ = run_app(gpu, "--case", case, "--model", model, "--steps", 30, "--Re", 96,
+                         "--seed", 3, "--dump", dump)
+    p = P.lattice_parameters(mnum, case, 96.0, 0.3, 4)
+    W, H = p["dim_x"], p["dim_y"]
+    types = G.reflecting(W, H, "back") if case == "box" else G.periodic(W, H)
+    D = P.NUM_DIR[mnum]
+    st = oracle.init_bernoulli(mnum, W, H, types, seed=3, p_move=1 / D, p_rest=1 / D)
+    want = oracle.run(mnum, st, summary["steps"], types=types, seed=3)
+    got = np.fromfile(dump, np.uint8).reshape(H, W)
+    assert np.array_equal(got, want)
