@@ -393,7 +393,7 @@ def run_ours(args):
         # the batched workload: 512 mixed lattices x 1000 steps, batched vs one at a time
         from lgca_gb300 import batched as BT
         batched = BT.compare(512, 1000, tune=True)
-        batched.pop("tuned_words_per_lane", None)
+        batched.pop("tuned", None)
         batched.update(oracle_check(batched.pop("final_sha")))
     served = None
     if rank == 0 and not args.no_served:

@@ -281,7 +281,10 @@ int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes);
 
 /* Batches: many lattices (any sizes, models, geometries) advanced together,
  * one launch per step over a device work-list of the members' rows, the
- * steps captured in CUDA graphs.  Members stay owned by
+ * steps captured in CUDA graphs.  A member whose kernel variant is 2 (the
+ * register wavefront) with depth 2, 4 or 8 (8: HPP) and whose dim_x is a
+ * multiple of 64 runs its steps as passes of `depth` steps over its state
+ * (after nsteps % depth single steps with the others).  Members stay owned by
  * the caller and keep their own state, counters and settings; each member
  * gives exactly the bits it gives when stepped alone.  No reference
  * counterpart (the reference steps one lattice per object).
@@ -311,6 +314,14 @@ int lgca_batch_set_graph_steps(lgca_batch_handle b, int steps_per_graph); /* 0: 
  * 1 G sites); fewer give more parallelism to small calls.  A tuning knob:
  * results do not depend on it.  (No reference counterpart.) */
 int lgca_batch_set_warp_tasks(lgca_batch_handle b, int n);
+/* Persistent form (on = 1): the one-step work of each call runs as one
+ * cooperative launch per stretch of steps with an unchanged set of members,
+ * the resident blocks walking the work-list with a grid barrier between
+ * steps, instead of one launch per step (on = 0, default).  A barrier wait
+ * is bounded (2 s): when one gives up, the next lgca_batch_sync returns
+ * LGCA_ERR_TIMEOUT once and the members' states are unspecified.  Results do
+ * not depend on the form.  (No reference counterpart.) */
+int lgca_batch_set_persistent(lgca_batch_handle b, int on);
 int lgca_batch_sync(lgca_batch_handle b);
 const char *lgca_batch_last_error(lgca_batch_handle b);
 void *lgca_batch_stream(lgca_batch_handle b);

@@ -104,6 +104,7 @@ def lib() -> C.CDLL:
             "lgca_batch_set_graph_steps": (C.c_int, [vp, C.c_int]),
             "lgca_batch_set_warp_tasks": (C.c_int, [vp, C.c_int]),
             "lgca_batch_sync": (C.c_int, [vp]),
+            "lgca_batch_set_persistent": (C.c_int, [vp, C.c_int]),
             "lgca_batch_last_error": (C.c_char_p, [vp]),
             "lgca_batch_stream": (vp, [vp]),
             "lgca_apply_body_force_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, C.c_size_t,
@@ -391,6 +392,10 @@ class GpuBatch:
 
     def step(self, nsteps: int) -> None:
         self._chk(lib().lgca_batch_step(self._b, int(nsteps)))
+
+    def set_persistent(self, on: bool) -> None:
+        """One cooperative launch per stretch of steps (grid barrier per step)."""
+        self._chk(lib().lgca_batch_set_persistent(self._b, int(bool(on))))
 
     def set_warp_tasks(self, n: int) -> None:
         """Warp tasks per warp of the batched kernel (1, 2, 4 or 8; 0 = per call)."""

@@ -105,7 +105,7 @@ def compare(n_jobs: int = 512, steps: int = 1000, tune: bool = True) -> dict:
             "batched_gsite_updates_s": sites * steps / tb / 1e9,
             "one_by_one_gsite_updates_s": sites * steps / ts / 1e9,
             "speedup": ts / tb, "bit_exact": hb == hs,
-            "tuned_words_per_lane": tuned, "final_sha": hb}
+            "tuned": {k: list(v) for k, v in tuned.items()}, "final_sha": hb}
 
 
 def main(argv=None):

@@ -117,6 +117,10 @@ struct BatchEntry {
     int tasks;
     int gm, wpt;  // geometry mode, words per lane
     int code;     // model family * 9 + geometry mode * 3 + path (0 word, 1 pair, 2 pair, odd words)
+    // members on the register wavefront (k_batch_wave): steps per pass K, the
+    // single steps r that come before the passes, slab rows S and strips of
+    // 30 words per row; tasks = strips x slabs
+    int K, r, S, nstrips;
 };
 // total_tasks: warp tasks of the active members (each member's tasks padded
 // to whole blocks of 8 * warp_tasks); block_lat[b] = member of block b;
@@ -125,6 +129,18 @@ struct BatchEntry {
 cudaError_t launch_batch(const BatchEntry *E, const int *block_lat, int total_tasks, int s_local,
                          const int *s_base, int gmax, int warp_tasks, cudaStream_t stream);
 cudaError_t launch_batch_keys(const BatchEntry *E, int n, int max_steps, cudaStream_t stream);
+// Persistent form of launch_batch: steps s0 .. s0 + nsteps - 1 (batch-local)
+// in one cooperative launch with a grid barrier between steps; *bar must be
+// zero before the launch; *err is set when a barrier wait passes wait_ns.
+cudaError_t launch_batch_persist(const BatchEntry *E, const int *block_lat, int total_tasks, int s0,
+                                 int nsteps, unsigned *bar, int *err, uint64_t wait_ns, int gmax,
+                                 int warp_tasks, cudaStream_t stream);
+// Pass j_base[0] + j_local of K steps for the wave members: total_tasks warp
+// tasks (each member's padded to whole blocks of WAVE_BLOCK_WARPS warps),
+// block_lat[b] = member of block b.
+cudaError_t launch_batch_wave(const BatchEntry *E, const int *block_lat, int total_tasks, int j_local,
+                              const int *j_base, int gmax, int K, cudaStream_t stream);
+static constexpr int WAVE_BLOCK_WARPS = 4;
 cudaError_t launch_advance(int *s_base, int by, cudaStream_t stream);
 cudaError_t launch_set_base(int *s_base, int v, cudaStream_t stream);
 

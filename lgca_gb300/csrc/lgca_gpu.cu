@@ -1007,25 +1007,19 @@ int lgca_device_bytes(lgca_handle h, size_t *bytes)
 // ------------------------------------------------------------------ batches
 }  // extern "C"
 
-struct lgca_batch {
-    std::vector<lgca_lattice *> members;
-    // one per member: its stream's work before a call, recorded only when the
-    // member's stream was used since it last stepped
-    std::vector<cudaEvent_t> ev;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr;  // end of the latest call; members' streams wait on it lazily
-    int *s_base = nullptr;       // device: first batch-local step of a graph replay
-    int graph_steps = 32;        // steps captured per CUDA graph (0: no graphs)
-    int warp_tasks = 0;          // warp tasks per warp of the batched kernel (0: per call)
-    int call_wt = 1;             // the value used by the current call
-    // device work-list: entries, task prefix, block -> lattice map, key table
+namespace {
+// One launch sequence of a batch call: the device work-list (entries, task
+// prefix and block -> entry map in one allocation, the key table), its
+// pinned staging and the device counter of graph replays.  Entries come in
+// descending order of their sort key `nsteps` (units to run: steps or
+// passes), so the entries active at unit u are a prefix of the list.
+struct WorkList {
     BatchEntry *dE = nullptr;
     int *dP = nullptr, *dB = nullptr;  // dB points into dP's allocation
     uint64_t *dK = nullptr;
     size_t capE = 0, capB = 0, capK = 0;
     std::vector<BatchEntry> E;
-    std::vector<int> P, Bl, nsteps;  // nsteps per entry, descending
+    std::vector<int> P, Bl, nsteps;
     // pinned staging of the work-list, two slots used in turn; a slot is
     // rewritten once the copies out of it (two calls back) have run
     struct Staging {
@@ -1034,6 +1028,31 @@ struct lgca_batch {
         cudaEvent_t copied = nullptr;
     } stage[2];
     int slot = 0;
+    int *base = nullptr;  // device: first unit of a graph replay
+};
+constexpr int WAVE_DEPTHS[3] = {2, 4, 8};
+constexpr int WAVE_SLAB_ROWS = 64;  // output rows per wavefront warp task
+}  // namespace
+
+struct lgca_batch {
+    std::vector<lgca_lattice *> members;
+    // one per member: its stream's work before a call, recorded only when the
+    // member's stream was used since it last stepped
+    std::vector<cudaEvent_t> ev;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;  // end of the latest call; members' streams wait on it lazily
+    int graph_steps = 32;        // steps captured per CUDA graph (0: no graphs)
+    int warp_tasks = 0;          // warp tasks per warp of the batched kernel (0: per call)
+    int call_wt = 1;             // the value used by the current call
+    WorkList main;               // one step per launch (k_batch), all members' keys
+    WorkList wave[3];            // passes of 2, 4, 8 steps (k_batch_wave)
+    // persistent form of the one-step work: one cooperative launch per
+    // segment, grid barrier counter and error flag (device), the flag's
+    // pinned copy read by lgca_batch_sync
+    int persistent = 0;
+    unsigned *pbar = nullptr;
+    int *perr = nullptr, *perr_host = nullptr;
     std::string err;
 };
 
@@ -1059,18 +1078,6 @@ int bcuda(lgca_batch *b, cudaError_t e, const char *what)
         if (e_ != cudaSuccess) return bcuda((b), e_, #expr);        \
     } while (0)
 
-// Launches of batch-local steps [0, n) of one segment (fixed active set),
-// steps numbered from *s_base + s_local; then *s_base advances by n.
-int enqueue_steps(lgca_batch *b, int n_active, int tasks, int n)
-{
-    int gmax = GEOM_NONE;  // the active members are the first n_active entries
-    for (int i = 0; i < n_active; ++i) gmax = std::max(gmax, b->E[i].gm);
-    for (int s = 0; s < n; ++s)
-        BCK(b, launch_batch(b->dE, b->dB, tasks, s, b->s_base, gmax, b->call_wt, b->stream));
-    BCK(b, launch_advance(b->s_base, n, b->stream));
-    return LGCA_OK;
-}
-
 template <class T> int grow(lgca_batch *b, T *&p, size_t &cap, size_t n)
 {
     if (cap >= n) return LGCA_OK;
@@ -1081,6 +1088,155 @@ template <class T> int grow(lgca_batch *b, T *&p, size_t &cap, size_t n)
     BCK(b, cudaMalloc(&p, n * sizeof(T)));
     cap = n;
     return LGCA_OK;
+}
+
+void wl_clear(WorkList &w)
+{
+    w.E.clear();
+    w.P.assign(1, 0);
+    w.nsteps.clear();
+}
+
+// Append an entry with `own` warp tasks (padded to whole blocks of
+// per_block) and sort key n, not larger than the previous entry's.
+int wl_add(lgca_batch *b, WorkList &w, BatchEntry e, long long own, int n, int per_block)
+{
+    e.task0 = w.P.back();
+    e.tasks = (int)std::min(own, 0x7fffffffLL);
+    const long long tasks = (long long)w.P.back() + (own + per_block - 1) / per_block * per_block;
+    if (tasks > 0x7fffffffLL) return bfail(b, LGCA_ERR_INVALID, "batch work-list too long");
+    w.E.push_back(e);
+    w.P.push_back((int)tasks);
+    w.nsteps.push_back(n);
+    return LGCA_OK;
+}
+
+// Block map, device arrays (and a key table of nkeys words, to which the
+// entries' key offsets are rebased), and the copy through a pinned slot.
+int wl_upload(lgca_batch *b, WorkList &w, int per_block, size_t nkeys)
+{
+    const int ne = (int)w.E.size();
+    if (ne == 0) return LGCA_OK;
+    const int nblocks = w.P.back() / per_block;  // every entry's tasks fill whole blocks
+    w.Bl.resize(nblocks);
+    for (int l = 0; l < ne; ++l)
+        for (int blk = w.P[l] / per_block; blk < w.P[l + 1] / per_block; ++blk) w.Bl[blk] = l;
+    int st;
+    if ((st = grow(b, w.dE, w.capE, (size_t)ne)) != LGCA_OK) return st;
+    if ((st = grow(b, w.dP, w.capB, (size_t)ne + 1 + nblocks)) != LGCA_OK) return st;
+    if (nkeys) {
+        if ((st = grow(b, w.dK, w.capK, nkeys)) != LGCA_OK) return st;
+        for (auto &e : w.E) e.keys = w.dK + reinterpret_cast<size_t>(e.keys);
+    }
+    w.dB = w.dP + ne + 1;
+    if (!w.base) BCK(b, cudaMalloc(&w.base, sizeof(int)));
+    for (auto &sg : w.stage)
+        if (!sg.copied) BCK(b, cudaEventCreateWithFlags(&sg.copied, cudaEventDisableTiming));
+    // entries, then prefix and block map (contiguous on the device as on the host)
+    auto &sg = w.stage[w.slot];
+    w.slot ^= 1;
+    BCK(b, cudaEventSynchronize(sg.copied));
+    const size_t eb = (ne * sizeof(BatchEntry) + 15) & ~(size_t)15;
+    const size_t ib = ((size_t)ne + 1 + nblocks) * sizeof(int);
+    if (sg.cap < eb + ib) {
+        if (sg.host) cudaFreeHost(sg.host);
+        sg.host = nullptr;
+        sg.cap = 0;
+        BCK(b, cudaHostAlloc(&sg.host, 2 * (eb + ib), cudaHostAllocDefault));
+        sg.cap = 2 * (eb + ib);
+    }
+    char *hp = static_cast<char *>(sg.host);
+    memcpy(hp, w.E.data(), ne * sizeof(BatchEntry));
+    memcpy(hp + eb, w.P.data(), (ne + 1) * sizeof(int));
+    memcpy(hp + eb + (ne + 1) * sizeof(int), w.Bl.data(), nblocks * sizeof(int));
+    BCK(b, cudaMemcpyAsync(w.dE, hp, ne * sizeof(BatchEntry), cudaMemcpyHostToDevice, b->stream));
+    BCK(b, cudaMemcpyAsync(w.dP, hp + eb, ib, cudaMemcpyHostToDevice, b->stream));
+    BCK(b, cudaEventRecord(sg.copied, b->stream));
+    return LGCA_OK;
+}
+
+// The launch sequence of a list: units 0 .. max-1 in segments of constant
+// active prefix; enqueue(k, tasks, n, u) queues n units u .. u + n - 1 over
+// the first k entries (launches read their unit from *base + local index, and
+// advance *base by n).  Segments of at least two graphs' worth of units
+// replay a graph of `per_graph` units.
+template <class Enqueue>
+int wl_run(lgca_batch *b, WorkList &w, int per_graph, Enqueue enqueue)
+{
+    const int ne = (int)w.E.size();
+    const int max_units = ne ? w.nsteps[0] : 0;
+    int s0 = 0;
+    while (s0 < max_units) {
+        int k = 0;
+        while (k < ne && w.nsteps[k] > s0) ++k;
+        const int s1 = w.nsteps[k - 1], len = s1 - s0, tasks = w.P[k];
+        BCK(b, launch_set_base(w.base, s0, b->stream));
+        const int G = per_graph > 0 ? std::min(per_graph, len) : 0;
+        int done = 0;
+        if (G > 1 && len >= 2 * G) {
+            cudaGraph_t graph = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            const int st = enqueue(k, tasks, G, s0);
+            cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+            if (st != LGCA_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                return st;
+            }
+            BCK(b, e);
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            BCK(b, e);
+            for (; done + G <= len; done += G) {
+                e = cudaGraphLaunch(exec, b->stream);
+                if (e != cudaSuccess) {
+                    cudaGraphExecDestroy(exec);
+                    return bcuda(b, e, "cudaGraphLaunch");
+                }
+            }
+            cudaGraphExecDestroy(exec);  // released once its queued launches complete
+        }
+        if (done < len) {
+            const int st = enqueue(k, tasks, len - done, s0 + done);
+            if (st != LGCA_OK) return st;
+        }
+        s0 = s1;
+    }
+    return LGCA_OK;
+}
+
+// Device state of the persistent form, at first use.
+int persist_state(lgca_batch *b)
+{
+    if (b->pbar) return LGCA_OK;
+    BCK(b, cudaMalloc(&b->pbar, sizeof(unsigned) + sizeof(int)));
+    b->perr = reinterpret_cast<int *>(b->pbar + 1);
+    BCK(b, cudaMemsetAsync(b->pbar, 0, sizeof(unsigned) + sizeof(int), b->stream));
+    BCK(b, cudaHostAlloc(&b->perr_host, sizeof(int), cudaHostAllocDefault));
+    *b->perr_host = 0;
+    return LGCA_OK;
+}
+
+void wl_free(WorkList &w)
+{
+    cudaFree(w.dE);
+    cudaFree(w.dP);  // dB lives in the same allocation
+    cudaFree(w.dK);
+    cudaFree(w.base);
+    for (auto &sg : w.stage) {
+        if (sg.host) cudaFreeHost(sg.host);
+        if (sg.copied) cudaEventDestroy(sg.copied);
+    }
+}
+
+// Steps per pass of a member on the register wavefront, or 0: a member
+// whose kernel variant is the wavefront and whose depth the wavefront
+// supports for its model and width, when the call gives it a whole pass.
+int wave_depth(const lgca_lattice *h, int nsteps)
+{
+    if (h->variant != VARIANT_WAVE || nsteps < h->depth) return 0;
+    if (!(h->depth == 2 || h->depth == 4 || h->depth == 8)) return 0;
+    return wave_supported(h->model, h->g, h->depth) ? h->depth : 0;
 }
 
 }  // namespace
@@ -1096,9 +1252,6 @@ int lgca_batch_create(lgca_batch_handle *out)
     cudaGetDevice(&b->device);
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaMalloc(&b->s_base, sizeof(int));
-    for (auto &sg : b->stage)
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sg.copied, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         int st = bcuda(nullptr, e, "lgca_batch_create");
         lgca_batch_destroy(b);
@@ -1120,14 +1273,10 @@ int lgca_batch_destroy(lgca_batch_handle b)
         m->after_batch = false;
     }
     for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
-    cudaFree(b->dE);
-    cudaFree(b->dP);  // dB lives in the same allocation
-    cudaFree(b->dK);
-    cudaFree(b->s_base);
-    for (auto &sg : b->stage) {
-        if (sg.host) cudaFreeHost(sg.host);
-        if (sg.copied) cudaEventDestroy(sg.copied);
-    }
+    wl_free(b->main);
+    for (auto &w : b->wave) wl_free(w);
+    cudaFree(b->pbar);  // the error flag lives in the same allocation
+    if (b->perr_host) cudaFreeHost(b->perr_host);
     if (b->done) cudaEventDestroy(b->done);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -1231,19 +1380,25 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
                 if (nsteps[i] > 0) b->members[i]->after_batch = true;
         }
     } on_failure{b, nsteps};
+    // Members on the register wavefront (kernel variant 2, depth K) run
+    // nsteps % K single steps with the others, then nsteps / K passes of K
+    // steps; the rest run every step one launch at a time.
+    std::vector<int> K(nm, 0);
+    for (size_t i = 0; i < nm; ++i) K[i] = nsteps[i] > 0 ? wave_depth(b->members[i], nsteps[i]) : 0;
+    auto single_steps = [&](size_t i) { return K[i] ? nsteps[i] % K[i] : nsteps[i]; };
     // lane items per row of a member: word pairs where the width allows
     auto pair_of = [](const lgca_lattice *h) {
         return h->variant != VARIANT_PLAIN && h->wpt == 2 && (h->g.W % 64) == 0;
     };
-    // warp tasks per warp: the caller's choice, else 2 once the call's work
-    // fills at least four waves of resident warps at 2 tasks per warp (4
-    // blocks of 8 warps per SM), 4 for calls 16 times larger; small calls keep
-    // one task per warp for parallelism
+    // warp tasks per warp: the caller's choice, else 2 once the call's
+    // one-step work fills at least four waves of resident warps at 2 tasks per
+    // warp (4 blocks of 8 warps per SM), 4 for calls 16 times larger; small
+    // calls keep one task per warp for parallelism
     b->call_wt = b->warp_tasks;
     if (b->call_wt == 0) {
         long long all = 0;
         for (size_t i = 0; i < nm; ++i)
-            if (nsteps[i] > 0) {
+            if (single_steps(i) > 0) {
                 const lgca_lattice *h = b->members[i];
                 all += flat_tasks(h->g.H, pair_of(h) ? (h->g.nw + 1) / 2 : h->g.nw);
             }
@@ -1256,24 +1411,10 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         const int path = pair_of(h) ? ((h->g.nw & 1) ? 2 : 1) : 0;
         return fam * 9 + geom_mode(h) * 3 + path;
     };
-    // one work-list, lattices sorted by steps (descending: a segment's active
-    // members are a prefix), then by kernel code, so that the blocks resident
-    // at one time mostly run one code path (fewer instruction-cache misses)
-    std::vector<int> order(nm), code(nm);
-    for (size_t i = 0; i < nm; ++i) {
-        order[i] = (int)i;
-        code[i] = code_of(b->members[i]);
-    }
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-        return nsteps[x] != nsteps[y] ? nsteps[x] > nsteps[y] : code[x] < code[y];
-    });
-    b->E.clear();
-    b->P.assign(1, 0);
-    b->nsteps.clear();
-    size_t nkeys = 0;
-    for (int i : order) {
-        if (nsteps[i] == 0) continue;
-        lgca_lattice *h = b->members[i];
+    std::vector<int> code(nm);
+    for (size_t i = 0; i < nm; ++i) code[i] = code_of(b->members[i]);
+    auto entry_of = [&](size_t i) {
+        const lgca_lattice *h = b->members[i];
         BatchEntry e;
         memset(&e, 0, sizeof(e));
         e.a.solid = h->solid;
@@ -1283,105 +1424,122 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         e.a.chunks = (h->g.nw + 31) / 32;
         e.a.force_thr = h->force_thr;
         e.a.fx = h->force_x;
-        const bool pair = pair_of(h);
-        e.a.wpt = pair ? 2 : 1;
-        e.wpt = e.a.wpt;
         e.gm = geom_mode(h);
         e.code = code[i];
-        e.items = pair ? (h->g.nw + 1) / 2 : h->g.nw;  // lane items per row (last pair may be half)
-        e.a.fmagic = flat_magic(h->g.H, e.items);
         e.buf0 = h->buf[h->cur];
         e.buf1 = h->buf[h->cur ^ 1];
         e.seed = h->seed;
         e.t0 = h->t;
-        e.nsteps = nsteps[i];
-        e.keys = reinterpret_cast<uint64_t *>(nkeys);  // offset; rebased below
+        e.nsteps = nsteps[i];  // keys of all its steps in the call
+        return e;
+    };
+
+    // ---- one-step work-list: members sorted by single steps (descending:
+    // a segment's active members are a prefix), then by kernel code, so that
+    // the blocks resident at one time mostly run one code path; it holds the
+    // key table of every member stepping in the call
+    std::vector<int> order(nm);
+    for (size_t i = 0; i < nm; ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        const int sx = single_steps(x), sy = single_steps(y);
+        return sx != sy ? sx > sy : code[x] < code[y];
+    });
+    WorkList &M = b->main;
+    wl_clear(M);
+    const int per_block = 8 * b->call_wt;
+    size_t nkeys = 0;
+    std::vector<size_t> key_off(nm, 0);
+    for (int i : order) {
+        if (nsteps[i] == 0) continue;
+        const lgca_lattice *h = b->members[i];
+        BatchEntry e = entry_of(i);
+        const bool pair = pair_of(h);
+        e.a.wpt = pair ? 2 : 1;
+        e.wpt = e.a.wpt;
+        e.items = pair ? (h->g.nw + 1) / 2 : h->g.nw;  // lane items per row (last pair may be half)
+        e.a.fmagic = flat_magic(h->g.H, e.items);
+        key_off[i] = nkeys;
+        e.keys = reinterpret_cast<uint64_t *>(nkeys);  // offset; rebased on upload
         nkeys += 2 * (size_t)nsteps[i];
-        const long long own = flat_tasks(h->g.H, e.items);
-        e.task0 = b->P.back();
-        e.tasks = (int)std::min(own, 0x7fffffffLL);
-        const long long per_block = 8LL * b->call_wt;
-        const long long tasks = (long long)b->P.back() + (own + per_block - 1) / per_block * per_block;
-        if (tasks > 0x7fffffffLL) return bfail(b, LGCA_ERR_INVALID, "batch work-list too long");
-        b->E.push_back(e);
-        b->P.push_back((int)tasks);
-        b->nsteps.push_back(nsteps[i]);
+        const int n1 = single_steps(i);
+        const int st = wl_add(b, M, e, n1 > 0 ? flat_tasks(h->g.H, e.items) : 0, n1, per_block);
+        if (st) return st;
     }
-    const int ne = (int)b->E.size();
-    const int max_steps = ne ? b->nsteps[0] : 0;
-    if (ne > 0) {
-        const int total = b->P.back(), per_block = 8 * b->call_wt;
-        const int nblocks = total / per_block;  // every member's tasks fill whole blocks
-        b->Bl.resize(nblocks);
-        for (int l = 0; l < ne; ++l)
-            for (int blk = b->P[l] / per_block; blk < b->P[l + 1] / per_block; ++blk) b->Bl[blk] = l;
-        int st;
-        if ((st = grow(b, b->dE, b->capE, (size_t)ne)) != LGCA_OK) return st;
-        if ((st = grow(b, b->dP, b->capB, (size_t)ne + 1 + nblocks)) != LGCA_OK) return st;
-        if ((st = grow(b, b->dK, b->capK, nkeys)) != LGCA_OK) return st;
-        b->dB = b->dP + ne + 1;
-        for (auto &e : b->E) e.keys = b->dK + reinterpret_cast<size_t>(e.keys);
-        // work-list through a pinned slot: entries, then prefix and block map
-        // (contiguous on the device as on the host)
-        auto &sg = b->stage[b->slot];
-        b->slot ^= 1;
-        BCK(b, cudaEventSynchronize(sg.copied));
-        const size_t eb = (ne * sizeof(BatchEntry) + 15) & ~(size_t)15;
-        const size_t ib = ((size_t)ne + 1 + nblocks) * sizeof(int);
-        if (sg.cap < eb + ib) {
-            if (sg.host) cudaFreeHost(sg.host);
-            sg.host = nullptr;
-            sg.cap = 0;
-            BCK(b, cudaHostAlloc(&sg.host, 2 * (eb + ib), cudaHostAllocDefault));
-            sg.cap = 2 * (eb + ib);
+    if (!M.E.empty()) {
+        int st = wl_upload(b, M, per_block, nkeys);
+        if (st) return st;
+        int max_steps = 0;
+        for (const auto &e : M.E) max_steps = std::max(max_steps, e.nsteps);
+        BCK(b, launch_batch_keys(M.dE, (int)M.E.size(), max_steps, b->stream));
+    }
+    // ---- wavefront work-lists, one per depth: members sorted by passes
+    std::vector<int> worder[3];
+    for (int i : order)
+        for (int d = 0; d < 3; ++d)
+            if (K[i] == WAVE_DEPTHS[d]) worder[d].push_back(i);
+    for (int d = 0; d < 3; ++d) {
+        WorkList &Wl = b->wave[d];
+        wl_clear(Wl);
+        const int Kd = WAVE_DEPTHS[d];
+        std::stable_sort(worder[d].begin(), worder[d].end(), [&](int x, int y) {
+            return nsteps[x] / Kd != nsteps[y] / Kd ? nsteps[x] / Kd > nsteps[y] / Kd : code[x] < code[y];
+        });
+        for (int i : worder[d]) {
+            const lgca_lattice *h = b->members[i];
+            BatchEntry e = entry_of(i);
+            e.K = Kd;
+            e.r = nsteps[i] % Kd;
+            e.S = WAVE_SLAB_ROWS;
+            e.nstrips = (h->g.nw + 29) / 30;
+            e.keys = M.dK + key_off[i];
+            const long long own = (long long)e.nstrips * ((h->g.H + e.S - 1) / e.S);
+            const int st = wl_add(b, Wl, e, own, nsteps[i] / Kd, WAVE_BLOCK_WARPS);
+            if (st) return st;
         }
-        char *hp = static_cast<char *>(sg.host);
-        memcpy(hp, b->E.data(), ne * sizeof(BatchEntry));
-        memcpy(hp + eb, b->P.data(), (ne + 1) * sizeof(int));
-        memcpy(hp + eb + (ne + 1) * sizeof(int), b->Bl.data(), nblocks * sizeof(int));
-        BCK(b, cudaMemcpyAsync(b->dE, hp, ne * sizeof(BatchEntry), cudaMemcpyHostToDevice,
+        const int st = wl_upload(b, Wl, WAVE_BLOCK_WARPS, 0);
+        if (st) return st;
+    }
+
+    // ---- launches: the single steps of every member, then the passes
+    auto gmax_of = [](const WorkList &w, int k) {
+        int g = GEOM_NONE;  // the active entries are the first k
+        for (int i = 0; i < k; ++i) g = std::max(g, w.E[i].gm);
+        return g;
+    };
+    if (b->persistent) {
+        // one cooperative launch per segment, a grid barrier between steps
+        if (const int st = persist_state(b)) return st;
+        const int st = wl_run(b, M, 0, [&](int k, int tasks, int n, int u) -> int {
+            BCK(b, cudaMemsetAsync(b->pbar, 0, sizeof(unsigned), b->stream));
+            BCK(b, launch_batch_persist(M.dE, M.dB, tasks, u, n, b->pbar, b->perr, 2000000000ull,
+                                        gmax_of(M, k), b->call_wt, b->stream));
+            return LGCA_OK;
+        });
+        if (st) return st;
+        BCK(b, cudaMemcpyAsync(b->perr_host, b->perr, sizeof(int), cudaMemcpyDeviceToHost,
                                b->stream));
-        BCK(b, cudaMemcpyAsync(b->dP, hp + eb, ib, cudaMemcpyHostToDevice, b->stream));
-        BCK(b, cudaEventRecord(sg.copied, b->stream));
-        BCK(b, launch_batch_keys(b->dE, ne, max_steps, b->stream));
+    } else {
+        const int st = wl_run(b, M, b->graph_steps, [&](int k, int tasks, int n, int) -> int {
+            const int gmax = gmax_of(M, k);
+            for (int s = 0; s < n; ++s)
+                BCK(b, launch_batch(M.dE, M.dB, tasks, s, M.base, gmax, b->call_wt, b->stream));
+            BCK(b, launch_advance(M.base, n, b->stream));
+            return LGCA_OK;
+        });
+        if (st) return st;
     }
-    // segments of constant active sets: [s0, s1) where no lattice finishes
-    int s0 = 0;
-    while (s0 < max_steps) {
-        int k = 0;
-        while (k < ne && b->nsteps[k] > s0) ++k;
-        const int s1 = b->nsteps[k - 1], len = s1 - s0, tasks = b->P[k];
-        BCK(b, launch_set_base(b->s_base, s0, b->stream));
-        const int G = b->graph_steps > 0 ? std::min(b->graph_steps, len) : 0;
-        int done = 0;
-        if (G > 1 && len >= 2 * G) {
-            cudaGraph_t graph = nullptr;
-            cudaGraphExec_t exec = nullptr;
-            BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-            const int st = enqueue_steps(b, k, tasks, G);
-            cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
-            if (st != LGCA_OK) {
-                if (graph) cudaGraphDestroy(graph);
-                return st;
-            }
-            BCK(b, e);
-            e = cudaGraphInstantiate(&exec, graph, 0);
-            cudaGraphDestroy(graph);
-            BCK(b, e);
-            for (; done + G <= len; done += G) {
-                e = cudaGraphLaunch(exec, b->stream);
-                if (e != cudaSuccess) {
-                    cudaGraphExecDestroy(exec);
-                    return bcuda(b, e, "cudaGraphLaunch");
-                }
-            }
-            cudaGraphExecDestroy(exec);  // released once its queued launches complete
-        }
-        if (done < len) {
-            const int st = enqueue_steps(b, k, tasks, len - done);
-            if (st != LGCA_OK) return st;
-        }
-        s0 = s1;
+    for (int d = 0; d < 3; ++d) {
+        WorkList &Wl = b->wave[d];
+        const int Kd = WAVE_DEPTHS[d];
+        const int per_graph = b->graph_steps > 0 ? std::max(1, b->graph_steps / Kd) : 0;
+        const int st = wl_run(b, Wl, per_graph, [&](int k, int tasks, int n, int) -> int {
+            const int gmax = gmax_of(Wl, k);
+            for (int j = 0; j < n; ++j)
+                BCK(b, launch_batch_wave(Wl.dE, Wl.dB, tasks, j, Wl.base, gmax, Kd, b->stream));
+            BCK(b, launch_advance(Wl.base, n, b->stream));
+            return LGCA_OK;
+        });
+        if (st) return st;
     }
     // members continue after the batch: each member's stream waits on `done`
     // at its next use (enter); `done` is recorded again by later calls, which
@@ -1391,7 +1549,9 @@ int lgca_batch_step_each(lgca_batch_handle b, const int *nsteps)
         if (nsteps[i] == 0) continue;
         lgca_lattice *h = b->members[i];
         h->after_batch = true;
-        if (nsteps[i] & 1) h->cur ^= 1;
+        // buffer swaps: one per single step and one per pass
+        const int swaps = K[i] ? nsteps[i] % K[i] + nsteps[i] / K[i] : nsteps[i];
+        if (swaps & 1) h->cur ^= 1;
         h->t += (uint64_t)nsteps[i];
     }
     on_failure.armed = false;
@@ -1410,6 +1570,22 @@ int lgca_batch_sync(lgca_batch_handle b)
     if (!b) return bfail(nullptr, LGCA_ERR_INVALID, "invalid batch");
     DeviceGuard dg(b->device);
     BCK(b, cudaStreamSynchronize(b->stream));
+    if (b->perr_host && *b->perr_host) {
+        // reported once; the device flag is cleared for the next calls
+        *b->perr_host = 0;
+        BCK(b, cudaMemsetAsync(b->perr, 0, sizeof(int), b->stream));
+        BCK(b, cudaStreamSynchronize(b->stream));
+        return bfail(b, LGCA_ERR_TIMEOUT,
+                     "a grid barrier of the persistent batch kernel timed out; the members' states "
+                     "are unspecified");
+    }
+    return LGCA_OK;
+}
+
+int lgca_batch_set_persistent(lgca_batch_handle b, int on)
+{
+    if (!b || !(on == 0 || on == 1)) return bfail(b, LGCA_ERR_INVALID, "persistent must be 0 or 1");
+    b->persistent = on;
     return LGCA_OK;
 }
 

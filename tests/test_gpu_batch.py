@@ -179,3 +179,76 @@ def test_membership_rules(gpu):
         B1.step(5)
         assert np.array_equal(b.download(), want)
     b.close()
+
+
+@pytest.mark.parametrize("graph_steps", [0, 32])
+def test_batch_with_wavefront_members_equals_alone(gpu, graph_steps):
+    """Members on the register wavefront (kernel variant 2, depth 2, 4 or 8)
+    run their single steps with the others and then passes of K steps; mixed
+    with one-step members, every member equals its lone run."""
+    rng = np.random.default_rng(100 + graph_steps)
+    jobs = make_jobs(gpu, 20, rng, max_side=900)
+    for i, (model, W, H) in enumerate([(0, 3200, 200), (1, 2048, 130), (3, 1984, 96)]):
+        # several strips of 30 words per row, several slabs
+        L = gpu.GpuLattice(model, W, H, seed=77 + i)
+        L.set_cell_types(GEOMS[i](W, H))
+        L.init_random(0.3, 0.3)
+        L.set_forcing_column(int(rng.integers(W)), 0.05)
+        jobs.append(L)
+    depths = []
+    for L in jobs:
+        K = int(rng.choice([1, 2, 4, 8]))
+        if K > 1:
+            L.set_kernel_variant(2)
+            L.set_temporal_depth(K)
+        depths.append(K)
+    steps = [int(x) for x in rng.integers(0, 150, len(jobs))]
+    steps[0] = 150
+    want = []
+    for L, n in zip(jobs, steps):
+        twin = gpu.GpuLattice(L.model, L.dim_x, L.dim_y)
+        twin.restore(L.checkpoint())
+        twin.set_kernel_variant(1)  # one step per pass, one word per lane
+        twin.collide_and_propagate(n)
+        want.append((twin.download(), twin.step_count))
+        twin.close()
+    with gpu.GpuBatch(graph_steps=graph_steps) as B:
+        for L in jobs:
+            B.add(L)
+        B.step_each(steps)
+        for L, (w, t), K in zip(jobs, want, depths):
+            assert L.step_count == t
+            assert np.array_equal(L.download(), w), (L.model, L.dim_x, L.dim_y, K)
+        # a second call continues from the first on every path
+        B.step_each([7] * len(jobs))
+    for L in jobs:
+        L.close()
+
+
+@pytest.mark.parametrize("warp_tasks", [1, 2])
+def test_persistent_batch_equals_alone(gpu, warp_tasks):
+    """The persistent form (one cooperative launch per stretch of steps with
+    an unchanged member set, a grid barrier between steps) gives every member
+    the bits of its lone run, also when members leave part way."""
+    rng = np.random.default_rng(200 + warp_tasks)
+    jobs = make_jobs(gpu, 24, rng)
+    steps = [int(x) for x in rng.integers(0, 90, len(jobs))]
+    steps[0] = 90
+    want = []
+    for L, n in zip(jobs, steps):
+        twin = gpu.GpuLattice(L.model, L.dim_x, L.dim_y)
+        twin.restore(L.checkpoint())
+        twin.collide_and_propagate(n)
+        want.append(twin.download())
+        twin.close()
+    with gpu.GpuBatch() as B:
+        B.set_persistent(True)
+        B.set_warp_tasks(warp_tasks)
+        for L in jobs:
+            B.add(L)
+        B.step_each(steps)
+        B.sync()
+        for L, w in zip(jobs, want):
+            assert np.array_equal(L.download(), w), (L.model, L.dim_x, L.dim_y)
+    for L in jobs:
+        L.close()

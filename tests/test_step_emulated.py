@@ -223,19 +223,21 @@ def batch_emu(tmp_path_factory):
 
 
 def test_emulated_batch_kernel_equals_oracle(batch_emu, tmp_path, oracle):
-    """k_batch_keys and k_batch on their grids, with the call's work-list:
-    random mixed batches (models, pair / odd / one-word widths, geometries
-    with cell-type noise, forcing, start steps, 0 to 6 steps per member so
-    members leave the work-list part way) at 1, 2, 4 and 8 tasks per warp;
-    every member equals its lone oracle run."""
+    """k_batch_keys, k_batch and k_batch_wave on their grids, with the
+    call's work-lists: random mixed batches (models, pair / odd / one-word
+    widths, geometries with cell-type noise, forcing, start steps, 0 to 6
+    steps per member so members leave the work-list part way) at 1, 2, 4 and
+    8 tasks per warp, then batches whose members ask for 2, 4 or 8 steps per
+    pass (single steps first, then passes, several slabs per member); every
+    member equals its lone oracle run."""
     rng = np.random.default_rng(77)
-    for trial in range(16):
+    for trial in range(32):
         wt = (1, 2, 4, 8)[trial % 4]
         mem = []
         for _ in range(int(rng.integers(1, 10))):
             model = int(rng.integers(4))
             W = 64 * int(rng.integers(1, 10)) if rng.random() < 0.7 else int(rng.integers(1, 400))
-            H = 2 * int(rng.integers(1, 24))
+            H = 2 * int(rng.integers(1, 24 if trial < 16 else 80))
             kind = int(rng.integers(4))
             types = [G.periodic(W, H), G.pipe(W, H), G.reflecting(W, H, "forward"),
                      rng.choice([0, 0, 0, 1, 2], size=(H, W))][kind]
@@ -244,20 +246,24 @@ def test_emulated_batch_kernel_equals_oracle(batch_emu, tmp_path, oracle):
                                        p_move=0.3, p_rest=0.3)
             fx = int(rng.integers(W)) if rng.random() < 0.6 else -1
             p = float(rng.uniform(0.05, 1.0))
-            mem.append((model, W, H, int(rng.integers(0, 7)), fx, int(rng.integers(1 << 40)),
-                        int(rng.integers(1 << 20)), p, st, types))
+            # from trial 16 on, members ask for the wavefront (2, 4 or 8 steps
+            # per pass; those it does not apply to run one step per launch)
+            K = int(rng.choice([0, 2, 4, 8])) if trial >= 16 else 0
+            n = int(rng.integers(0, 7)) if trial < 16 else int(rng.integers(0, 20))
+            mem.append((model, W, H, n, fx, int(rng.integers(1 << 40)),
+                        int(rng.integers(1 << 20)), p, st, types, K))
         inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
         with open(inp, "wb") as f:
             f.write(struct.pack("<2i", len(mem), wt))
-            for model, W, H, n, fx, seed, t0, p, st, types in mem:
+            for model, W, H, n, fx, seed, t0, p, st, types, K in mem:
                 thr = oracle.prob_threshold(p) if fx >= 0 else 0
-                f.write(struct.pack("<5i3Q", model, W, H, n, fx, seed, t0, thr))
+                f.write(struct.pack("<6i3Q", model, W, H, n, fx, K, seed, t0, thr))
                 f.write(st.tobytes())
                 f.write(types.astype(np.uint8).tobytes())
         r = subprocess.run([str(batch_emu), str(inp), str(out)], capture_output=True)
         assert r.returncode == 0, r.returncode
         data, off = out.read_bytes(), 0
-        for model, W, H, n, fx, seed, t0, p, st, types in mem:
+        for model, W, H, n, fx, seed, t0, p, st, types, K in mem:
             got = np.frombuffer(data[off:off + W * H], np.uint8).reshape(H, W)
             off += W * H
             want = oracle.run(model, st, n, types=types, seed=seed, t0=t0, force_x=fx,
