@@ -314,13 +314,14 @@ int lgca_batch_set_graph_steps(lgca_batch_handle b, int steps_per_graph); /* 0: 
  * 1 G sites); fewer give more parallelism to small calls.  A tuning knob:
  * results do not depend on it.  (No reference counterpart.) */
 int lgca_batch_set_warp_tasks(lgca_batch_handle b, int n);
-/* Persistent form (on = 1): the one-step work of each call runs as one
- * cooperative launch per stretch of steps with an unchanged set of members,
- * the resident blocks walking the work-list with a grid barrier between
- * steps, instead of one launch per step (on = 0, default).  A barrier wait
- * is bounded (2 s): when one gives up, the next lgca_batch_sync returns
- * LGCA_ERR_TIMEOUT once and the members' states are unspecified.  Results do
- * not depend on the form.  (No reference counterpart.) */
+/* Persistent form (on = 1, default): the one-step work of each call runs as
+ * one cooperative launch per stretch of steps with an unchanged set of
+ * members, the resident blocks walking the work-list with a grid barrier
+ * between steps; on = 0 makes one launch per step, captured in CUDA graphs
+ * (lgca_batch_set_graph_steps).  A barrier wait is bounded (2 s): when one
+ * gives up, the next lgca_batch_sync returns LGCA_ERR_TIMEOUT once and the
+ * members' states are unspecified.  Results do not depend on the form.
+ * (No reference counterpart.) */
 int lgca_batch_set_persistent(lgca_batch_handle b, int on);
 int lgca_batch_sync(lgca_batch_handle b);
 const char *lgca_batch_last_error(lgca_batch_handle b);

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(32 * WAVE_BLOCK_WARPS)
     const BatchEntry &e = E[block_lat[blockIdx.x]];
     const int local = blockIdx.x * WAVE_BLOCK_WARPS + (int)(threadIdx.x >> 5) - e.task0;
     const int j = *j_base + j_local;
-    const TableKeys keys{e.keys + 2 * (e.r + j * K)};
+    const TableKeys<K> keys(e.keys + 2 * (e.r + j * K));
     const bool odd = ((e.r + j) & 1) != 0;
     const uint64_t *src = odd ? e.buf1 : e.buf0;
     uint64_t *dst = odd ? e.buf0 : e.buf1;

@@ -1047,10 +1047,11 @@ struct lgca_batch {
     int call_wt = 1;             // the value used by the current call
     WorkList main;               // one step per launch (k_batch), all members' keys
     WorkList wave[3];            // passes of 2, 4, 8 steps (k_batch_wave)
-    // persistent form of the one-step work: one cooperative launch per
-    // segment, grid barrier counter and error flag (device), the flag's
-    // pinned copy read by lgca_batch_sync
-    int persistent = 0;
+    // persistent form of the one-step work (the default: on the 512-lattice
+    // mix a step took 0.257 ms against 0.274 ms with one launch per step):
+    // one cooperative launch per segment, grid barrier counter and error flag
+    // (device), the flag's pinned copy read by lgca_batch_sync
+    int persistent = 1;
     unsigned *pbar = nullptr;
     int *perr = nullptr, *perr_host = nullptr;
     std::string err;

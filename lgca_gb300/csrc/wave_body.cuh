@@ -32,10 +32,18 @@ struct ParamKeys {
     __device__ __forceinline__ uint64_t chir(int L) const { return m.chir_keys[L]; }
     __device__ __forceinline__ uint64_t force(int L) const { return m.force_keys[L]; }
 };
-struct TableKeys {
-    const uint64_t *p;  // keys of the pass's first step
-    __device__ __forceinline__ uint64_t chir(int L) const { return __ldg(p + 2 * L); }
-    __device__ __forceinline__ uint64_t force(int L) const { return __ldg(p + 2 * L + 1); }
+template <int K> struct TableKeys {
+    uint64_t c[K], f[K];  // held in registers for the whole pass
+    __device__ __forceinline__ explicit TableKeys(const uint64_t *p)  // keys of the pass's first step
+    {
+#pragma unroll
+        for (int L = 0; L < K; ++L) {
+            c[L] = __ldg(p + 2 * L);
+            f[L] = __ldg(p + 2 * L + 1);
+        }
+    }
+    __device__ __forceinline__ uint64_t chir(int L) const { return c[L]; }
+    __device__ __forceinline__ uint64_t force(int L) const { return f[L]; }
 };
 
 // One warp's strip sx (30 output words) and slab sy (S output rows) of a

@@ -49,6 +49,7 @@ def test_mixed_batch_equals_alone(gpu, graph_steps, warp_tasks):
         want.append((twin.download(), twin.step_count))
         twin.close()
     with gpu.GpuBatch(graph_steps=graph_steps) as B:
+        B.set_persistent(graph_steps == 0)  # graphs belong to the one-launch-per-step form
         B.set_warp_tasks(warp_tasks)
         for L in jobs:
             B.add(L)
@@ -225,7 +226,7 @@ def test_batch_with_wavefront_members_equals_alone(gpu, graph_steps):
         L.close()
 
 
-@pytest.mark.parametrize("warp_tasks", [1, 2])
+@pytest.mark.parametrize("warp_tasks", [1, 2, 4])
 def test_persistent_batch_equals_alone(gpu, warp_tasks):
     """The persistent form (one cooperative launch per stretch of steps with
     an unchanged member set, a grid barrier between steps) gives every member
@@ -252,3 +253,18 @@ def test_persistent_batch_equals_alone(gpu, warp_tasks):
             assert np.array_equal(L.download(), w), (L.model, L.dim_x, L.dim_y)
     for L in jobs:
         L.close()
+
+
+def test_batched_workload_equals_oracle(gpu):
+    """The batched workload at full size -- 512 lattices of 256..4096 x
+    256..4096 sites, the four models, periodic / pipe with forcing / disc,
+    1000 steps -- run as one batch with the autotuned kernels: every job's
+    final state equals its lone oracle run (hashes in the fixture)."""
+    from conftest import load_json
+    from lgca_gb300 import batched as BT
+    g = load_json("batched_512.json")
+    jobs = BT.make_jobs(512)
+    assert jobs == g["jobs"] and g["steps"] == 1000
+    _, hashes, _ = BT.run_batched(jobs, 1000, tune=True)
+    bad = [i for i, (a, b) in enumerate(zip(hashes, g["final_sha"])) if a != b]
+    assert len(hashes) == 512 and not bad, bad[:10]
