@@ -3,8 +3,9 @@ self-contained program for profilers (ncu) and for quick timings.
 
     python -m lgca_gb300.profile_case --model 3 --W 32768 --H 16384 --steps 3
     python -m lgca_gb300.profile_case --geometry karman --W 8192 --H 2048 --force-x 16 --force-p 0.02
+    python -m lgca_gb300.profile_case --batch 512 --steps 4   # the batched workload, one step per call
 
-Prints the average time per step measured with CUDA events.
+Prints the average time per step (host clock around the steps and a wait).
 """
 from __future__ import annotations
 
@@ -30,9 +31,35 @@ def main(argv=None):
     ap.add_argument("--force-p", type=float, default=0.0)
     ap.add_argument("--p", type=float, default=0.5)
     ap.add_argument("--block", type=int, default=0, help="also compute BxB block sums per step")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="run the first N jobs of the batched workload as one batch instead")
+    ap.add_argument("--launches", action="store_true",
+                    help="(with --batch) one launch per step instead of the persistent form")
     args = ap.parse_args(argv)
 
     gpu.build()
+    if args.batch:
+        from lgca_gb300 import batched as BT
+        jobs = BT.make_jobs(args.batch)
+        lats = [BT.build(j) for j in jobs]
+        with gpu.GpuBatch() as B:
+            B.set_persistent(not args.launches)
+            for L in lats:
+                B.add(L)
+            for _ in range(args.warmup):
+                B.step(1)
+            B.sync()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                B.step(1)
+            B.sync()
+            dt = time.perf_counter() - t0
+        sites = sum(j["W"] * j["H"] for j in jobs)
+        print(f"batch of {args.batch}: {dt / args.steps * 1e3:.4f} ms/step (host clock), "
+              f"{sites * args.steps / dt / 1e9:.1f} GSite-updates/s")
+        for L in lats:
+            L.close()
+        return
     L = gpu.GpuLattice(args.model, args.W, args.H, seed=3)
     if args.geometry == "pipe":
         L.set_cell_types(G.pipe(args.W, args.H))
