@@ -63,17 +63,21 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(name):
-    """Per-launch DRAM bytes from a committed ncu summary (line
-    `traffic_bytes_per_launch: N`), or None."""
+def profiled_value(name, key="traffic_bytes_per_launch"):
+    """A per-launch figure from a committed ncu summary (a line `key: N`, e.g.
+    DRAM bytes or warp instructions per launch), or None."""
     path = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(path):
-            if line.strip().startswith("traffic_bytes_per_launch:"):
+            if line.strip().startswith(key + ":"):
                 return float(line.split(":", 1)[1])
     except OSError:
         pass
     return None
+
+
+def profiled_traffic(name):
+    return profiled_value(name, "traffic_bytes_per_launch")
 
 
 class ClockSampler:
@@ -229,6 +233,16 @@ def oracle_check(final_sha):
             "oracle_all_equal": same == len(want) == len(final_sha)}
 
 
+def batched_bytes_per_step():
+    """Algorithmic bytes of one step of the 512-job batched workload."""
+    from lgca_gb300 import batched as BT
+    total = 0.0
+    for j in BT.make_jobs(512):
+        D = {0: 4, 1: 6, 2: 7, 3: 7}[j["model"]]
+        total += j["W"] * j["H"] * (2 * D / 8 + (1 / 8 if j["geometry"] != "periodic" else 0))
+    return total
+
+
 def served_leg(rate, duration):
     """The served workload, bounded: Poisson arrivals at `rate` jobs/s for
     `duration` s (sizes 256x256..8192x4096, 100..20000 steps, 16x16 fields
@@ -328,7 +342,21 @@ def run_ours(args):
                 "frac": achieved / hbm_peak, "traffic": profiled_traffic("step_fhp3_karman_8192x2048.md"),
                 "peak_kind": peak_kind, "kernel": "k_step2<FHP_II/III, GEOM_NOSLIP> (two words per lane)",
                 "bytes_per_launch": bytes_launch,
-                "note": "state (2 x 14.7 MB) + solid plane stay L2-resident within a step chunk"}
+                "note": "state (2 x 14.7 MB) + solid plane stay L2-resident within a step chunk, so "
+                        "this is algorithmic bytes over time, not DRAM traffic; the kernel's bound "
+                        "is ALU issue (see alu_issue); the HBM gate is roofline_gate"}
+    # the same launches against the SMs' instruction issue: warp instructions
+    # per launch (ncu, committed summary) over the launch time, against one
+    # warp instruction per clock per SM sub-partition at the sampled clock
+    inst = profiled_value("step_fhp3_karman_8192x2048.md", "inst_per_launch")
+    if inst:
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        clk_hz = (clk.summary().get("sm_mhz") or 2070) * 1e6
+        roofline["alu_issue"] = {
+            "achieved": inst / launch_s, "peak": sms * 4 * clk_hz, "unit": "warp-instructions/s",
+            "frac": inst / launch_s / (sms * 4 * clk_hz), "inst_per_launch": inst,
+            "note": "ALU pipe 71 % and issue 59 % busy while SMs are active (ncu); the ALU "
+                    "pipe runs logic at half the issue rate"}
 
     # end to end through the C ABI with host buffers: every bench step is one
     # job -- upload the input state from pinned memory, 100 lattice steps,
@@ -395,6 +423,16 @@ def run_ours(args):
         batched = BT.compare(512, 1000, tune=True)
         batched.pop("tuned", None)
         batched.update(oracle_check(batched.pop("final_sha")))
+        # HBM roofline of the batched kernel: algorithmic bytes of one step of
+        # all members (2 D/8 B per site, + 1/8 B with a solid plane) per step time
+        step_s = batched["batched_s"] / batched["steps"]
+        bytes_step = batched_bytes_per_step()
+        batched["roofline"] = {"bound": "hbm", "achieved": bytes_step / step_s / 1e9,
+                               "peak": hbm_peak, "unit": "GB/s",
+                               "frac": bytes_step / step_s / 1e9 / hbm_peak,
+                               "bytes_per_step": bytes_step,
+                               "traffic": profiled_traffic("batch_512_mixed.md"),
+                               "kernel": "k_batch_persist (persistent form, grid barrier per step)"}
     served = None
     if rank == 0 and not args.no_served:
         served = served_leg(args.served_rate, args.served_duration)
