@@ -24,6 +24,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liblgca_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_oracle.so")
+# The reference checkout the harness is compiled from: $LGCA_REFERENCE_DIR, by
+# default the path of the build machine's read-only copy.  The recipe names
+# this path in this one place; the GPU machine has no copy and only uses the
+# restatement and the committed fixtures.
 REFERENCE_DIR = os.environ.get("LGCA_REFERENCE_DIR", "/root/reference")
 
 HPP, FHP_I, FHP_II, FHP_III = 0, 1, 2, 3
