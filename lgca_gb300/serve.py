@@ -412,14 +412,20 @@ class Server:
         }
 
 
-def fcfs_baseline(jobs, step_time) -> dict:
+def fcfs_baseline(jobs, step_time, out_every: int = 500) -> dict:
     """First-come-first-served single-lattice execution of the same jobs: one
     job at a time, each taking steps * step_time(job) seconds (step times of
-    the plain kernel measured on the GPU), queueing simulated exactly."""
+    the plain kernel measured on the GPU) plus, when step_time measured them,
+    the job's own costs -- creating and initialising its lattice once and
+    copying its fields back every out_every steps and at its end -- with
+    queueing simulated exactly."""
+    overhead = getattr(step_time, "job_overhead", None)
     t, lat, busy = 0.0, [], 0.0
     for j in sorted(jobs, key=lambda j: j.arrival):
         start = max(t, j.arrival)
         service = j.steps * step_time(j)
+        if overhead is not None:
+            service += overhead(j, -(-j.steps // out_every))
         t = start + service
         busy += service
         lat.append(t - j.arrival)
@@ -431,21 +437,35 @@ def fcfs_baseline(jobs, step_time) -> dict:
 
 class StepTimeTable:
     """Per-step time of the plain single-lattice kernel by (model, W, H),
-    measured once per shape class on the GPU and interpolated by site count.
+    measured once per shape class on the GPU and interpolated by site count,
+    and the per-job costs around the steps.
 
     Each point is the wall time of `steps` steps of a lattice run alone
     (launches included), repeated `repeats` times: `stat` "median" uses the
-    median repeat, "best" the fastest (the baseline at its best)."""
+    median repeat, "best" the fastest (the baseline at its best).  Each point
+    also holds the wall time of setting a job's lattice up (create, pipe
+    walls painted, occupation drawn, waited for) and of one field output
+    (16 x 16 block sums copied to the host), medians of `repeats`."""
 
     def __init__(self, samples_per_model=(256, 512, 1024, 2048, 4096, 8192), steps: int = 50,
                  repeats: int = 5, stat: str = "median"):
         import lgca_gb300 as gpu
         self.stat = stat
         self.samples = {}  # model -> [(sites, [seconds per step of each repeat])]
+        self.costs = {}    # model -> [(sites, setup seconds, output seconds)]
         for m in range(4):
-            pts = []
+            pts, costs = [], []
             for s in samples_per_model:
                 W, H = s, max(256, s // 2)
+                setup = []
+                for _ in range(repeats):
+                    t0 = time.perf_counter()
+                    L = gpu.GpuLattice(m, W, H, seed=1)
+                    L.apply_bc_pipe()
+                    L.init_random(0.25, 0.25)
+                    L.sync()
+                    setup.append(time.perf_counter() - t0)
+                    L.close()
                 L = gpu.GpuLattice(m, W, H, seed=1)
                 L.init_random(0.25, 0.25)
                 L.set_kernel_variant(0)  # the plain kernel: one step per pass, its fastest form
@@ -457,14 +477,22 @@ class StepTimeTable:
                     L.collide_and_propagate(steps)
                     L.sync()
                     reps.append((time.perf_counter() - t0) / steps)
+                out = []
+                for _ in range(repeats):
+                    t0 = time.perf_counter()
+                    L.block_sums(16)
+                    out.append(time.perf_counter() - t0)
                 pts.append((W * H, reps))
+                costs.append((W * H, float(np.median(setup)), float(np.median(out))))
                 L.close()
             self.samples[m] = pts
+            self.costs[m] = costs
 
     def with_stat(self, stat: str) -> "StepTimeTable":
         """The same samples read with another statistic."""
         other = object.__new__(StepTimeTable)
         other.samples, other.stat = self.samples, stat
+        other.costs = getattr(self, "costs", {})
         return other
 
     def __call__(self, job: Job) -> float:
@@ -473,6 +501,17 @@ class StepTimeTable:
         xs = np.log([p[0] for p in pts])
         ys = np.log([f(p[1]) for p in pts])
         return float(np.exp(np.interp(math.log(job.sites), xs, ys)))
+
+    def job_overhead(self, job: Job, outputs: int) -> float:
+        """Seconds a job spends outside its steps when run alone: set-up and
+        `outputs` field copies (0 without measured costs)."""
+        costs = getattr(self, "costs", {}).get(job.model)
+        if not costs:
+            return 0.0
+        xs = np.log([c[0] for c in costs])
+        setup = float(np.exp(np.interp(math.log(job.sites), xs, np.log([c[1] for c in costs]))))
+        out = float(np.exp(np.interp(math.log(job.sites), xs, np.log([c[2] for c in costs]))))
+        return setup + outputs * out
 
 
 def build_alone(job: Job):
@@ -595,7 +634,7 @@ def serve(rate: float, duration: float, budget: float = 150e9, drain_limit: floa
         # prediction for the same jobs
         meas = fcfs_measured(jobs, fcfs_sample)
         sel = sorted(jobs, key=lambda j: j.arrival)[:fcfs_sample]
-        pred = sum(j.steps * table(j) for j in sel)
+        pred = sum(j.steps * table(j) + table.job_overhead(j, -(-j.steps // 500)) for j in sel)
         meas["table_predicted_seconds"] = pred
         meas["table_gsite_updates_s"] = meas["site_updates"] / pred / 1e9 if pred else 0.0
         rep["fcfs_measured"] = meas

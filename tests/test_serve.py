@@ -193,6 +193,12 @@ def test_step_time_table_statistics():
     assert t(job) == pytest.approx((2e-6 * 2e-4) ** 0.5)
     assert t.with_stat("best")(job) == pytest.approx((1e-6 * 1e-4) ** 0.5)
     assert t.stat == "median"
+    # per-job costs: set-up plus one field copy per output, interpolated alike
+    assert t.job_overhead(job, 3) == 0.0  # no measured costs
+    t.costs = {m: [(1000, 1e-3, 1e-5), (100000, 1e-1, 1e-3)] for m in range(4)}
+    assert t.job_overhead(job, 3) == pytest.approx(1e-2 + 3 * 1e-4)
+    base = S.fcfs_baseline([job], t)  # 10 steps + set-up + one output
+    assert base["makespan_s"] == pytest.approx(10 * t(job) + 1e-2 + 1e-4)
 
 
 def test_job_stream_shapes():
