@@ -129,10 +129,19 @@ def test_config_pipe_fhp1_1024x512_1000_steps(gpu):
     assert np.array_equal(N, g["N"]) and np.array_equal(Jx2, g["Jx2"]) and np.array_equal(Jy, g["Jy"])
 
 
-def test_config_karman_fhp3_8192x2048(gpu):
-    """BASELINE workload 2 at full size: the first 200 steps bit-exact with the
-    reference (its CPU run is pinned at 100 and 200 steps)."""
+def blocksum_sha(N, Jx2, Jy):
+    return sha(np.stack([N.astype(np.int32), Jx2.astype(np.int32), Jy.astype(np.int32)]))
+
+
+def run_karman_config(gpu, depth=1, variant=0):
+    """BASELINE workload 2 over its whole run: FHP-III 8192x2048, disc r=128
+    at (1024,1024), forcing column x=16 p=0.02, 10000 steps, 32x32 block sums
+    every 100 steps.  Asserted against the reference run: the full block sums
+    at t=100 and t=200, the hash of every one of the 100 block-sum sets and
+    the state hash every 1000 steps."""
     pins = load_json("config_pins.json")["karman_fhp3_8192x2048"]
+    long = load_json("config_karman_long.json")
+    assert long["engine"] == "ref" and long["steps"] == 10000
     g = load_npz("config_karman_blocksums.npz")
     W, H = 8192, 2048
     types = G.disc(W, H, 1024, 1024, 128)
@@ -140,21 +149,33 @@ def test_config_karman_fhp3_8192x2048(gpu):
     with gpu.GpuLattice(3, W, H, seed=2) as L:
         L.set_cell_types(types)
         L.init_random(0.3, 0.3)
-        assert sha(L.download()) == pins["init_sha"]
+        assert sha(L.download()) == pins["init_sha"] == long["init_sha"]
         L.set_forcing_column(16, 0.02)
+        L.set_temporal_depth(depth)
+        L.set_kernel_variant(variant)
         n0 = L.count_particles()
-        for tag in ("t100", "t200"):
+        checked = 0
+        for t in range(100, 10001, 100):
             L.collide_and_propagate(100)
-            assert sha(L.download()) == pins[f"{tag}_sha"], tag
             N, Jx2, Jy = L.block_sums(32)
-            assert np.array_equal(N, g[f"{tag}_N"]) and np.array_equal(Jx2, g[f"{tag}_Jx2"])
-            assert np.array_equal(Jy, g[f"{tag}_Jy"])
-        # the remaining steps of the 10000-step run: forcing only turns
-        # particles around, walls and the disc reflect them, so mass is conserved
-        L.collide_and_propagate(9800)
+            assert blocksum_sha(N, Jx2, Jy) == long["blocksum_sha"][str(t)], t
+            assert [int(N.sum()), int(Jx2.sum()), int(Jy.sum())] == long["blocksum_total"][t // 100 - 1]
+            if t in (100, 200):
+                tag = f"t{t}"
+                assert np.array_equal(N, g[f"{tag}_N"]) and np.array_equal(Jx2, g[f"{tag}_Jx2"])
+                assert np.array_equal(Jy, g[f"{tag}_Jy"])
+                assert sha(L.download()) == pins[f"{tag}_sha"]
+            if t % 1000 == 0:
+                assert sha(L.download()) == long["state_sha"][str(t)], t
+            checked += 1
+        # forcing turns particles around, walls and the disc reflect them
         assert L.count_particles() == n0
-        N, _, _ = L.block_sums(32)
-        assert int(N.sum()) == n0
+    assert checked == 100
+
+
+def test_config_karman_fhp3_8192x2048(gpu):
+    """The plain kernel over the whole Karman run, bit-exact with the reference."""
+    run_karman_config(gpu)
 
 
 @pytest.mark.parametrize("model", MODELS)
@@ -215,19 +236,9 @@ def test_temporal_blocking_frozen_chirality(gpu, oracle, model, variant):
 @pytest.mark.parametrize("depth", [2, 4, 8])
 @pytest.mark.parametrize("variant", [2, 3, 4])
 def test_temporal_blocking_karman_config(gpu, depth, variant):
-    """Full-size Karman workload with k steps per pass: pinned reference states."""
-    pins = load_json("config_pins.json")["karman_fhp3_8192x2048"]
-    W, H = 8192, 2048
-    with gpu.GpuLattice(3, W, H, seed=2) as L:
-        L.set_cell_types(G.disc(W, H, 1024, 1024, 128))
-        L.init_random(0.3, 0.3)
-        L.set_forcing_column(16, 0.02)
-        L.set_temporal_depth(depth)
-        L.set_kernel_variant(variant)
-        L.collide_and_propagate(100)
-        assert sha(L.download()) == pins["t100_sha"]
-        L.collide_and_propagate(100)
-        assert sha(L.download()) == pins["t200_sha"]
+    """The whole Karman run with k steps per pass (register wavefront, shared-
+    memory tiles) and with the persistent kernel: the same reference pins."""
+    run_karman_config(gpu, depth=depth, variant=variant)
 
 
 @pytest.mark.parametrize("model", MODELS)
