@@ -3,11 +3,13 @@
 Runs the unmodified reference OMP_Lattice (keva92/lgca src/lattice.cpp,
 src/omp_lattice.cpp) through the hook harness oracle/ref_harness.cpp, built
 from the reference sources by `make -C oracle ref`.  Needs the reference
-checkout (LGCA_REFERENCE_DIR, default /root/reference); the fixtures it
+checkout that oracle/oracle.py names (LGCA_REFERENCE_DIR); the fixtures it
 writes are committed so that the tests run without it.
 
     python tests/golden/gen_golden.py            # small fixtures (seconds)
     python tests/golden/gen_golden.py --configs  # + full-size workload pins (minutes)
+    python tests/golden/gen_golden.py --karman-long ref  # Karman workload, 10000 steps (about 50 min)
+    python tests/golden/gen_golden.py --batched  # batched workload, 512 jobs x 1000 steps (about 90 min)
 """
 from __future__ import annotations
 

@@ -155,6 +155,34 @@ def test_config_pipe_pin(oracle):
     assert np.array_equal(N, g["N"]) and np.array_equal(Jx2, g["Jx2"]) and np.array_equal(Jy, g["Jy"])
 
 
+def test_batched_fixture_matches_workload_and_oracle(oracle):
+    """The batched-workload fixture lists exactly the jobs the batched form
+    builds, and its hashes are the oracle's: the smallest job of each model
+    and geometry is re-run here for the full 1000 steps."""
+    from lgca_gb300 import batched as BT
+    g = load_json("batched_512.json")
+    jobs = BT.make_jobs(512)
+    assert g["jobs"] == jobs and g["steps"] == 1000 and len(g["final_sha"]) == 512
+    smallest = {}
+    for j in jobs:
+        k = (j["model"], j["geometry"])
+        if k not in smallest or j["W"] * j["H"] < smallest[k]["W"] * smallest[k]["H"]:
+            smallest[k] = j
+    assert len(smallest) >= 8
+    for j in sorted(smallest.values(), key=lambda j: j["W"] * j["H"])[:8]:
+        W, H = j["W"], j["H"]
+        types = (G.pipe(W, H) if j["geometry"] == "pipe" else
+                 G.disc(W, H, W // 8, H // 2, max(1, H // 16), walls=False)
+                 if j["geometry"] == "disc" else G.periodic(W, H))
+        st = oracle.init_bernoulli(j["model"], j["W"], j["H"], types, seed=j["seed"],
+                                   p_move=j["p"], p_rest=j["p"])
+        assert sha(st) == g["init_sha"][j["index"]]
+        pipe = j["geometry"] == "pipe"
+        fin = oracle.run(j["model"], st, 1000, types=types, seed=j["seed"],
+                         force_x=8 if pipe else -1, force_p=0.01 if pipe else 0.0)
+        assert sha(fin) == g["final_sha"][j["index"]], j
+
+
 # ----------------------------------------------- against the compiled reference
 @pytest.mark.parametrize("model", MODELS)
 def test_restatement_equals_reference_random_cases(ref, model):
