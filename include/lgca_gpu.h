@@ -150,7 +150,11 @@ int lgca_set_temporal_depth(lgca_handle h, int depth);
  * bounded wait, only for its two neighbour bands between steps; a wait that
  * times out marks the handle failed: see lgca_clear_error),
  * 5 = one step per pass with two words per lane where dim_x is a multiple of
- * 128 (variant 1 keeps one word per lane).  Results do not depend on it.
+ * 128 (variant 1 keeps one word per lane), 6 = resident (all steps of a call
+ * in one cooperative launch with the state held on chip between steps; for
+ * dim_x a multiple of 128 and lattices whose rows, at one row of up to 4096
+ * sites per warp, fit the GPU at once, e.g. 8192 x 2048; otherwise one step
+ * per pass; waits as for 4).  Results do not depend on it.
  * No reference counterpart (a scheduling choice of this engine). */
 int lgca_set_kernel_variant(lgca_handle h, int variant);
 

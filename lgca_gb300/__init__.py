@@ -260,7 +260,9 @@ class GpuLattice:
         _check(self._h, lib().lgca_set_block_warps(self._h, int(warps)))
 
     def set_kernel_variant(self, variant: int) -> None:
-        """0 auto, 1 one step per pass, 2 register wavefront, 3 shared-memory tiles."""
+        """0 auto, 1 one step per pass, 2 register wavefront, 3 shared-memory tiles,
+        4 persistent bands, 5 one step per pass with two words per lane, 6 resident
+        (state on chip across the steps of a call)."""
         _check(self._h, lib().lgca_set_kernel_variant(self._h, int(variant)))
 
     def set_step(self, t: int) -> None:

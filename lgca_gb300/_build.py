@@ -12,7 +12,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "liblgca_gpu.so")
 SOURCES = ["step.cu", "multistep.cu", "wave.cu", "aux.cu", "bodyforce.cu", "batch.cu",
-           "lgca_gpu.cu", "noalloc.cu"]
+           "lgca_gpu.cu", "noalloc.cu", "resident.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 APPS = {"lgca_headless": "apps/lgca_headless.cpp"}
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]

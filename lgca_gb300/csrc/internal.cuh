@@ -179,6 +179,22 @@ cudaError_t launch_persistent(int model, int geom_mode, const StepArgs &a, uint6
                               uint64_t *buf1, uint64_t seed, uint64_t t0, int nsteps, int *flags,
                               int *err, int max_blocks, const PersistWait &w, cudaStream_t stream);
 
+// Resident form (resident.cu): nsteps steps in one cooperative launch with
+// the state held on chip between steps; for lattices of whole word pairs per
+// row whose one-row-per-warp tasks fit on the GPU at once.  The result is in
+// `a.dst`.  `flags` (flag_count counters) must be zero before the launch;
+// `halo` holds halo_words words; *err as for launch_persistent.
+struct ResidentShape {
+    int nblk, wpr, rpb;  // blocks (bands), warps per row, most rows in a band
+    size_t smem;         // dynamic shared memory per block
+    size_t halo_words, flag_count;
+};
+static constexpr size_t RES_MAX_SMEM = 200 * 1024;
+bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out);
+cudaError_t launch_resident(int model, int geom_mode, const StepArgs &a, const ResidentShape &sh,
+                            uint64_t *halo, unsigned *flags, int *err, uint64_t seed, uint64_t t0,
+                            int nsteps, const PersistWait &w, cudaStream_t stream);
+
 // Kernel families selectable per handle.
 enum : int {
     VARIANT_AUTO = 0,
@@ -186,7 +202,8 @@ enum : int {
     VARIANT_WAVE = 2,
     VARIANT_TILE = 3,
     VARIANT_PERSIST = 4,
-    VARIANT_PLAIN2 = 5  // one step per pass, two words per lane
+    VARIANT_PLAIN2 = 5,   // one step per pass, two words per lane
+    VARIANT_RESIDENT = 6  // state held on chip across the steps of a call
 };
 
 // Layout conversion between the reference byte-per-cell format and planes.

@@ -41,6 +41,9 @@ struct lgca_lattice {
     // random-cell body force: its first-occurrence table (kept all ones
     // between calls), per-call state, the table's clean mark and the count
     void *bf = nullptr;
+    // resident form: the band edges' halo slots, then the edge warps' step
+    // counters (resident_shape of the lattice)
+    void *res = nullptr;
     // persistent kernel: sync[0] = error flag (sticky: set when a bounded
     // neighbour wait gave up, cleared only by lgca_clear_error), then one step
     // flag per block; sync_err_host is its pinned copy, refreshed after each
@@ -341,7 +344,8 @@ int lgca_destroy(lgca_handle h)
     if (h->batch && lgca_batch_remove(h->batch, h) != LGCA_OK) cudaDeviceSynchronize();
     // memory goes back to the pool in stream order, after the handle's queued
     // work (batch steps of a member are ordered before it); no host wait
-    void *mem[] = {h->buf[0], h->buf[1], h->solid, h->slip, h->chir, h->scratch, h->sync, h->bf};
+    void *mem[] = {h->buf[0], h->buf[1], h->solid, h->slip, h->chir, h->scratch, h->sync, h->bf,
+                   h->res};
     for (void *p : mem) dfree(h, p);
     if (h->sync_err_host) {
         cudaStreamSynchronize(h->stream);
@@ -564,7 +568,7 @@ int lgca_set_temporal_depth(lgca_handle h, int depth)
 int lgca_set_kernel_variant(lgca_handle h, int variant)
 {
     CHECK_VALID(h);
-    if (variant < VARIANT_AUTO || variant > VARIANT_PLAIN2)
+    if (variant < VARIANT_AUTO || variant > VARIANT_RESIDENT)
         return fail(h, LGCA_ERR_INVALID, "unknown kernel variant %d", variant);
     h->variant = variant;
     return LGCA_OK;
@@ -609,12 +613,36 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
         h->t += (uint64_t)nsteps;
         return LGCA_OK;
     }
+    ResidentShape rs;
+    if (nsteps > 0 && h->variant == VARIANT_RESIDENT && resident_shape(h->model, h->g, rs)) {
+        if (const int fst = error_flag(h)) return fst;
+        const size_t halo_bytes = rs.halo_words * sizeof(uint64_t);
+        if (!h->res) {
+            int st = dalloc(h, &h->res, halo_bytes + rs.flag_count * sizeof(unsigned), false,
+                            "resident halo");
+            if (st) return st;
+        }
+        unsigned *flags = reinterpret_cast<unsigned *>(static_cast<char *>(h->res) + halo_bytes);
+        CK(h, cudaMemsetAsync(flags, 0, rs.flag_count * sizeof(unsigned), h->stream));
+        a.src = h->buf[h->cur];
+        a.dst = h->buf[h->cur ^ 1];
+        const PersistWait w{h->wait_ns, h->withhold};
+        CK(h, launch_resident(h->model, gm, a, rs, static_cast<uint64_t *>(h->res), flags, h->sync,
+                              h->seed, h->t, nsteps, w, h->stream));
+        CK(h, cudaMemcpyAsync(h->sync_err_host, h->sync, sizeof(int), cudaMemcpyDeviceToHost,
+                              h->stream));
+        h->cur ^= 1;
+        h->t += (uint64_t)nsteps;
+        return LGCA_OK;
+    }
     int done = 0;
     while (done < nsteps) {
         // largest supported depth that fits, else one step per pass
         int k = std::min(h->depth, nsteps - done);
         const bool tile = h->variant == VARIANT_TILE;
-        if (h->variant == VARIANT_PLAIN || h->variant == VARIANT_PLAIN2) k = 1;
+        if (h->variant == VARIANT_PLAIN || h->variant == VARIANT_PLAIN2 ||
+            h->variant == VARIANT_RESIDENT)
+            k = 1;
         while (k > 1 && !(tile ? multistep_supported(h->model, h->g, k)
                                : wave_supported(h->model, h->g, k)))
             --k;
@@ -939,7 +967,7 @@ int lgca_checkpoint_load(lgca_handle h, const void *buf, size_t bytes)
                     hd.model, hd.dim_x, hd.dim_y);
     // the settings pass the same checks as their setters before anything changes
     if ((hd.flags & ~15) != 0) return fail(h, LGCA_ERR_INVALID, "checkpoint flags 0x%x invalid", hd.flags);
-    if (hd.variant < VARIANT_AUTO || hd.variant > VARIANT_PLAIN2)
+    if (hd.variant < VARIANT_AUTO || hd.variant > VARIANT_RESIDENT)
         return fail(h, LGCA_ERR_INVALID, "checkpoint kernel variant %d invalid", hd.variant);
     if (hd.wpt != 1 && hd.wpt != 2)
         return fail(h, LGCA_ERR_INVALID, "checkpoint words per lane %d invalid", hd.wpt);

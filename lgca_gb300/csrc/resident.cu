@@ -1,0 +1,508 @@
+// Resident form of the lattice step: for lattices whose one-step warp tasks
+// (two words per lane, one row per warp) all fit on the GPU at once, e.g.
+// FHP-III 8192 x 2048 = 4096 warps on 152 SMs.  One cooperative launch
+// advances nsteps steps; the state never goes back to global memory between
+// them.
+//
+// Reference: OMP_Lattice<M>::collide_and_propagate, keva92/lgca
+// src/omp_lattice.cpp:100-249 (the pull table and rules are those of
+// step_body.cuh, which states them per model and row parity).
+//
+// Decomposition.  Block b owns the band of rows [H*b/nb, H*(b+1)/nb); warp
+// (r, h) of the block owns pairs 32h .. 32h+31 of band row r.  Between steps
+// a warp keeps the channels its own row pulls from itself (FHP 0, 3 and the
+// rest channel 6; HPP 0 and 2) in registers, and writes every moving channel
+// of its pair to the block's shared memory, from which the rows above and
+// below, and the lanes at its ends, pull:
+//   FHP: row y-1 gives channels 1, 2; row y+1 gives 4, 5
+//   HPP: row y-1 gives channel 1;     row y+1 gives 3
+// A band's first and last rows also pull from the neighbouring bands: each
+// block writes its first row's "from below" channels and its last row's
+// "from above" channels to a halo slot in global memory (two slots per
+// block and side, by step parity) and then raises a per-warp step counter;
+// the edge warps of the neighbouring block wait for those counters before
+// they load the slot.  Interior rows never wait for another block.
+//
+// Forcing belongs to the start of a step (it flips source words before the
+// pull).  Here the owner of the forcing column applies the flips of step j+1
+// to its registers at the end of step j, before it writes them to shared
+// memory, so that every lane that pulls the forced words sees them; the
+// state written back to global memory after the last step carries no flips.
+//
+// Synchronisation per step: one block barrier, plus the edge warps' waits.
+// Every wait is bounded (wait_ns, measured with %globaltimer): past it, or
+// when another block has given up, a warp records the error in *err, the
+// block finishes the step without further waits and returns after the
+// barrier.  *err is sticky: a launch that finds it set does nothing.
+#include "step_body.cuh"
+
+#include <algorithm>
+
+namespace lgca_gpu {
+
+static constexpr int RES_MAX_WARPS = 28;  // warps per block (<= 72 registers per thread)
+
+struct ResidentArgs {
+    uint64_t *halo;   // [2 parities][nblk][2 sides][2 channels][nw] words
+    unsigned *flags;  // [nblk][2 sides][wpr] step counters, zero before the launch
+    int *err;
+    uint64_t seed, t0;
+    int nsteps;
+    int nblk, wpr, rpb;  // blocks, warps per row, most rows in a band
+    uint64_t wait_ns;
+    int withhold;  // block that never raises its counters (test hook), -1 none
+};
+
+#ifndef LGCA_HOST_EMULATION
+// the block's shared memory: 8 control words, then two buffers of
+// rpb x SP x nw words
+__device__ __forceinline__ uint64_t *res_smem()
+{
+    extern __shared__ uint4 res_sm[];
+    return reinterpret_cast<uint64_t *>(res_sm);
+}
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t res_timer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+#endif
+
+template <int MODEL>
+struct ResPlanes {
+    static constexpr bool HPP = MODEL == M_HPP;
+    static constexpr int SP = HPP ? 4 : 6;     // moving channels (kept in shared memory)
+    static constexpr int NV = HPP ? 1 : 2;     // channels pulled from each of rows y-1, y+1
+    static constexpr int A0 = 1;               // first channel from row y-1 (then A0 + 1 for FHP)
+    static constexpr int B0 = HPP ? 3 : 4;     // first channel from row y+1
+    static constexpr int WEST = HPP ? 2 : 3;   // the forcing's west-moving channel
+};
+
+template <int MODEL, int GM>
+__global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
+    k_resident(const __grid_constant__ StepArgs a, const __grid_constant__ ResidentArgs R)
+{
+    using P = ResPlanes<MODEL>;
+    constexpr int D = ModelTraits<MODEL>::D;
+    constexpr int SP = P::SP, NV = P::NV, A0 = P::A0, B0 = P::B0, WEST = P::WEST;
+    uint64_t *const sm = res_smem();
+    // control words: chirality keys [0..1] and forcing keys [2..3], and the
+    // stop flags [4..5], by step parity.  A stop flag is written before the
+    // barrier that ends its step and read by every warp right after it; the
+    // slot is not written again until every warp has passed the next
+    // barrier, so all warps of the block read the same value and return
+    // together.  The checks before the first step use slot 1.
+    volatile uint64_t *const ctl = sm;
+    uint64_t *const rows = sm + 8;
+    const PlaneGeom &g = a.g;
+    const int nw = g.nw, np = nw >> 1;
+    const size_t ps = g.ps;
+    const size_t bufw = (size_t)R.rpb * SP * nw, roww = (size_t)SP * nw;
+    const int nb = R.nblk, b = blockIdx.x;
+    const int bl = b == 0 ? nb - 1 : b - 1, br = b == nb - 1 ? 0 : b + 1;
+    const int y0 = (int)((long long)g.H * b / nb), y1 = (int)((long long)g.H * (b + 1) / nb);
+    const int nrows = y1 - y0;
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int r = warp / R.wpr, hw = warp - r * R.wpr;
+    const int t = hw * 32 + lane, w0 = 2 * t;
+    const bool rowok = r < nrows;  // warp-uniform
+    const bool active = rowok && t < np;
+    const int y = y0 + (rowok ? r : 0);
+    const bool even = (y & 1) == 0;
+    const bool top = rowok && r == 0, bot = rowok && r == nrows - 1;
+    const bool need_w = active && lane == 0;
+    const bool need_e = active && (lane == 31 || t == np - 1);
+    const int widx = t == 0 ? nw - 1 : w0 - 1;
+    const int eidx = t == np - 1 ? 0 : w0 + 2;
+    const unsigned row0 = (unsigned)y * (unsigned)g.pitch;
+    const int fw = a.fx >> 6;
+    const bool fowner = a.force_thr != 0 && active && (fw >> 1) == t;
+    auto halo_slot = [&](int par, int blk, int side) -> uint64_t * {
+        return R.halo + (size_t)((par * nb + blk) * 2 + side) * 2 * nw;
+    };
+    auto flag_of = [&](int blk, int side, int k) -> unsigned * {
+        return R.flags + ((size_t)blk * 2 + side) * R.wpr + k;
+    };
+
+    if (warp == 0 && lane == 0) {
+        ctl[4] = 0;
+        ctl[5] = (uint64_t)(*(volatile int *)R.err);
+        ctl[0] = lgca_rng_key(R.seed, LGCA_STREAM_CHIR, R.t0);
+        ctl[3] = lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0 + 1);
+    }
+
+    // the row's state at the launch's first step
+    uint64_t s[2][7] = {};
+    uint64_t solid[2] = {0, 0}, slip[2] = {0, 0}, fz[2] = {0, 0};
+    if (active) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(a.src + d * ps + row0 + w0));
+            s[0][d] = v.x;
+            s[1][d] = v.y;
+        }
+        if (GM >= GEOM_NOSLIP) {
+            const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(a.solid + row0 + w0));
+            solid[0] = v.x;
+            solid[1] = v.y;
+        }
+        if (GM == GEOM_FULL) {
+            const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(a.slip + row0 + w0));
+            slip[0] = v.x;
+            slip[1] = v.y;
+        }
+        if (a.chir) {
+            const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(a.chir + row0 + w0));
+            fz[0] = v.x;
+            fz[1] = v.y;
+        }
+    }
+    // warps without wall or obstacle cells skip the boundary multiplexer
+    const bool walls = GM != GEOM_NONE &&
+                       __any_sync(FULL, (solid[0] | solid[1] | slip[0] | slip[1]) != 0ull);
+
+    // forcing flips of one step on the registers (the owner of the column)
+    auto force = [&](uint64_t fkey) {
+        if (!fowner) return;
+        const uint64_t u = lgca_rng_draw(fkey, lgca_rng_index((uint32_t)y, (uint32_t)a.fx)) >> 32;
+        const uint64_t bit = (u < a.force_thr) ? (1ull << (a.fx & 63)) : 0ull;
+        const uint64_t m0 = (fw & 1) ? 0ull : bit, m1 = (fw & 1) ? bit : 0ull;
+        const uint64_t f0 = ~s[0][0] & s[0][WEST] & ~solid[0] & ~slip[0] & m0;
+        const uint64_t f1 = ~s[1][0] & s[1][WEST] & ~solid[1] & ~slip[1] & m1;
+        s[0][0] |= f0;
+        s[0][WEST] &= ~f0;
+        s[1][0] |= f1;
+        s[1][WEST] &= ~f1;
+    };
+    // the moving channels to shared memory buffer `par`; the band's edge rows
+    // also to their halo slots, then the step counter `stepval`
+    auto publish = [&](int par, unsigned stepval) {
+        if (active) {
+            uint64_t *dr = rows + par * bufw + (size_t)r * roww;
+#pragma unroll
+            for (int d = 0; d < SP; ++d)
+                *reinterpret_cast<ulonglong2 *>(dr + (size_t)d * nw + w0) = make_ulonglong2(s[0][d], s[1][d]);
+        }
+        if (top || bot) {  // warp-uniform
+            if (active && top) {  // row y0: channels the last row of block bl pulls from below
+                uint64_t *hs = halo_slot(par, b, 0);
+#pragma unroll
+                for (int k = 0; k < NV; ++k)
+                    *reinterpret_cast<ulonglong2 *>(hs + (size_t)k * nw + w0) =
+                        make_ulonglong2(s[0][B0 + k], s[1][B0 + k]);
+            }
+            if (active && bot) {  // row y1-1: channels the first row of block br pulls from above
+                uint64_t *hs = halo_slot(par, b, 1);
+#pragma unroll
+                for (int k = 0; k < NV; ++k)
+                    *reinterpret_cast<ulonglong2 *>(hs + (size_t)k * nw + w0) =
+                        make_ulonglong2(s[0][A0 + k], s[1][A0 + k]);
+            }
+            __threadfence();
+            __syncwarp();
+            if (lane == 0 && b != R.withhold) {
+                if (top) st_release_u32(flag_of(b, 0, hw), stepval);
+                if (bot) st_release_u32(flag_of(b, 1, hw), stepval);
+            }
+        }
+    };
+    // an edge warp's wait for the counters of side `side` of block `blk`:
+    // every lane waits for all of them itself (an acquire of its own before
+    // it loads the slot); false when it gave up
+    auto wait_for = [&](int blk, int side, unsigned want, int j) -> bool {
+        bool ok = true;
+        const uint64_t t_start = res_timer_ns();
+        for (int k = 0; k < R.wpr && ok; ++k) {
+            const unsigned *f = flag_of(blk, side, k);
+            while (ld_acquire_u32(f) < want) {
+                if (*(volatile int *)R.err || res_timer_ns() - t_start > R.wait_ns) {
+                    ok = false;
+                    break;
+                }
+                __nanosleep(20);
+            }
+        }
+        ok = __all_sync(FULL, ok);
+        if (!ok && lane == 0) {
+            atomicExch(R.err, 1);
+            ctl[4 + (j & 1)] = 1;
+        }
+        return ok;
+    };
+
+    force(lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0));
+    publish(0, 1u);
+    __syncthreads();
+    if (ctl[5]) return;  // an earlier launch gave up: do not step a partial state (block-uniform)
+
+    const bool nsrow = (y == 0) || (y == g.H - 1);
+    bool waiting = true;  // false once this warp gave up a wait
+    for (int j = 0; j < R.nsteps; ++j) {
+        const int cur = j & 1;
+        const uint64_t ck = ctl[cur], fk = ctl[2 + (cur ^ 1)];
+        if (warp == 0 && lane == 0) {  // keys of the next steps, read after the barrier
+            ctl[cur ^ 1] = lgca_rng_key(R.seed, LGCA_STREAM_CHIR, R.t0 + (uint64_t)j + 1);
+            ctl[2 + cur] = lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0 + (uint64_t)j + 2);
+        }
+        uint64_t c0 = 0, c1 = 0;
+        if (MODEL != M_HPP) {
+            if (a.chir) {
+                c0 = fz[0];
+                c1 = fz[1];
+            } else {
+                const uint64_t z = ck + lgca_rng_index((uint32_t)y, (uint32_t)w0) * LGCA_RNG_GAMMA;
+                c0 = lgca_mix64(z);
+                c1 = lgca_mix64(z + LGCA_RNG_GAMMA);
+            }
+        }
+
+        // ---- gather: own channels from registers, the others from rows y-1, y+1
+        uint64_t n[2][7];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            n[0][d] = s[0][d];
+            n[1][d] = s[1][d];
+        }
+        // edge words in the order the pulls use them (step_body.cuh):
+        //   FHP, even row: west 0 (row y), 1 (y-1), 5 (y+1); east 3 (row y)
+        //   FHP, odd row:  west 0 (row y); east 3 (row y), 2 (y-1), 4 (y+1)
+        //   HPP:           west 0 (row y); east 2 (row y)
+        uint64_t eg[4] = {0, 0, 0, 0};
+        const uint64_t *own = rows + cur * bufw + (size_t)r * roww;
+        if (MODEL == M_HPP) {
+            if (need_w) eg[0] = own[widx];
+            if (need_e) eg[1] = own[(size_t)2 * nw + eidx];
+        } else if (even) {
+            if (need_w) eg[0] = own[widx];
+            if (need_e) eg[3] = own[(size_t)3 * nw + eidx];
+        } else {
+            if (need_w) eg[0] = own[widx];
+            if (need_e) eg[1] = own[(size_t)3 * nw + eidx];
+        }
+        // row y-1
+        if (top) {
+            if (waiting) waiting = wait_for(bl, 1, (unsigned)j + 1, j);
+            const uint64_t *hs = halo_slot(cur, bl, 1);
+            if (active) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(hs + (size_t)k * nw + w0));
+                    n[0][A0 + k] = v.x;
+                    n[1][A0 + k] = v.y;
+                }
+                if (MODEL != M_HPP) {
+                    if (even && need_w) eg[1] = __ldcg(hs + widx);            // channel 1
+                    if (!even && need_e) eg[2] = __ldcg(hs + (size_t)nw + eidx);  // channel 2
+                }
+            }
+        } else if (active) {
+            const uint64_t *up = rows + cur * bufw + (size_t)(r - 1) * roww;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(up + (size_t)(A0 + k) * nw + w0);
+                n[0][A0 + k] = v.x;
+                n[1][A0 + k] = v.y;
+            }
+            if (MODEL != M_HPP) {
+                if (even && need_w) eg[1] = up[(size_t)1 * nw + widx];
+                if (!even && need_e) eg[2] = up[(size_t)2 * nw + eidx];
+            }
+        }
+        // row y+1
+        if (bot) {
+            if (waiting) waiting = wait_for(br, 0, (unsigned)j + 1, j);
+            const uint64_t *hs = halo_slot(cur, br, 0);
+            if (active) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(hs + (size_t)k * nw + w0));
+                    n[0][B0 + k] = v.x;
+                    n[1][B0 + k] = v.y;
+                }
+                if (MODEL != M_HPP) {
+                    if (even && need_w) eg[2] = __ldcg(hs + (size_t)nw + widx);  // channel 5
+                    if (!even && need_e) eg[3] = __ldcg(hs + eidx);             // channel 4
+                }
+            }
+        } else if (active) {
+            const uint64_t *dn = rows + cur * bufw + (size_t)(r + 1) * roww;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(dn + (size_t)(B0 + k) * nw + w0);
+                n[0][B0 + k] = v.x;
+                n[1][B0 + k] = v.y;
+            }
+            if (MODEL != M_HPP) {
+                if (even && need_w) eg[2] = dn[(size_t)5 * nw + widx];
+                if (!even && need_e) eg[3] = dn[(size_t)4 * nw + eidx];
+            }
+        }
+
+        // ---- pull: x-1 / x+1 shifts of the pairs (one shuffle each)
+        auto shl = [&](uint64_t v0, uint64_t v1, uint64_t edge, uint64_t &r0, uint64_t &r1) {
+            const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v1 >> 32), 1);
+            const uint64_t in = need_w ? (edge >> 63) : (uint64_t)(hi >> 31);
+            r0 = (v0 << 1) | in;
+            r1 = (v1 << 1) | (v0 >> 63);
+        };
+        auto shr = [&](uint64_t v0, uint64_t v1, uint64_t edge, uint64_t &r0, uint64_t &r1) {
+            const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v0, 1);
+            const uint64_t in = need_e ? (edge & 1ull) : (uint64_t)(lo & 1u);
+            r0 = (v0 >> 1) | (v1 << 63);
+            r1 = (v1 >> 1) | (in << 63);
+        };
+        uint64_t q[2][7];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            q[0][d] = n[0][d];
+            q[1][d] = n[1][d];
+        }
+        if (MODEL == M_HPP) {
+            shl(n[0][0], n[1][0], eg[0], q[0][0], q[1][0]);
+            shr(n[0][2], n[1][2], eg[1], q[0][2], q[1][2]);
+        } else if (even) {  // warp-uniform: one row per warp
+            shl(n[0][0], n[1][0], eg[0], q[0][0], q[1][0]);
+            shl(n[0][1], n[1][1], eg[1], q[0][1], q[1][1]);
+            shl(n[0][5], n[1][5], eg[2], q[0][5], q[1][5]);
+            shr(n[0][3], n[1][3], eg[3], q[0][3], q[1][3]);
+        } else {
+            shl(n[0][0], n[1][0], eg[0], q[0][0], q[1][0]);
+            shr(n[0][3], n[1][3], eg[1], q[0][3], q[1][3]);
+            shr(n[0][2], n[1][2], eg[2], q[0][2], q[1][2]);
+            shr(n[0][4], n[1][4], eg[3], q[0][4], q[1][4]);
+        }
+
+        // ---- collision and boundaries (as step_body.cuh)
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            uint64_t c[7];
+#pragma unroll
+            for (int d = 0; d < D; ++d) c[d] = q[k][d];
+            collide<MODEL>(c, k ? c1 : c0);
+            if (GM == GEOM_NONE || !walls) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) s[k][d] = c[d];
+            } else {
+                const uint64_t fl = ~(solid[k] | slip[k]);
+                const uint64_t ew = (w0 + k == 0 ? 1ull : 0ull) | (w0 + k == nw - 1 ? (1ull << 63) : 0ull);
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    uint64_t o = (fl & c[d]) | (solid[k] & q[k][Dirs<MODEL>::inv(d)]);
+                    if (GM == GEOM_FULL) {
+                        const uint64_t sx = nsrow ? q[k][Dirs<MODEL>::mirx(d)] : q[k][d];
+                        o |= slip[k] & ((ew & q[k][Dirs<MODEL>::miry(d)]) | (~ew & sx));
+                    }
+                    s[k][d] = o;
+                }
+            }
+        }
+
+        if (j + 1 < R.nsteps) {
+            force(fk);
+            publish(cur ^ 1, (unsigned)j + 2);
+        } else if (active && !ctl[4 + cur]) {
+            uint64_t *dp = a.dst + row0 + w0;
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                *reinterpret_cast<ulonglong2 *>(dp + d * ps) = make_ulonglong2(s[0][d], s[1][d]);
+        }
+        __syncthreads();
+        if (ctl[4 + cur]) return;  // a wait of this step gave up (block-uniform)
+    }
+}
+
+#ifndef LGCA_HOST_EMULATION
+// ------------------------------------------------------------------ launcher
+
+size_t resident_smem_bytes(int model, const PlaneGeom &g, int rpb)
+{
+    const int SP = model == M_HPP ? 4 : 6;
+    return (8 + 2 * (size_t)rpb * SP * g.nw) * sizeof(uint64_t);
+}
+
+bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out)
+{
+    if (g.W % 64 != 0 || (g.nw & 1) || g.H < 1) return false;
+    const int np = g.nw / 2;
+    const int wpr = (np + 31) / 32;
+    const int nblk = std::min(sm_count(), g.H);
+    const int rpb = (g.H + nblk - 1) / nblk;
+    if (rpb * wpr > RES_MAX_WARPS) return false;
+    const size_t smem = resident_smem_bytes(model, g, rpb);
+    if (smem > RES_MAX_SMEM) return false;
+    out.nblk = nblk;
+    out.wpr = wpr;
+    out.rpb = rpb;
+    out.smem = smem;
+    out.halo_words = (size_t)2 * nblk * 2 * 2 * g.nw;
+    out.flag_count = (size_t)nblk * 2 * wpr;
+    return true;
+}
+
+template <int MODEL, int GM>
+static cudaError_t res_launch(const StepArgs &a, const ResidentShape &sh, const ResidentArgs &R,
+                              cudaStream_t st)
+{
+    auto kern = k_resident<MODEL, GM>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    const int threads = 32 * sh.rpb * sh.wpr;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, sh.smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1 || sh.nblk > per_sm * sm_count()) return cudaErrorCooperativeLaunchTooLarge;
+    StepArgs aa = a;
+    ResidentArgs rr = R;
+    void *args[] = {(void *)&aa, (void *)&rr};
+    return cudaLaunchCooperativeKernel((void *)kern, dim3(sh.nblk), dim3(32, sh.rpb * sh.wpr), args,
+                                      sh.smem, st);
+}
+
+template <int MODEL>
+static cudaError_t res_model(int gm, const StepArgs &a, const ResidentShape &sh,
+                             const ResidentArgs &R, cudaStream_t st)
+{
+    switch (gm) {
+    case GEOM_NONE: return res_launch<MODEL, GEOM_NONE>(a, sh, R, st);
+    case GEOM_NOSLIP: return res_launch<MODEL, GEOM_NOSLIP>(a, sh, R, st);
+    default: return res_launch<MODEL, GEOM_FULL>(a, sh, R, st);
+    }
+}
+
+cudaError_t launch_resident(int model, int gm, const StepArgs &a, const ResidentShape &sh,
+                            uint64_t *halo, unsigned *flags, int *err, uint64_t seed, uint64_t t0,
+                            int nsteps, const PersistWait &w, cudaStream_t st)
+{
+    if (w.wait_ns == 0 || nsteps < 1) return cudaErrorInvalidValue;
+    ResidentArgs R;
+    R.halo = halo;
+    R.flags = flags;
+    R.err = err;
+    R.seed = seed;
+    R.t0 = t0;
+    R.nsteps = nsteps;
+    R.nblk = sh.nblk;
+    R.wpr = sh.wpr;
+    R.rpb = sh.rpb;
+    R.wait_ns = w.wait_ns;
+    R.withhold = w.withhold;
+    switch (model) {
+    case M_HPP: return res_model<M_HPP>(gm, a, sh, R, st);
+    case M_FHP_I: return res_model<M_FHP_I>(gm, a, sh, R, st);
+    default: return res_model<M_FHP_II>(gm, a, sh, R, st);  // FHP-II and FHP-III share one rule set
+    }
+}
+#endif
+
+}  // namespace lgca_gpu

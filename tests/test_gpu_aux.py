@@ -296,8 +296,10 @@ def test_paint_rejects_bad_arguments(gpu):
         assert not L.get_cell_types().any()
 
 
-def test_persistent_wait_timeout_marks_handle_failed_until_cleared(gpu, oracle):
-    """One block of the persistent kernel withholds its progress (test hook),
+@pytest.mark.parametrize("variant", [4, 6])
+def test_persistent_wait_timeout_marks_handle_failed_until_cleared(gpu, oracle, variant):
+    """One block of the persistent (4) or resident (6) kernel withholds its
+    progress (test hook),
     so its neighbours' bounded waits run out after the 1 ms limit.  Every call
     that waits for the handle then reports LGCA_ERR_TIMEOUT, and persistent
     calls queued behind the failure do not step, until lgca_clear_error; after
@@ -306,7 +308,7 @@ def test_persistent_wait_timeout_marks_handle_failed_until_cleared(gpu, oracle):
     st = oracle.init_bernoulli(model, W, H, None, seed=4, p_move=0.3, p_rest=0.3)
     with gpu.GpuLattice(model, W, H, seed=4) as L:
         L.upload(st)
-        L.set_kernel_variant(4)
+        L.set_kernel_variant(variant)
         L.set_wait_limit(1_000_000)
         L.test_withhold_progress(1)
         L.collide_and_propagate(10)

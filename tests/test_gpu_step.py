@@ -233,6 +233,44 @@ def test_temporal_blocking_frozen_chirality(gpu, oracle, model, variant):
     assert np.array_equal(got, want)
 
 
+def test_resident_karman_config(gpu):
+    """The whole Karman run on the resident kernel (152 bands of 13-14 rows,
+    two warps per row), 100 steps per launch: the same reference pins."""
+    run_karman_config(gpu, variant=6)
+
+
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("geom", sorted(GEOMS))
+def test_resident_kernel_vs_oracle(gpu, oracle, model, geom):
+    """The resident kernel gives the oracle's bits: bands of one row and of
+    many, one to four warps per row, the forcing column on the x seam and
+    inside, steps split over launches (forcing at the launch boundary).
+    Widths it cannot hold (odd word counts) take one step per pass."""
+    rng = np.random.default_rng(model * 13 + len(geom))
+    for W, H in [(128, 10), (256, 64), (4096, 40), (8192, 300), (16384, 160), (2048, 2048),
+                 (4160, 40)]:
+        types = GEOMS[geom](W, H)
+        seed = int(rng.integers(1 << 40))
+        st = oracle.init_bernoulli(model, W, H, types, seed=seed, p_move=0.35, p_rest=0.3)
+        for fx in (W - 1, int(rng.integers(W))):
+            kw = dict(types=types, seed=seed, force_x=fx, force_p=0.5, t0=int(rng.integers(50)))
+            want = oracle.run(model, st, 17, **kw)
+            for chunks in (None, [1, 9, 7]):
+                got = run_gpu(gpu, model, st, 17, variant=6, chunks=chunks, **kw)
+                assert np.array_equal(got, want), (W, H, fx, chunks)
+
+
+@pytest.mark.parametrize("model", [1, 3])
+def test_resident_kernel_frozen_chirality(gpu, oracle, model):
+    rng = np.random.default_rng(7)
+    W, H = 4096, 36
+    st = oracle.init_bernoulli(model, W, H, None, seed=9, p_move=0.4)
+    chir = rng.integers(0, 2, (H, W), dtype=np.uint8)
+    want = oracle.run(model, st, 16, chir=chir, seed=9)
+    got = run_gpu(gpu, model, st, 16, chir=chir, seed=9, variant=6)
+    assert np.array_equal(got, want)
+
+
 @pytest.mark.parametrize("depth", [2, 4, 8])
 @pytest.mark.parametrize("variant", [2, 3, 4])
 def test_temporal_blocking_karman_config(gpu, depth, variant):

@@ -299,3 +299,100 @@ def test_emulated_block_sums_equal_oracle(tmp_path, oracle):
                 want = oracle.block_sums(model, st, B)
                 for i in range(3):
                     assert np.array_equal(got[i], want[i]), (model, W, H, B, i)
+
+
+def _build_resident(out, sanitize=False):
+    gxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if gxx is None or not os.path.isdir(cuda_inc):
+        pytest.skip("g++ or the CUDA headers not available")
+    flags = (["-O0", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
+              "-fno-omit-frame-pointer"] if sanitize else ["-O1"])
+    r = subprocess.run([gxx, *flags, "-std=c++20", "-Wno-attributes", "-I", cuda_inc,
+                        os.path.join(ROOT, "tests", "resident_emu.cpp"), "-o", str(out),
+                        "-pthread", *CUDART], capture_output=True)
+    if r.returncode != 0:
+        if sanitize:
+            pytest.skip("sanitizer runtime not available")
+        raise AssertionError(r.stderr[-2000:])
+    return out
+
+
+@pytest.fixture(scope="module")
+def resident_emu(tmp_path_factory):
+    return _build_resident(tmp_path_factory.mktemp("res") / "resident_emu")
+
+
+def run_resident(exe, tmp, model, cells, types, steps, seed, t0, force_x, force_thr, nblk,
+                 chunk, withhold=-1, wait_ns=10_000_000_000):
+    H, W = cells.shape
+    inp, out = tmp / "rin.bin", tmp / "rout.bin"
+    with open(inp, "wb") as f:
+        f.write(struct.pack("<8i4Q", model, W, H, steps, force_x, nblk, chunk, withhold, seed, t0,
+                            force_thr, wait_ns))
+        f.write(np.ascontiguousarray(cells, np.uint8).tobytes())
+        f.write(np.ascontiguousarray(types, np.uint8).tobytes())
+    r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True, env=ENV, timeout=600)
+    assert r.returncode == 0, (r.returncode, r.stderr[-800:])
+    raw = out.read_bytes()
+    err = struct.unpack("<i", raw[:4])[0]
+    return err, np.frombuffer(raw[4:], np.uint8).reshape(H, W)
+
+
+# (W, H, blocks): one and two warps per row, a row of a single word pair,
+# bands of one row (top row = bottom row), one band for the whole lattice,
+# unequal bands
+RESIDENT = [(4096, 12, 3), (8192, 8, 2), (128, 6, 6), (1024, 10, 1), (2048, 14, 4),
+            (4096, 6, 6)]
+
+
+@pytest.mark.parametrize("model", [0, 1, 3])
+@pytest.mark.parametrize("geom", list(GEOMS))
+def test_emulated_resident_kernel_equals_oracle(resident_emu, tmp_path, oracle, model, geom):
+    """The resident kernel k_resident (state on chip across steps, band edges
+    exchanged through halo slots and step counters) on its whole grid: every
+    model and geometry mode, forcing at the x seam and inside a row, steps
+    run as one launch and split over several (forcing at the launch
+    boundary, results written back unforced)."""
+    rng = np.random.default_rng(model * 7 + len(geom))
+    for W, H, nblk in RESIDENT:
+        if model != 0 and H % 2:
+            continue
+        types = GEOMS[geom](W, H)
+        st = oracle.init_bernoulli(model, W, H, types, seed=5, p_move=0.35, p_rest=0.3)
+        for fx in (W - 1, int(rng.integers(W))):
+            p = 0.4
+            thr = oracle.prob_threshold(p)
+            want = oracle.run(model, st, 6, types=types, seed=13, t0=9, force_x=fx, force_p=p)
+            for chunk in (6, 4):
+                err, got = run_resident(resident_emu, tmp_path, model, st, types.astype(np.uint8),
+                                        6, 13, 9, fx, thr, nblk, chunk)
+                assert err == 0
+                assert np.array_equal(got, want), (model, geom, W, H, nblk, fx, chunk)
+
+
+def test_emulated_resident_kernel_stays_in_bounds(tmp_path, oracle):
+    """k_resident's shared-memory, halo and state accesses stay in bounds:
+    the emulator built with the address and undefined-behaviour sanitizers."""
+    exe = _build_resident(tmp_path / "resident_emu_asan", sanitize=True)
+    for model in (0, 3):
+        for W, H, nblk in [(4096, 6, 3), (8192, 4, 2), (128, 4, 4)]:
+            types = GEOMS["slip"](W, H)
+            st = oracle.init_bernoulli(model, W, H, types, seed=5, p_move=0.35, p_rest=0.3)
+            thr = oracle.prob_threshold(0.4)
+            want = oracle.run(model, st, 3, types=types, seed=13, t0=9, force_x=W - 1,
+                              force_p=0.4)
+            err, got = run_resident(exe, tmp_path, model, st, types.astype(np.uint8), 3, 13, 9,
+                                    W - 1, thr, nblk, 3)
+            assert err == 0 and np.array_equal(got, want), (model, W, H, nblk)
+
+
+def test_emulated_resident_wait_gives_up(resident_emu, tmp_path, oracle):
+    """A block that never raises its step counters makes its neighbours'
+    bounded waits run out: every block returns, the error flag is set."""
+    W, H = 4096, 12
+    types = GEOMS["periodic"](W, H)
+    st = oracle.init_bernoulli(3, W, H, types, seed=5, p_move=0.35, p_rest=0.3)
+    err, _ = run_resident(resident_emu, tmp_path, 3, st, types.astype(np.uint8), 5, 13, 0, -1, 0,
+                          3, 5, withhold=1, wait_ns=2_000_000)
+    assert err == 1
