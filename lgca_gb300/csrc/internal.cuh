@@ -182,17 +182,17 @@ cudaError_t launch_persistent(int model, int geom_mode, const StepArgs &a, uint6
 // Resident form (resident.cu): nsteps steps in one cooperative launch with
 // the state held on chip between steps; for lattices of whole word pairs per
 // row whose one-row-per-warp tasks fit on the GPU at once.  The result is in
-// `a.dst`.  `flags` (flag_count counters) must be zero before the launch;
-// `halo` holds halo_words words; *err as for launch_persistent.
+// `a.dst`.  `halo` holds halo_words words, zero before the launch; *err as
+// for launch_persistent.
 struct ResidentShape {
     int nblk, wpr, rpb;  // blocks (bands), warps per row, most rows in a band
     size_t smem;         // dynamic shared memory per block
-    size_t halo_words, flag_count;
+    size_t halo_words;
 };
 static constexpr size_t RES_MAX_SMEM = 200 * 1024;
 bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out);
 cudaError_t launch_resident(int model, int geom_mode, const StepArgs &a, const ResidentShape &sh,
-                            uint64_t *halo, unsigned *flags, int *err, uint64_t seed, uint64_t t0,
+                            uint64_t *halo, int *err, uint64_t seed, uint64_t t0,
                             int nsteps, const PersistWait &w, cudaStream_t stream);
 
 // Kernel families selectable per handle.

@@ -41,8 +41,7 @@ struct lgca_lattice {
     // random-cell body force: its first-occurrence table (kept all ones
     // between calls), per-call state, the table's clean mark and the count
     void *bf = nullptr;
-    // resident form: the band edges' halo slots, then the edge warps' step
-    // counters (resident_shape of the lattice)
+    // resident form: the band edges' halo slots (resident_shape of the lattice)
     void *res = nullptr;
     // persistent kernel: sync[0] = error flag (sticky: set when a bounded
     // neighbour wait gave up, cleared only by lgca_clear_error), then one step
@@ -618,16 +617,15 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
         if (const int fst = error_flag(h)) return fst;
         const size_t halo_bytes = rs.halo_words * sizeof(uint64_t);
         if (!h->res) {
-            int st = dalloc(h, &h->res, halo_bytes + rs.flag_count * sizeof(unsigned), false,
-                            "resident halo");
+            int st = dalloc(h, &h->res, halo_bytes, false, "resident halo");
             if (st) return st;
         }
-        unsigned *flags = reinterpret_cast<unsigned *>(static_cast<char *>(h->res) + halo_bytes);
-        CK(h, cudaMemsetAsync(flags, 0, rs.flag_count * sizeof(unsigned), h->stream));
+        // items carry the step they belong to: none may survive from an earlier call
+        CK(h, cudaMemsetAsync(h->res, 0, halo_bytes, h->stream));
         a.src = h->buf[h->cur];
         a.dst = h->buf[h->cur ^ 1];
         const PersistWait w{h->wait_ns, h->withhold};
-        CK(h, launch_resident(h->model, gm, a, rs, static_cast<uint64_t *>(h->res), flags, h->sync,
+        CK(h, launch_resident(h->model, gm, a, rs, static_cast<uint64_t *>(h->res), h->sync,
                               h->seed, h->t, nsteps, w, h->stream));
         CK(h, cudaMemcpyAsync(h->sync_err_host, h->sync, sizeof(int), cudaMemcpyDeviceToHost,
                               h->stream));

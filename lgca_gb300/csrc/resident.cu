@@ -18,10 +18,17 @@
 //   HPP: row y-1 gives channel 1;     row y+1 gives 3
 // A band's first and last rows also pull from the neighbouring bands: each
 // block writes its first row's "from below" channels and its last row's
-// "from above" channels to a halo slot in global memory (two slots per
-// block and side, by step parity) and then raises a per-warp step counter;
-// the edge warps of the neighbouring block wait for those counters before
-// they load the slot.  Interior rows never wait for another block.
+// "from above" channels to a halo slot in global memory (three slots per
+// block and side, by step modulo 3), and the edge warps of the neighbouring
+// block load them from there.  Every word goes out as two 64-bit items, one
+// half of the word in the low 32 bits and the step it belongs to in the high
+// 32 bits; an item is written and read whole (single-copy atomic), so a
+// reader that sees the step it wants has the data, with no fence and no
+// separate flag between writer and reader.  Interior rows never wait for
+// another block.  A writer overwrites a slot three steps later, by which
+// time every reader of the old contents has passed a block barrier that the
+// writer waited behind (it read the readers' own edge row of the step in
+// between).
 //
 // Forcing belongs to the start of a step (it flips source words before the
 // pull).  Here the owner of the forcing column applies the flips of step j+1
@@ -43,15 +50,16 @@ namespace lgca_gpu {
 static constexpr int RES_MAX_WARPS = 28;  // warps per block (<= 72 registers per thread)
 
 struct ResidentArgs {
-    uint64_t *halo;   // [2 parities][nblk][2 sides][2 channels][nw] words
-    unsigned *flags;  // [nblk][2 sides][wpr] step counters, zero before the launch
+    uint64_t *halo;  // [3 steps][nblk][2 sides][2 channels][nw][2] items, zero before the launch
     int *err;
     uint64_t seed, t0;
     int nsteps;
     int nblk, wpr, rpb;  // blocks, warps per row, most rows in a band
     uint64_t wait_ns;
-    int withhold;  // block that never raises its counters (test hook), -1 none
+    int withhold;  // block that never writes its halo slots (test hook), -1 none
 };
+
+static constexpr int RES_HALO_SLOTS = 3;
 
 #ifndef LGCA_HOST_EMULATION
 // the block's shared memory: 8 control words, then two buffers of
@@ -61,15 +69,16 @@ __device__ __forceinline__ uint64_t *res_smem()
     extern __shared__ uint4 res_sm[];
     return reinterpret_cast<uint64_t *>(res_sm);
 }
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
+// two halo items (each 64-bit access single-copy atomic, coherent at GPU scope)
+__device__ __forceinline__ ulonglong2 ld_items(const uint64_t *p)
 {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    ulonglong2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v)
+__device__ __forceinline__ void st_items(uint64_t *p, uint64_t a, uint64_t b)
 {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b) : "memory");
 }
 __device__ __forceinline__ uint64_t res_timer_ns()
 {
@@ -128,11 +137,9 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
     const unsigned row0 = (unsigned)y * (unsigned)g.pitch;
     const int fw = a.fx >> 6;
     const bool fowner = a.force_thr != 0 && active && (fw >> 1) == t;
-    auto halo_slot = [&](int par, int blk, int side) -> uint64_t * {
-        return R.halo + (size_t)((par * nb + blk) * 2 + side) * 2 * nw;
-    };
-    auto flag_of = [&](int blk, int side, int k) -> unsigned * {
-        return R.flags + ((size_t)blk * 2 + side) * R.wpr + k;
+    // slot of the halo items of time `tm` of side `side` (0: first row, 1: last row) of block blk
+    auto halo_slot = [&](unsigned tm, int blk, int side) -> uint64_t * {
+        return R.halo + (size_t)(((int)(tm % RES_HALO_SLOTS) * nb + blk) * 2 + side) * 2 * nw * 2;
     };
 
     if (warp == 0 && lane == 0) {
@@ -185,64 +192,73 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
         s[1][0] |= f1;
         s[1][WEST] &= ~f1;
     };
-    // the moving channels to shared memory buffer `par`; the band's edge rows
-    // also to their halo slots, then the step counter `stepval`
-    auto publish = [&](int par, unsigned stepval) {
-        if (active) {
-            uint64_t *dr = rows + par * bufw + (size_t)r * roww;
+    // the moving channels of time `tm` to shared memory buffer tm & 1; the
+    // band's edge rows also to their halo slots
+    auto publish = [&](unsigned tm) {
+        if (!active) return;
+        uint64_t *dr = rows + (tm & 1) * bufw + (size_t)r * roww;
 #pragma unroll
-            for (int d = 0; d < SP; ++d)
-                *reinterpret_cast<ulonglong2 *>(dr + (size_t)d * nw + w0) = make_ulonglong2(s[0][d], s[1][d]);
+        for (int d = 0; d < SP; ++d)
+            *reinterpret_cast<ulonglong2 *>(dr + (size_t)d * nw + w0) = make_ulonglong2(s[0][d], s[1][d]);
+        if (b == R.withhold) return;
+        const uint64_t tag = (uint64_t)(tm + 1) << 32;
+        auto put = [&](uint64_t *slot, int k, uint64_t v0, uint64_t v1) {
+            uint64_t *p = slot + ((size_t)k * nw + w0) * 2;
+            st_items(p, tag | (v0 & 0xffffffffull), tag | (v0 >> 32));
+            st_items(p + 2, tag | (v1 & 0xffffffffull), tag | (v1 >> 32));
+        };
+        if (top) {  // row y0: channels the last row of block bl pulls from below
+            uint64_t *hs = halo_slot(tm, b, 0);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) put(hs, k, s[0][B0 + k], s[1][B0 + k]);
         }
-        if (top || bot) {  // warp-uniform
-            if (active && top) {  // row y0: channels the last row of block bl pulls from below
-                uint64_t *hs = halo_slot(par, b, 0);
+        if (bot) {  // row y1-1: channels the first row of block br pulls from above
+            uint64_t *hs = halo_slot(tm, b, 1);
 #pragma unroll
-                for (int k = 0; k < NV; ++k)
-                    *reinterpret_cast<ulonglong2 *>(hs + (size_t)k * nw + w0) =
-                        make_ulonglong2(s[0][B0 + k], s[1][B0 + k]);
-            }
-            if (active && bot) {  // row y1-1: channels the first row of block br pulls from above
-                uint64_t *hs = halo_slot(par, b, 1);
-#pragma unroll
-                for (int k = 0; k < NV; ++k)
-                    *reinterpret_cast<ulonglong2 *>(hs + (size_t)k * nw + w0) =
-                        make_ulonglong2(s[0][A0 + k], s[1][A0 + k]);
-            }
-            __threadfence();
-            __syncwarp();
-            if (lane == 0 && b != R.withhold) {
-                if (top) st_release_u32(flag_of(b, 0, hw), stepval);
-                if (bot) st_release_u32(flag_of(b, 1, hw), stepval);
-            }
+            for (int k = 0; k < NV; ++k) put(hs, k, s[0][A0 + k], s[1][A0 + k]);
         }
     };
-    // an edge warp's wait for the counters of side `side` of block `blk`:
-    // every lane waits for all of them itself (an acquire of its own before
-    // it loads the slot); false when it gave up
-    auto wait_for = [&](int blk, int side, unsigned want, int j) -> bool {
-        bool ok = true;
-        const uint64_t t_start = res_timer_ns();
-        for (int k = 0; k < R.wpr && ok; ++k) {
-            const unsigned *f = flag_of(blk, side, k);
-            while (ld_acquire_u32(f) < want) {
-                if (*(volatile int *)R.err || res_timer_ns() - t_start > R.wait_ns) {
-                    ok = false;
-                    break;
+    // an edge warp's words of time `tm` from a neighbour's halo slot: the
+    // pair of each of its NV channels and, when `ek` >= 0, word `ew` of
+    // channel slot ek (lanes with need_edge).  Polls until every item carries
+    // the step; false when the wait gave up (every lane returns alike)
+    auto halo_get = [&](const uint64_t *slot, unsigned tm, int ek, int ew, bool need_edge,
+                        uint64_t (&v)[2][2], uint64_t &edge) -> bool {
+        const uint64_t tag = (uint64_t)(tm + 1);
+        uint64_t t_start = 0;
+        for (int spin = 0;; ++spin) {
+            bool ok = true;
+            if (active) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    const uint64_t *p = slot + ((size_t)k * nw + w0) * 2;
+                    const ulonglong2 x = ld_items(p), y2 = ld_items(p + 2);
+                    ok = ok && (x.x >> 32) == tag && (x.y >> 32) == tag && (y2.x >> 32) == tag &&
+                         (y2.y >> 32) == tag;
+                    v[0][k] = (x.x & 0xffffffffull) | (x.y << 32);
+                    v[1][k] = (y2.x & 0xffffffffull) | (y2.y << 32);
                 }
-                __nanosleep(20);
+                if (ek >= 0 && need_edge) {
+                    const ulonglong2 x = ld_items(slot + ((size_t)ek * nw + ew) * 2);
+                    ok = ok && (x.x >> 32) == tag && (x.y >> 32) == tag;
+                    edge = (x.x & 0xffffffffull) | (x.y << 32);
+                }
             }
+            if (__all_sync(FULL, ok)) return true;
+            if (spin == 0) t_start = res_timer_ns();
+            // the lanes decide together whether to give up
+            const bool give_up =
+                spin > 0 && (*(volatile int *)R.err || res_timer_ns() - t_start > R.wait_ns);
+            if (__any_sync(FULL, give_up)) {
+                if (lane == 0) atomicExch(R.err, 1);
+                return false;
+            }
+            __nanosleep(32);
         }
-        ok = __all_sync(FULL, ok);
-        if (!ok && lane == 0) {
-            atomicExch(R.err, 1);
-            ctl[4 + (j & 1)] = 1;
-        }
-        return ok;
     };
 
     force(lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0));
-    publish(0, 1u);
+    publish(0u);
     __syncthreads();
     if (ctl[5]) return;  // an earlier launch gave up: do not step a partial state (block-uniform)
 
@@ -292,19 +308,22 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
         }
         // row y-1
         if (top) {
-            if (waiting) waiting = wait_for(bl, 1, (unsigned)j + 1, j);
-            const uint64_t *hs = halo_slot(cur, bl, 1);
-            if (active) {
+            uint64_t v[2][2] = {{0, 0}, {0, 0}}, e = 0;
+            // FHP: the edge word is channel 1 west (even rows) or channel 2 east (odd rows)
+            const int ek = MODEL == M_HPP ? -1 : (even ? 0 : 1);
+            if (waiting && !halo_get(halo_slot((unsigned)j, bl, 1), (unsigned)j, ek,
+                                     even ? widx : eidx, even ? need_w : need_e, v, e)) {
+                waiting = false;
+                if (lane == 0) ctl[4 + cur] = 1;
+            }
 #pragma unroll
-                for (int k = 0; k < NV; ++k) {
-                    const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(hs + (size_t)k * nw + w0));
-                    n[0][A0 + k] = v.x;
-                    n[1][A0 + k] = v.y;
-                }
-                if (MODEL != M_HPP) {
-                    if (even && need_w) eg[1] = __ldcg(hs + widx);            // channel 1
-                    if (!even && need_e) eg[2] = __ldcg(hs + (size_t)nw + eidx);  // channel 2
-                }
+            for (int k = 0; k < NV; ++k) {
+                n[0][A0 + k] = v[0][k];
+                n[1][A0 + k] = v[1][k];
+            }
+            if (MODEL != M_HPP) {
+                if (even) eg[1] = e;
+                else eg[2] = e;
             }
         } else if (active) {
             const uint64_t *up = rows + cur * bufw + (size_t)(r - 1) * roww;
@@ -321,19 +340,22 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
         }
         // row y+1
         if (bot) {
-            if (waiting) waiting = wait_for(br, 0, (unsigned)j + 1, j);
-            const uint64_t *hs = halo_slot(cur, br, 0);
-            if (active) {
+            uint64_t v[2][2] = {{0, 0}, {0, 0}}, e = 0;
+            // FHP: the edge word is channel 5 west (even rows) or channel 4 east (odd rows)
+            const int ek = MODEL == M_HPP ? -1 : (even ? 1 : 0);
+            if (waiting && !halo_get(halo_slot((unsigned)j, br, 0), (unsigned)j, ek,
+                                     even ? widx : eidx, even ? need_w : need_e, v, e)) {
+                waiting = false;
+                if (lane == 0) ctl[4 + cur] = 1;
+            }
 #pragma unroll
-                for (int k = 0; k < NV; ++k) {
-                    const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(hs + (size_t)k * nw + w0));
-                    n[0][B0 + k] = v.x;
-                    n[1][B0 + k] = v.y;
-                }
-                if (MODEL != M_HPP) {
-                    if (even && need_w) eg[2] = __ldcg(hs + (size_t)nw + widx);  // channel 5
-                    if (!even && need_e) eg[3] = __ldcg(hs + eidx);             // channel 4
-                }
+            for (int k = 0; k < NV; ++k) {
+                n[0][B0 + k] = v[0][k];
+                n[1][B0 + k] = v[1][k];
+            }
+            if (MODEL != M_HPP) {
+                if (even) eg[2] = e;
+                else eg[3] = e;
             }
         } else if (active) {
             const uint64_t *dn = rows + cur * bufw + (size_t)(r + 1) * roww;
@@ -410,7 +432,7 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
 
         if (j + 1 < R.nsteps) {
             force(fk);
-            publish(cur ^ 1, (unsigned)j + 2);
+            publish((unsigned)j + 1);
         } else if (active && !ctl[4 + cur]) {
             uint64_t *dp = a.dst + row0 + w0;
 #pragma unroll
@@ -445,8 +467,7 @@ bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out)
     out.wpr = wpr;
     out.rpb = rpb;
     out.smem = smem;
-    out.halo_words = (size_t)2 * nblk * 2 * 2 * g.nw;
-    out.flag_count = (size_t)nblk * 2 * wpr;
+    out.halo_words = (size_t)RES_HALO_SLOTS * nblk * 2 * 2 * g.nw * 2;
     return true;
 }
 
@@ -481,13 +502,12 @@ static cudaError_t res_model(int gm, const StepArgs &a, const ResidentShape &sh,
 }
 
 cudaError_t launch_resident(int model, int gm, const StepArgs &a, const ResidentShape &sh,
-                            uint64_t *halo, unsigned *flags, int *err, uint64_t seed, uint64_t t0,
+                            uint64_t *halo, int *err, uint64_t seed, uint64_t t0,
                             int nsteps, const PersistWait &w, cudaStream_t st)
 {
     if (w.wait_ns == 0 || nsteps < 1) return cudaErrorInvalidValue;
     ResidentArgs R;
     R.halo = halo;
-    R.flags = flags;
     R.err = err;
     R.seed = seed;
     R.t0 = t0;

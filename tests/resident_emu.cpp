@@ -4,9 +4,8 @@
 // thread and all blocks run at once, as a cooperative launch guarantees:
 // a warp shuffle is an exchange through a shared array between two barrier
 // waits of the warp's 32 threads, __syncthreads a barrier of the block's
-// threads, the block's shared memory a host array, and the edge warps'
-// step counters are atomics with acquire / release order.  Waits are
-// bounded by the host clock.  tests/test_step_emulated.py compares the
+// threads, the block's shared memory a host array, and the 64-bit halo
+// items relaxed atomics.  Waits are bounded by the host clock.  tests/test_step_emulated.py compares the
 // result with the oracle.
 //
 //   resident_emu IN OUT
@@ -106,8 +105,18 @@ thread_local dim3 gridDim;
 #define LGCA_HOST_EMULATION 1
 namespace lgca_gpu {
 inline uint64_t *res_smem() { return emu::smem; }
-inline unsigned ld_acquire_u32(const unsigned *p) { return __atomic_load_n(p, __ATOMIC_ACQUIRE); }
-inline void st_release_u32(unsigned *p, unsigned v) { __atomic_store_n(p, v, __ATOMIC_RELEASE); }
+inline ulonglong2 ld_items(const uint64_t *p)
+{
+    ulonglong2 v;
+    v.x = __atomic_load_n(p, __ATOMIC_RELAXED);
+    v.y = __atomic_load_n(p + 1, __ATOMIC_RELAXED);
+    return v;
+}
+inline void st_items(uint64_t *p, uint64_t a, uint64_t b)
+{
+    __atomic_store_n(p, a, __ATOMIC_RELAXED);
+    __atomic_store_n(p + 1, b, __ATOMIC_RELAXED);
+}
 inline uint64_t res_timer_ns()
 {
     return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
@@ -208,8 +217,7 @@ int main(int argc, char **argv)
             if (ty == 2) slip[o] |= bit, any_slip = true;
         }
     const int gm = any_slip ? GEOM_FULL : (any_solid ? GEOM_NOSLIP : GEOM_NONE);
-    std::vector<uint64_t> halo((size_t)2 * nblk * 2 * 2 * g.nw, 0);
-    std::vector<unsigned> flags((size_t)nblk * 2 * wpr, 0);
+    std::vector<uint64_t> halo((size_t)RES_HALO_SLOTS * nblk * 2 * 2 * g.nw * 2, 0);
     int err = 0;
 
     StepArgs a{};
@@ -224,12 +232,11 @@ int main(int argc, char **argv)
     int cur = 0;
     for (int done = 0; done < steps; done += chunk) {
         const int n = std::min(chunk, steps - done);
-        std::fill(flags.begin(), flags.end(), 0u);
+        std::fill(halo.begin(), halo.end(), 0ull);
         a.src = buf[cur].data();
         a.dst = buf[cur ^ 1].data();
         ResidentArgs R{};
         R.halo = halo.data();
-        R.flags = flags.data();
         R.err = &err;
         R.seed = seed;
         R.t0 = t0 + (uint64_t)done;
