@@ -40,12 +40,15 @@ template <> struct ModelTraits<M_FHP_I> { static constexpr int D = 6; };
 template <> struct ModelTraits<M_FHP_II> { static constexpr int D = 7; };
 template <> struct ModelTraits<M_FHP_III> { static constexpr int D = 7; };
 
+// The rules below work on words of any unsigned type Word (64 or 32 sites).
+//
 // HPP: a head-on pair swaps to the perpendicular pair when the other pair is
 // empty.  The chirality is not used.  The state is exactly {0, 2} or exactly
 // {1, 3} when n0 != n1, n0 == n2 and n1 == n3.
-LGCA_HDI void collide_hpp(uint64_t n[4])
+template <class Word = uint64_t>
+LGCA_HDI void collide_hpp(Word n[4])
 {
-    const uint64_t ch = (n[0] ^ n[1]) & ~(n[0] ^ n[2]) & ~(n[1] ^ n[3]);
+    const Word ch = (n[0] ^ n[1]) & ~(n[0] ^ n[2]) & ~(n[1] ^ n[3]);
     n[0] ^= ch; n[1] ^= ch; n[2] ^= ch; n[3] ^= ch;
 }
 
@@ -74,34 +77,34 @@ LGCA_HDI void collide_hpp(uint64_t n[4])
 //       K_x = (R1 & n_x) | (R2 & n_x-1 & n_x+1),
 //     and flip exactly channels x-1, x, x+1 and the rest channel.
 // Checked exhaustively against the reference rules in the tests.
-template <bool REST>
-LGCA_HDI void collide_fhp(uint64_t n[7], uint64_t p)
+template <bool REST, class Word = uint64_t>
+LGCA_HDI void collide_fhp(Word n[7], Word p)
 {
-    const uint64_t n0 = n[0], n1 = n[1], n2 = n[2], n3 = n[3], n4 = n[4], n5 = n[5];
+    const Word n0 = n[0], n1 = n[1], n2 = n[2], n3 = n[3], n4 = n[4], n5 = n[5];
 
     // half-hexagon counts: s + 2k for (n0, n1, n2) and (n3, n4, n5)
-    const uint64_t s1 = n0 ^ n1 ^ n2, k1 = (n0 & n1) | (n2 & (n0 ^ n1));
-    const uint64_t s2 = n3 ^ n4 ^ n5, k2 = (n3 & n4) | (n5 & (n3 ^ n4));
-    const uint64_t sx = s1 ^ s2;
-    const uint64_t is3 = sx & (k1 ^ k2);
-    const uint64_t is2 = ~sx & ((s1 & ~(k1 | k2)) | (~s1 & (k1 ^ k2)));
+    const Word s1 = n0 ^ n1 ^ n2, k1 = (n0 & n1) | (n2 & (n0 ^ n1));
+    const Word s2 = n3 ^ n4 ^ n5, k2 = (n3 & n4) | (n5 & (n3 ^ n4));
+    const Word sx = s1 ^ s2;
+    const Word is3 = sx & (k1 ^ k2);
+    const Word is2 = ~sx & ((s1 & ~(k1 | k2)) | (~s1 & (k1 ^ k2)));
 
-    const uint64_t P0 = n0 & n3 & is2, P1 = n1 & n4 & is2, P2 = n2 & n5 & is2;
-    const uint64_t T = is3 & ~((n0 ^ n2) | (n2 ^ n4));
-    const uint64_t X0 = T | P0 | ((p & P1) | (~p & P2));
-    const uint64_t X1 = T | P1 | ((p & P2) | (~p & P0));
-    const uint64_t X2 = T | P2 | ((p & P0) | (~p & P1));
+    const Word P0 = n0 & n3 & is2, P1 = n1 & n4 & is2, P2 = n2 & n5 & is2;
+    const Word T = is3 & ~((n0 ^ n2) | (n2 ^ n4));
+    const Word X0 = T | P0 | ((p & P1) | (~p & P2));
+    const Word X1 = T | P1 | ((p & P2) | (~p & P0));
+    const Word X2 = T | P2 | ((p & P0) | (~p & P1));
 
     if (REST) {
-        const uint64_t r = n[6];
-        const uint64_t is1 = sx & ~(k1 | k2);
-        const uint64_t R1 = r & is1, R2 = ~r & is2;
-        const uint64_t K0 = (R1 & n0) | (R2 & n5 & n1);
-        const uint64_t K1 = (R1 & n1) | (R2 & n0 & n2);
-        const uint64_t K2 = (R1 & n2) | (R2 & n1 & n3);
-        const uint64_t K3 = (R1 & n3) | (R2 & n2 & n4);
-        const uint64_t K4 = (R1 & n4) | (R2 & n3 & n5);
-        const uint64_t K5 = (R1 & n5) | (R2 & n4 & n0);
+        const Word r = n[6];
+        const Word is1 = sx & ~(k1 | k2);
+        const Word R1 = r & is1, R2 = ~r & is2;
+        const Word K0 = (R1 & n0) | (R2 & n5 & n1);
+        const Word K1 = (R1 & n1) | (R2 & n0 & n2);
+        const Word K2 = (R1 & n2) | (R2 & n1 & n3);
+        const Word K3 = (R1 & n3) | (R2 & n2 & n4);
+        const Word K4 = (R1 & n4) | (R2 & n3 & n5);
+        const Word K5 = (R1 & n5) | (R2 & n4 & n0);
         n[0] = n0 ^ (X0 | K5 | K0 | K1);
         n[1] = n1 ^ (X1 | K0 | K1 | K2);
         n[2] = n2 ^ (X2 | K1 | K2 | K3);
@@ -116,12 +119,17 @@ LGCA_HDI void collide_fhp(uint64_t n[7], uint64_t p)
     }
 }
 
+template <int MODEL, class Word>
+LGCA_HDI void collide_w(Word *n, Word p)
+{
+    if (MODEL == M_HPP) collide_hpp<Word>(n);
+    else if (MODEL == M_FHP_I) collide_fhp<false, Word>(n, p);
+    else collide_fhp<true, Word>(n, p);
+}
 template <int MODEL>
 LGCA_HDI void collide(uint64_t *n, uint64_t p)
 {
-    if (MODEL == M_HPP) collide_hpp(n);
-    else if (MODEL == M_FHP_I) collide_fhp<false>(n, p);
-    else collide_fhp<true>(n, p);
+    collide_w<MODEL, uint64_t>(n, p);
 }
 
 // Inverse and mirror direction tables (src/lgca_models.h:44-48 HPP,

@@ -190,6 +190,7 @@ struct ResidentShape {
     size_t halo_words;
 };
 static constexpr size_t RES_MAX_SMEM = 200 * 1024;
+static constexpr int RESIDENT_MIN_STEPS = 8;  // fewest steps of a call the automatic choice gives it
 bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out);
 cudaError_t launch_resident(int model, int geom_mode, const StepArgs &a, const ResidentShape &sh,
                             uint64_t *halo, int *err, uint64_t seed, uint64_t t0,

@@ -612,8 +612,16 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
         h->t += (uint64_t)nsteps;
         return LGCA_OK;
     }
+    // the resident form: asked for, or chosen for calls of several steps on
+    // lattices it holds with at least half of every warp's lanes busy
     ResidentShape rs;
-    if (nsteps > 0 && h->variant == VARIANT_RESIDENT && resident_shape(h->model, h->g, rs)) {
+    const bool resident =
+        nsteps > 0 &&
+        (h->variant == VARIANT_RESIDENT ||
+         (h->variant == VARIANT_AUTO && h->depth == 1 && nsteps >= RESIDENT_MIN_STEPS &&
+          h->g.nw / 2 >= 16)) &&
+        resident_shape(h->model, h->g, rs);
+    if (resident) {
         if (const int fst = error_flag(h)) return fst;
         const size_t halo_bytes = rs.halo_words * sizeof(uint64_t);
         if (!h->res) {

@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
 
     // the row's state at the launch's first step
     uint64_t s[2][7] = {};
-    uint64_t solid[2] = {0, 0}, slip[2] = {0, 0}, fz[2] = {0, 0};
+    uint64_t solid[2] = {0, 0}, slip[2] = {0, 0};
     if (active) {
 #pragma unroll
         for (int d = 0; d < D; ++d) {
@@ -169,21 +169,21 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
             slip[0] = v.x;
             slip[1] = v.y;
         }
-        if (a.chir) {
-            const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(a.chir + row0 + w0));
-            fz[0] = v.x;
-            fz[1] = v.y;
-        }
     }
     // warps without wall or obstacle cells skip the boundary multiplexer
     const bool walls = GM != GEOM_NONE &&
                        __any_sync(FULL, (solid[0] | solid[1] | slip[0] | slip[1]) != 0ull);
 
     // forcing flips of one step on the registers (the owner of the column)
-    auto force = [&](uint64_t fkey) {
-        if (!fowner) return;
+    // (the draw of a step: does the forcing column flip in this row)
+    auto force_draw = [&](uint64_t fkey) -> bool {
+        if (!fowner) return false;
         const uint64_t u = lgca_rng_draw(fkey, lgca_rng_index((uint32_t)y, (uint32_t)a.fx)) >> 32;
-        const uint64_t bit = (u < a.force_thr) ? (1ull << (a.fx & 63)) : 0ull;
+        return u < a.force_thr;
+    };
+    auto force = [&](bool flip) {
+        if (!flip) return;
+        const uint64_t bit = 1ull << (a.fx & 63);
         const uint64_t m0 = (fw & 1) ? 0ull : bit, m1 = (fw & 1) ? bit : 0ull;
         const uint64_t f0 = ~s[0][0] & s[0][WEST] & ~solid[0] & ~slip[0] & m0;
         const uint64_t f1 = ~s[1][0] & s[1][WEST] & ~solid[1] & ~slip[1] & m1;
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
         }
     };
 
-    force(lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0));
+    force(force_draw(lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0)));
     publish(0u);
     __syncthreads();
     if (ctl[5]) return;  // an earlier launch gave up: do not step a partial state (block-uniform)
@@ -271,17 +271,14 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
             ctl[cur ^ 1] = lgca_rng_key(R.seed, LGCA_STREAM_CHIR, R.t0 + (uint64_t)j + 1);
             ctl[2 + cur] = lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0 + (uint64_t)j + 2);
         }
-        uint64_t c0 = 0, c1 = 0;
-        if (MODEL != M_HPP) {
-            if (a.chir) {
-                c0 = fz[0];
-                c1 = fz[1];
-            } else {
-                const uint64_t z = ck + lgca_rng_index((uint32_t)y, (uint32_t)w0) * LGCA_RNG_GAMMA;
-                c0 = lgca_mix64(z);
-                c1 = lgca_mix64(z + LGCA_RNG_GAMMA);
-            }
-        }
+        // the forcing draw of the next step, made now, off the step's end
+        const bool flip_next = force_draw(fk);
+        // chirality of word k of the pair, drawn (or, frozen, read) where it is used
+        auto chirality = [&](int k) -> uint64_t {
+            if (MODEL == M_HPP) return 0ull;
+            if (a.chir) return __ldg(a.chir + row0 + w0 + k);
+            return lgca_mix64(ck + lgca_rng_index((uint32_t)y, (uint32_t)(w0 + k)) * LGCA_RNG_GAMMA);
+        };
 
         // ---- gather: own channels from registers, the others from rows y-1, y+1
         uint64_t n[2][7];
@@ -405,33 +402,44 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
             shr(n[0][4], n[1][4], eg[3], q[0][4], q[1][4]);
         }
 
-        // ---- collision and boundaries (as step_body.cuh)
+        // ---- collision and boundaries (as step_body.cuh), on 32-bit halves
+        // of the words: a half's inputs are dead once it is done, which
+        // keeps the boundary multiplexer (inputs and outputs live together)
+        // within the registers of 28 warps per SM
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            uint64_t c[7];
+            const uint64_t chir = chirality(k);
+            const uint64_t ew = (w0 + k == 0 ? 1ull : 0ull) | (w0 + k == nw - 1 ? (1ull << 63) : 0ull);
 #pragma unroll
-            for (int d = 0; d < D; ++d) c[d] = q[k][d];
-            collide<MODEL>(c, k ? c1 : c0);
-            if (GM == GEOM_NONE || !walls) {
+            for (int hf = 0; hf < 2; ++hf) {
+                const int sh = 32 * hf;
+                uint32_t c[7], qh[7];
 #pragma unroll
-                for (int d = 0; d < D; ++d) s[k][d] = c[d];
-            } else {
-                const uint64_t fl = ~(solid[k] | slip[k]);
-                const uint64_t ew = (w0 + k == 0 ? 1ull : 0ull) | (w0 + k == nw - 1 ? (1ull << 63) : 0ull);
+                for (int d = 0; d < D; ++d) c[d] = qh[d] = (uint32_t)(q[k][d] >> sh);
+                collide_w<MODEL, uint32_t>(c, (uint32_t)(chir >> sh));
+                if (GM != GEOM_NONE && walls) {
+                    const uint32_t so = (uint32_t)(solid[k] >> sh), sl = (uint32_t)(slip[k] >> sh);
+                    const uint32_t fl = ~(so | sl), e = (uint32_t)(ew >> sh);
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        uint32_t o = (fl & c[d]) | (so & qh[Dirs<MODEL>::inv(d)]);
+                        if (GM == GEOM_FULL) {
+                            const uint32_t sx = nsrow ? qh[Dirs<MODEL>::mirx(d)] : qh[d];
+                            o |= sl & ((e & qh[Dirs<MODEL>::miry(d)]) | (~e & sx));
+                        }
+                        c[d] = o;
+                    }
+                }
 #pragma unroll
                 for (int d = 0; d < D; ++d) {
-                    uint64_t o = (fl & c[d]) | (solid[k] & q[k][Dirs<MODEL>::inv(d)]);
-                    if (GM == GEOM_FULL) {
-                        const uint64_t sx = nsrow ? q[k][Dirs<MODEL>::mirx(d)] : q[k][d];
-                        o |= slip[k] & ((ew & q[k][Dirs<MODEL>::miry(d)]) | (~ew & sx));
-                    }
-                    s[k][d] = o;
+                    if (hf == 0) s[k][d] = c[d];
+                    else s[k][d] |= (uint64_t)c[d] << 32;
                 }
             }
         }
 
         if (j + 1 < R.nsteps) {
-            force(fk);
+            force(flip_next);
             publish((unsigned)j + 1);
         } else if (active && !ctl[4 + cur]) {
             uint64_t *dp = a.dst + row0 + w0;

@@ -3,6 +3,7 @@ self-contained program for profilers (ncu) and for quick timings.
 
     python -m lgca_gb300.profile_case --model 3 --W 32768 --H 16384 --steps 3
     python -m lgca_gb300.profile_case --geometry karman --W 8192 --H 2048 --force-x 16 --force-p 0.02
+    python -m lgca_gb300.profile_case --geometry karman --W 8192 --H 2048 --force-x 16 --force-p 0.02 --chunk 100
     python -m lgca_gb300.profile_case --batch 512 --steps 4   # the batched workload, one step per call
 
 Prints the average time per step (host clock around the steps and a wait).
@@ -25,7 +26,11 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--depth", type=int, default=1)
     ap.add_argument("--variant", type=int, default=0,
-                    help="0 auto, 1 one step per pass, 2 register wavefront, 3 shared-memory tiles")
+                    help="0 auto, 1 one step per pass, 2 register wavefront, 3 shared-memory tiles, "
+                         "4 persistent bands, 5 two words per lane, 6 resident")
+    ap.add_argument("--chunk", type=int, default=0,
+                    help="steps per call (default: 1, or the depth); the automatic choice takes "
+                         "the resident form for calls of 8 steps or more where it fits")
     ap.add_argument("--geometry", default="periodic", choices=["periodic", "pipe", "karman"])
     ap.add_argument("--force-x", type=int, default=-1)
     ap.add_argument("--force-p", type=float, default=0.0)
@@ -72,14 +77,15 @@ def main(argv=None):
     L.set_kernel_variant(args.variant)
     L.collide_and_propagate(args.warmup)
     L.sync()
+    per_call = args.chunk or (1 if args.depth == 1 else args.depth)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        L.collide_and_propagate(1 if args.depth == 1 else args.depth)
+        L.collide_and_propagate(per_call)
         if args.block:
             L.block_sums(args.block)
     L.sync()
     dt = time.perf_counter() - t0
-    n = args.steps * (1 if args.depth == 1 else args.depth)
+    n = args.steps * per_call
     print(f"{args.W}x{args.H} model {args.model} depth {args.depth} variant {args.variant}: {n} steps, {dt / n * 1e3:.4f} ms/step (host clock), "
           f"{args.W * args.H * n / dt / 1e9:.1f} GSite-updates/s")
     L.close()
