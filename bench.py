@@ -12,8 +12,10 @@ the coarse-graining.  `--steps 100` is the whole 10000-step run.
 Prints one JSON line (rank 0).  `value` is site updates per second of the
 whole job with the lattice resident in HBM; `e2e` is the same metric through
 the C ABI with the state uploaded from / downloaded to pinned host memory
-every step; `roofline` is the step kernel against the measured HBM copy
-bandwidth; `cpu_baseline` is the CPU oracle (the reference algorithm in C,
+every step; `roofline` is the step kernel against its bound (the resident
+kernel that holds the lattice on chip: instruction issue; `roofline_gate` is
+the one-step kernel on a lattice 16x larger against the measured HBM copy
+bandwidth); `cpu_baseline` is the CPU oracle (the reference algorithm in C,
 OpenMP) on this host's cores.  Multi-GPU (torchrun) runs one independent
 lattice per rank (weak scaling; no collective on the data path).
 """
@@ -334,29 +336,50 @@ def run_ours(args):
     sites = W_K * H_K * STEPS_PER_CHUNK * args.steps
     value = sites * ws / t_dev / 1e9
 
-    # roofline of the step kernel: algorithmic bytes per launch / launch time
-    bytes_launch = W_K * H_K * (2 * 7 / 8 + 1 / 8)  # 7 planes read + written, solid plane read
-    launch_s = sum(kern_ms) / 1e3 / (STEPS_PER_CHUNK * args.steps)
-    achieved = bytes_launch / launch_s / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": profiled_traffic("step_fhp3_karman_8192x2048.md"),
-                "peak_kind": peak_kind, "kernel": "k_step2<FHP_II/III, GEOM_NOSLIP> (two words per lane)",
-                "bytes_per_launch": bytes_launch,
-                "note": "state (2 x 14.7 MB) + solid plane stay L2-resident within a step chunk, so "
-                        "this is algorithmic bytes over time, not DRAM traffic; the kernel's bound "
-                        "is ALU issue (see alu_issue); the HBM gate is roofline_gate"}
-    # the same launches against the SMs' instruction issue: warp instructions
-    # per launch (ncu, committed summary) over the launch time, against one
-    # warp instruction per clock per SM sub-partition at the sampled clock
-    inst = profiled_value("step_fhp3_karman_8192x2048.md", "inst_per_launch")
-    if inst:
-        sms = torch.cuda.get_device_properties(dev).multi_processor_count
-        clk_hz = (clk.summary().get("sm_mhz") or 2070) * 1e6
-        roofline["alu_issue"] = {
-            "achieved": inst / launch_s, "peak": sms * 4 * clk_hz, "unit": "warp-instructions/s",
-            "frac": inst / launch_s / (sms * 4 * clk_hz), "inst_per_launch": inst,
-            "note": "ALU pipe 71 % and issue 59 % busy while SMs are active (ncu); the ALU "
-                    "pipe runs logic at half the issue rate"}
+    # roofline of the step kernel.  A call of 100 steps is one launch of the
+    # resident kernel (the plan below says which kernels a call runs); the
+    # lattice stays on chip across its steps, so its bound is instruction
+    # issue, not memory: warp instructions per launch (ncu, committed
+    # summary) over the launch time, against one warp instruction per clock
+    # per SM sub-partition at the sampled clock.
+    family, launches_per_call = L.step_plan(STEPS_PER_CHUNK)
+    launch_s = sum(kern_ms) / 1e3 / (launches_per_call * args.steps)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    clk_hz = (clk.summary().get("sm_mhz") or 2070) * 1e6
+    issue_peak = sms * 4 * clk_hz
+    # algorithmic bytes of the same steps: 7 planes read + written, the solid plane read
+    bytes_step = W_K * H_K * (2 * 7 / 8 + 1 / 8)
+    step_s = sum(kern_ms) / 1e3 / (STEPS_PER_CHUNK * args.steps)
+    if family == 6:
+        prof = "resident_fhp3_karman_8192x2048.md"
+        inst = profiled_value(prof, "inst_per_launch")
+        roofline = {"bound": "alu-issue", "achieved": inst / launch_s if inst else None,
+                    "peak": issue_peak, "unit": "warp-instructions/s",
+                    "frac": inst / launch_s / issue_peak if inst else None,
+                    "traffic": profiled_traffic(prof), "inst_per_launch": inst,
+                    "steps_per_launch": STEPS_PER_CHUNK, "launch_ms": launch_s * 1e3,
+                    "alu_pipe_active": profiled_value(prof, "alu_pipe_active"),
+                    "kernel": "k_resident<FHP_II/III, GEOM_NOSLIP>: 100 steps per launch, the "
+                              "lattice on chip between steps",
+                    "hbm_equivalent": {"bytes_per_step": bytes_step,
+                                       "achieved": bytes_step / step_s / 1e9, "peak": hbm_peak,
+                                       "unit": "GB/s", "peak_kind": peak_kind},
+                    "note": "DRAM traffic per launch is the state read once (ncu); the ALU pipe "
+                            "is two-thirds busy while SMs are active and runs logic at half the "
+                            "issue rate, so frac (issue) near 0.6 is the ALU bound; "
+                            "hbm_equivalent is the algorithmic bytes of the same steps over "
+                            "time, which never reach HBM; the HBM gate is roofline_gate"}
+    else:
+        prof = "step_fhp3_karman_8192x2048.md"
+        inst = profiled_value(prof, "inst_per_launch")
+        achieved = bytes_step / launch_s / 1e9
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": achieved / hbm_peak, "traffic": profiled_traffic(prof),
+                    "peak_kind": peak_kind, "bytes_per_launch": bytes_step,
+                    "kernel": "k_step2<FHP_II/III, GEOM_NOSLIP> (two words per lane)",
+                    "alu_issue": {"achieved": inst / launch_s if inst else None,
+                                  "peak": issue_peak, "unit": "warp-instructions/s",
+                                  "frac": inst / launch_s / issue_peak if inst else None}}
 
     # end to end through the C ABI with host buffers: every bench step is one
     # job -- upload the input state from pinned memory, 100 lattice steps,
@@ -449,7 +472,8 @@ def run_ours(args):
             "wall_s": t_wall, "e2e": e2e, "roofline": roofline, "roofline_gate": gate,
             "batched": batched, "served": served,
             "cpu_baseline": cpu, "clocks": clk.summary(),
-            "gpu_launches": (STEPS_PER_CHUNK + 1) * args.steps,
+            # step-kernel launches of each call (lgca_step_plan) + one block-sum kernel
+            "gpu_launches": (launches_per_call + 1) * args.steps,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -161,6 +161,13 @@ int lgca_set_temporal_depth(lgca_handle h, int depth);
  * No reference counterpart (a scheduling choice of this engine). */
 int lgca_set_kernel_variant(lgca_handle h, int variant);
 
+/* The kernels a call lgca_collide_and_propagate(h, nsteps) would run with the
+ * handle's current settings: *family = 6 (resident), 4 (persistent bands) or
+ * 1 (passes of one or more steps), *launches = the step-kernel launches of
+ * the call (memory-set nodes not counted).  Either pointer may be NULL.
+ * No reference counterpart (introspection of this engine's scheduling). */
+int lgca_step_plan(lgca_handle h, int nsteps, int *family, int *launches);
+
 /* Launch shape of the one-step kernels: warps per block (1, 2, 4 or 8), or 0
  * to choose per launch the largest block whose grid spreads over the SMs with
  * the least wave-quantisation loss.  A tuning knob: results do not depend on

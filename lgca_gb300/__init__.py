@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
             "lgca_set_chirality": (C.c_int, [vp, vp]),
             "lgca_set_temporal_depth": (C.c_int, [vp, C.c_int]),
             "lgca_set_kernel_variant": (C.c_int, [vp, C.c_int]),
+            "lgca_step_plan": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
             "lgca_set_block_warps": (C.c_int, [vp, C.c_int]),
             "lgca_collide_and_propagate": (C.c_int, [vp, C.c_int]),
             "lgca_apply_body_force": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(u64)]),
@@ -264,6 +265,13 @@ class GpuLattice:
         4 persistent bands, 5 one step per pass with two words per lane, 6 resident
         (state on chip across the steps of a call)."""
         _check(self._h, lib().lgca_set_kernel_variant(self._h, int(variant)))
+
+    def step_plan(self, nsteps: int) -> tuple[int, int]:
+        """(kernel family, step-kernel launches) of a call advancing nsteps
+        steps: family 6 resident, 4 persistent bands, 1 passes."""
+        fam, n = C.c_int(), C.c_int()
+        _check(self._h, lib().lgca_step_plan(self._h, int(nsteps), C.byref(fam), C.byref(n)))
+        return fam.value, n.value
 
     def set_step(self, t: int) -> None:
         _check(self._h, lib().lgca_set_step(self._h, int(t)))

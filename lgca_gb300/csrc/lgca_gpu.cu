@@ -582,6 +582,62 @@ int lgca_set_block_warps(lgca_handle h, int warps)
     return LGCA_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// Which kernel family a call of nsteps steps runs (the resident form, the
+// persistent band form, or the per-pass loop); shared by the call itself
+// and lgca_step_plan.
+int step_family(const lgca_lattice *h, int nsteps, ResidentShape *rs)
+{
+    if (h->variant == VARIANT_PERSIST && nsteps > 1) return VARIANT_PERSIST;
+    // the resident form: asked for, or chosen for calls of several steps on
+    // lattices it holds with at least half of every warp's lanes busy
+    ResidentShape tmp;
+    if (nsteps > 0 &&
+        (h->variant == VARIANT_RESIDENT ||
+         (h->variant == VARIANT_AUTO && h->depth == 1 && nsteps >= RESIDENT_MIN_STEPS &&
+          h->g.nw / 2 >= 16)) &&
+        resident_shape(h->model, h->g, rs ? *rs : tmp))
+        return VARIANT_RESIDENT;
+    return VARIANT_PLAIN;
+}
+// Steps per pass of the next pass of the per-pass loop, `left` steps to go.
+int pass_depth(const lgca_lattice *h, int left)
+{
+    int k = std::min(h->depth, left);
+    const bool tile = h->variant == VARIANT_TILE;
+    if (h->variant == VARIANT_PLAIN || h->variant == VARIANT_PLAIN2 ||
+        h->variant == VARIANT_RESIDENT)
+        k = 1;
+    while (k > 1 && !(tile ? multistep_supported(h->model, h->g, k)
+                           : wave_supported(h->model, h->g, k)))
+        --k;
+    return k;
+}
+}  // namespace
+
+extern "C" {
+
+int lgca_step_plan(lgca_handle h, int nsteps, int *family, int *launches)
+{
+    CHECK_VALID(h);
+    if (nsteps < 0) return fail(h, LGCA_ERR_INVALID, "nsteps < 0");
+    const int f = step_family(h, nsteps, nullptr);
+    int n = 0;
+    if (f == VARIANT_PLAIN) {
+        for (int done = 0; done < nsteps; ++n) {
+            const int k = pass_depth(h, nsteps - done);
+            done += k;
+        }
+    } else {
+        n = 1;
+    }
+    if (family) *family = f == VARIANT_PLAIN ? 1 : f;
+    if (launches) *launches = n;
+    return LGCA_OK;
+}
+
 int lgca_collide_and_propagate(lgca_handle h, int nsteps)
 {
     CHECK_HANDLE(h);
@@ -598,7 +654,9 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     a.wpt = (h->variant == VARIANT_PLAIN) ? 1 : h->wpt;
     a.bw = h->bw;
     const int gm = geom_mode(h);
-    if (h->variant == VARIANT_PERSIST && nsteps > 1) {
+    ResidentShape rs;
+    const int family = step_family(h, nsteps, &rs);
+    if (family == VARIANT_PERSIST) {
         const size_t sync_bytes = (size_t)(PERSIST_MAX_BLOCKS + 1) * sizeof(int);
         if (const int fst = error_flag(h)) return fst;
         // step flags start at zero; the error flag keeps an earlier timeout
@@ -612,16 +670,7 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
         h->t += (uint64_t)nsteps;
         return LGCA_OK;
     }
-    // the resident form: asked for, or chosen for calls of several steps on
-    // lattices it holds with at least half of every warp's lanes busy
-    ResidentShape rs;
-    const bool resident =
-        nsteps > 0 &&
-        (h->variant == VARIANT_RESIDENT ||
-         (h->variant == VARIANT_AUTO && h->depth == 1 && nsteps >= RESIDENT_MIN_STEPS &&
-          h->g.nw / 2 >= 16)) &&
-        resident_shape(h->model, h->g, rs);
-    if (resident) {
+    if (family == VARIANT_RESIDENT) {
         if (const int fst = error_flag(h)) return fst;
         const size_t halo_bytes = rs.halo_words * sizeof(uint64_t);
         if (!h->res) {
@@ -644,14 +693,8 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     int done = 0;
     while (done < nsteps) {
         // largest supported depth that fits, else one step per pass
-        int k = std::min(h->depth, nsteps - done);
+        const int k = pass_depth(h, nsteps - done);
         const bool tile = h->variant == VARIANT_TILE;
-        if (h->variant == VARIANT_PLAIN || h->variant == VARIANT_PLAIN2 ||
-            h->variant == VARIANT_RESIDENT)
-            k = 1;
-        while (k > 1 && !(tile ? multistep_supported(h->model, h->g, k)
-                               : wave_supported(h->model, h->g, k)))
-            --k;
         if (k > 1) {
             MultiStepArgs m;
             m.base = a;

@@ -366,3 +366,25 @@ def test_roofline_sweep_kernels_at_1024(gpu, oracle, model, p):
         for depth in (2, 4, 8):
             got = run_gpu(gpu, model, st, 16, seed=3, depth=depth, variant=variant)
             assert np.array_equal(got, want), (variant, depth)
+
+
+def test_step_plan_names_the_kernels_a_call_runs(gpu, oracle):
+    """lgca_step_plan reports the kernel family and launches of a call; the
+    automatic choice takes the resident form for calls of 8 steps or more on
+    lattices it holds, and the call gives the same bits whichever it takes."""
+    W, H = 8192, 2048
+    with gpu.GpuLattice(3, W, H, seed=2) as L:
+        assert L.step_plan(100) == (6, 1)
+        assert L.step_plan(8) == (6, 1)
+        assert L.step_plan(7) == (1, 7)
+        L.set_temporal_depth(4)
+        assert L.step_plan(10)[0] == 1  # passes of up to 4 steps on the wavefront
+        L.set_temporal_depth(1)
+        L.set_kernel_variant(4)
+        assert L.step_plan(10) == (4, 1)
+        L.set_kernel_variant(1)
+        assert L.step_plan(10) == (1, 10)
+    with gpu.GpuLattice(3, 4160, 64, seed=2) as L:  # odd word count: not held
+        assert L.step_plan(100) == (1, 100)
+    with gpu.GpuLattice(3, 32768, 4096, seed=2) as L:  # too many rows per SM
+        assert L.step_plan(100) == (1, 100)
