@@ -226,3 +226,16 @@ def test_postprocess_and_bodyforce_equal_reference(ref):
             a, _ = ref.apply_body_force(m, st, f, types=types, seed=3, call=call, bf_dir=d)
             b = ref.ref_apply_body_force(m, st, f, types=types, seed=3, call=call, bf_dir=d)
             assert np.array_equal(a, b)
+
+
+def test_karman_long_run_port_equals_reference():
+    """The oracle's restatement and the compiled reference, each run over the
+    whole Karman workload (FHP-III 8192x2048, 10000 steps; tests/golden/
+    gen_golden.py --karman-long ref|port), agree on every 32x32 block-sum set
+    (every 100 steps) and every state hash (every 1000 steps)."""
+    ref = load_json("config_karman_long.json")
+    port = load_json("config_karman_long_port.json")
+    assert ref["engine"] == "ref" and port["engine"] == "port"
+    assert len(ref["blocksum_sha"]) == 100 and len(ref["state_sha"]) == 10
+    for k in ("W", "H", "steps", "block", "init_sha", "blocksum_sha", "blocksum_total", "state_sha"):
+        assert port[k] == ref[k], k
