@@ -271,181 +271,183 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
             ctl[cur ^ 1] = lgca_rng_key(R.seed, LGCA_STREAM_CHIR, R.t0 + (uint64_t)j + 1);
             ctl[2 + cur] = lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0 + (uint64_t)j + 2);
         }
-        // the forcing draw of the next step, made now, off the step's end
-        const bool flip_next = force_draw(fk);
-        // chirality of word k of the pair, drawn (or, frozen, read) where it is used
-        auto chirality = [&](int k) -> uint64_t {
-            if (MODEL == M_HPP) return 0ull;
-            if (a.chir) return __ldg(a.chir + row0 + w0 + k);
-            return lgca_mix64(ck + lgca_rng_index((uint32_t)y, (uint32_t)(w0 + k)) * LGCA_RNG_GAMMA);
-        };
+        if (rowok) {  // (warp-uniform: warps past the band's last row only meet the barrier)
+            // the forcing draw of the next step, made now, off the step's end
+            const bool flip_next = force_draw(fk);
+            // chirality of word k of the pair, drawn (or, frozen, read) where it is used
+            auto chirality = [&](int k) -> uint64_t {
+                if (MODEL == M_HPP) return 0ull;
+                if (a.chir) return __ldg(a.chir + row0 + w0 + k);
+                return lgca_mix64(ck + lgca_rng_index((uint32_t)y, (uint32_t)(w0 + k)) * LGCA_RNG_GAMMA);
+            };
 
-        // ---- gather: own channels from registers, the others from rows y-1, y+1
-        uint64_t n[2][7];
+            // ---- gather: own channels from registers, the others from rows y-1, y+1
+            uint64_t n[2][7];
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            n[0][d] = s[0][d];
-            n[1][d] = s[1][d];
-        }
-        // edge words in the order the pulls use them (step_body.cuh):
-        //   FHP, even row: west 0 (row y), 1 (y-1), 5 (y+1); east 3 (row y)
-        //   FHP, odd row:  west 0 (row y); east 3 (row y), 2 (y-1), 4 (y+1)
-        //   HPP:           west 0 (row y); east 2 (row y)
-        uint64_t eg[4] = {0, 0, 0, 0};
-        const uint64_t *own = rows + cur * bufw + (size_t)r * roww;
-        if (MODEL == M_HPP) {
-            if (need_w) eg[0] = own[widx];
-            if (need_e) eg[1] = own[(size_t)2 * nw + eidx];
-        } else if (even) {
-            if (need_w) eg[0] = own[widx];
-            if (need_e) eg[3] = own[(size_t)3 * nw + eidx];
-        } else {
-            if (need_w) eg[0] = own[widx];
-            if (need_e) eg[1] = own[(size_t)3 * nw + eidx];
-        }
-        // row y-1
-        if (top) {
-            uint64_t v[2][2] = {{0, 0}, {0, 0}}, e = 0;
-            // FHP: the edge word is channel 1 west (even rows) or channel 2 east (odd rows)
-            const int ek = MODEL == M_HPP ? -1 : (even ? 0 : 1);
-            if (waiting && !halo_get(halo_slot((unsigned)j, bl, 1), (unsigned)j, ek,
-                                     even ? widx : eidx, even ? need_w : need_e, v, e)) {
-                waiting = false;
-                if (lane == 0) ctl[4 + cur] = 1;
+            for (int d = 0; d < D; ++d) {
+                n[0][d] = s[0][d];
+                n[1][d] = s[1][d];
             }
+            // edge words in the order the pulls use them (step_body.cuh):
+            //   FHP, even row: west 0 (row y), 1 (y-1), 5 (y+1); east 3 (row y)
+            //   FHP, odd row:  west 0 (row y); east 3 (row y), 2 (y-1), 4 (y+1)
+            //   HPP:           west 0 (row y); east 2 (row y)
+            uint64_t eg[4] = {0, 0, 0, 0};
+            const uint64_t *own = rows + cur * bufw + (size_t)r * roww;
+            if (MODEL == M_HPP) {
+                if (need_w) eg[0] = own[widx];
+                if (need_e) eg[1] = own[(size_t)2 * nw + eidx];
+            } else if (even) {
+                if (need_w) eg[0] = own[widx];
+                if (need_e) eg[3] = own[(size_t)3 * nw + eidx];
+            } else {
+                if (need_w) eg[0] = own[widx];
+                if (need_e) eg[1] = own[(size_t)3 * nw + eidx];
+            }
+            // row y-1
+            if (top) {
+                uint64_t v[2][2] = {{0, 0}, {0, 0}}, e = 0;
+                // FHP: the edge word is channel 1 west (even rows) or channel 2 east (odd rows)
+                const int ek = MODEL == M_HPP ? -1 : (even ? 0 : 1);
+                if (waiting && !halo_get(halo_slot((unsigned)j, bl, 1), (unsigned)j, ek,
+                                         even ? widx : eidx, even ? need_w : need_e, v, e)) {
+                    waiting = false;
+                    if (lane == 0) ctl[4 + cur] = 1;
+                }
 #pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                n[0][A0 + k] = v[0][k];
-                n[1][A0 + k] = v[1][k];
-            }
-            if (MODEL != M_HPP) {
-                if (even) eg[1] = e;
-                else eg[2] = e;
-            }
-        } else if (active) {
-            const uint64_t *up = rows + cur * bufw + (size_t)(r - 1) * roww;
+                for (int k = 0; k < NV; ++k) {
+                    n[0][A0 + k] = v[0][k];
+                    n[1][A0 + k] = v[1][k];
+                }
+                if (MODEL != M_HPP) {
+                    if (even) eg[1] = e;
+                    else eg[2] = e;
+                }
+            } else if (active) {
+                const uint64_t *up = rows + cur * bufw + (size_t)(r - 1) * roww;
 #pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(up + (size_t)(A0 + k) * nw + w0);
-                n[0][A0 + k] = v.x;
-                n[1][A0 + k] = v.y;
+                for (int k = 0; k < NV; ++k) {
+                    const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(up + (size_t)(A0 + k) * nw + w0);
+                    n[0][A0 + k] = v.x;
+                    n[1][A0 + k] = v.y;
+                }
+                if (MODEL != M_HPP) {
+                    if (even && need_w) eg[1] = up[(size_t)1 * nw + widx];
+                    if (!even && need_e) eg[2] = up[(size_t)2 * nw + eidx];
+                }
             }
-            if (MODEL != M_HPP) {
-                if (even && need_w) eg[1] = up[(size_t)1 * nw + widx];
-                if (!even && need_e) eg[2] = up[(size_t)2 * nw + eidx];
-            }
-        }
-        // row y+1
-        if (bot) {
-            uint64_t v[2][2] = {{0, 0}, {0, 0}}, e = 0;
-            // FHP: the edge word is channel 5 west (even rows) or channel 4 east (odd rows)
-            const int ek = MODEL == M_HPP ? -1 : (even ? 1 : 0);
-            if (waiting && !halo_get(halo_slot((unsigned)j, br, 0), (unsigned)j, ek,
-                                     even ? widx : eidx, even ? need_w : need_e, v, e)) {
-                waiting = false;
-                if (lane == 0) ctl[4 + cur] = 1;
-            }
+            // row y+1
+            if (bot) {
+                uint64_t v[2][2] = {{0, 0}, {0, 0}}, e = 0;
+                // FHP: the edge word is channel 5 west (even rows) or channel 4 east (odd rows)
+                const int ek = MODEL == M_HPP ? -1 : (even ? 1 : 0);
+                if (waiting && !halo_get(halo_slot((unsigned)j, br, 0), (unsigned)j, ek,
+                                         even ? widx : eidx, even ? need_w : need_e, v, e)) {
+                    waiting = false;
+                    if (lane == 0) ctl[4 + cur] = 1;
+                }
 #pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                n[0][B0 + k] = v[0][k];
-                n[1][B0 + k] = v[1][k];
-            }
-            if (MODEL != M_HPP) {
-                if (even) eg[2] = e;
-                else eg[3] = e;
-            }
-        } else if (active) {
-            const uint64_t *dn = rows + cur * bufw + (size_t)(r + 1) * roww;
+                for (int k = 0; k < NV; ++k) {
+                    n[0][B0 + k] = v[0][k];
+                    n[1][B0 + k] = v[1][k];
+                }
+                if (MODEL != M_HPP) {
+                    if (even) eg[2] = e;
+                    else eg[3] = e;
+                }
+            } else if (active) {
+                const uint64_t *dn = rows + cur * bufw + (size_t)(r + 1) * roww;
 #pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(dn + (size_t)(B0 + k) * nw + w0);
-                n[0][B0 + k] = v.x;
-                n[1][B0 + k] = v.y;
+                for (int k = 0; k < NV; ++k) {
+                    const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(dn + (size_t)(B0 + k) * nw + w0);
+                    n[0][B0 + k] = v.x;
+                    n[1][B0 + k] = v.y;
+                }
+                if (MODEL != M_HPP) {
+                    if (even && need_w) eg[2] = dn[(size_t)5 * nw + widx];
+                    if (!even && need_e) eg[3] = dn[(size_t)4 * nw + eidx];
+                }
             }
-            if (MODEL != M_HPP) {
-                if (even && need_w) eg[2] = dn[(size_t)5 * nw + widx];
-                if (!even && need_e) eg[3] = dn[(size_t)4 * nw + eidx];
-            }
-        }
 
-        // ---- pull: x-1 / x+1 shifts of the pairs (one shuffle each)
-        auto shl = [&](uint64_t v0, uint64_t v1, uint64_t edge, uint64_t &r0, uint64_t &r1) {
-            const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v1 >> 32), 1);
-            const uint64_t in = need_w ? (edge >> 63) : (uint64_t)(hi >> 31);
-            r0 = (v0 << 1) | in;
-            r1 = (v1 << 1) | (v0 >> 63);
-        };
-        auto shr = [&](uint64_t v0, uint64_t v1, uint64_t edge, uint64_t &r0, uint64_t &r1) {
-            const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v0, 1);
-            const uint64_t in = need_e ? (edge & 1ull) : (uint64_t)(lo & 1u);
-            r0 = (v0 >> 1) | (v1 << 63);
-            r1 = (v1 >> 1) | (in << 63);
-        };
-        uint64_t q[2][7];
+            // ---- pull: x-1 / x+1 shifts of the pairs (one shuffle each)
+            auto shl = [&](uint64_t v0, uint64_t v1, uint64_t edge, uint64_t &r0, uint64_t &r1) {
+                const uint32_t hi = __shfl_up_sync(FULL, (uint32_t)(v1 >> 32), 1);
+                const uint64_t in = need_w ? (edge >> 63) : (uint64_t)(hi >> 31);
+                r0 = (v0 << 1) | in;
+                r1 = (v1 << 1) | (v0 >> 63);
+            };
+            auto shr = [&](uint64_t v0, uint64_t v1, uint64_t edge, uint64_t &r0, uint64_t &r1) {
+                const uint32_t lo = __shfl_down_sync(FULL, (uint32_t)v0, 1);
+                const uint64_t in = need_e ? (edge & 1ull) : (uint64_t)(lo & 1u);
+                r0 = (v0 >> 1) | (v1 << 63);
+                r1 = (v1 >> 1) | (in << 63);
+            };
+            uint64_t q[2][7];
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            q[0][d] = n[0][d];
-            q[1][d] = n[1][d];
-        }
-        if (MODEL == M_HPP) {
-            shl(n[0][0], n[1][0], eg[0], q[0][0], q[1][0]);
-            shr(n[0][2], n[1][2], eg[1], q[0][2], q[1][2]);
-        } else if (even) {  // warp-uniform: one row per warp
-            shl(n[0][0], n[1][0], eg[0], q[0][0], q[1][0]);
-            shl(n[0][1], n[1][1], eg[1], q[0][1], q[1][1]);
-            shl(n[0][5], n[1][5], eg[2], q[0][5], q[1][5]);
-            shr(n[0][3], n[1][3], eg[3], q[0][3], q[1][3]);
-        } else {
-            shl(n[0][0], n[1][0], eg[0], q[0][0], q[1][0]);
-            shr(n[0][3], n[1][3], eg[1], q[0][3], q[1][3]);
-            shr(n[0][2], n[1][2], eg[2], q[0][2], q[1][2]);
-            shr(n[0][4], n[1][4], eg[3], q[0][4], q[1][4]);
-        }
+            for (int d = 0; d < D; ++d) {
+                q[0][d] = n[0][d];
+                q[1][d] = n[1][d];
+            }
+            if (MODEL == M_HPP) {
+                shl(n[0][0], n[1][0], eg[0], q[0][0], q[1][0]);
+                shr(n[0][2], n[1][2], eg[1], q[0][2], q[1][2]);
+            } else if (even) {  // warp-uniform: one row per warp
+                shl(n[0][0], n[1][0], eg[0], q[0][0], q[1][0]);
+                shl(n[0][1], n[1][1], eg[1], q[0][1], q[1][1]);
+                shl(n[0][5], n[1][5], eg[2], q[0][5], q[1][5]);
+                shr(n[0][3], n[1][3], eg[3], q[0][3], q[1][3]);
+            } else {
+                shl(n[0][0], n[1][0], eg[0], q[0][0], q[1][0]);
+                shr(n[0][3], n[1][3], eg[1], q[0][3], q[1][3]);
+                shr(n[0][2], n[1][2], eg[2], q[0][2], q[1][2]);
+                shr(n[0][4], n[1][4], eg[3], q[0][4], q[1][4]);
+            }
 
-        // ---- collision and boundaries (as step_body.cuh), on 32-bit halves
-        // of the words: a half's inputs are dead once it is done, which
-        // keeps the boundary multiplexer (inputs and outputs live together)
-        // within the registers of 28 warps per SM
+            // ---- collision and boundaries (as step_body.cuh), on 32-bit halves
+            // of the words: a half's inputs are dead once it is done, which
+            // keeps the boundary multiplexer (inputs and outputs live together)
+            // within the registers of 28 warps per SM
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            const uint64_t chir = chirality(k);
-            const uint64_t ew = (w0 + k == 0 ? 1ull : 0ull) | (w0 + k == nw - 1 ? (1ull << 63) : 0ull);
+            for (int k = 0; k < 2; ++k) {
+                const uint64_t chir = chirality(k);
+                const uint64_t ew = (w0 + k == 0 ? 1ull : 0ull) | (w0 + k == nw - 1 ? (1ull << 63) : 0ull);
 #pragma unroll
-            for (int hf = 0; hf < 2; ++hf) {
-                const int sh = 32 * hf;
-                uint32_t c[7], qh[7];
+                for (int hf = 0; hf < 2; ++hf) {
+                    const int sh = 32 * hf;
+                    uint32_t c[7], qh[7];
 #pragma unroll
-                for (int d = 0; d < D; ++d) c[d] = qh[d] = (uint32_t)(q[k][d] >> sh);
-                collide_w<MODEL, uint32_t>(c, (uint32_t)(chir >> sh));
-                if (GM != GEOM_NONE && walls) {
-                    const uint32_t so = (uint32_t)(solid[k] >> sh), sl = (uint32_t)(slip[k] >> sh);
-                    const uint32_t fl = ~(so | sl), e = (uint32_t)(ew >> sh);
+                    for (int d = 0; d < D; ++d) c[d] = qh[d] = (uint32_t)(q[k][d] >> sh);
+                    collide_w<MODEL, uint32_t>(c, (uint32_t)(chir >> sh));
+                    if (GM != GEOM_NONE && walls) {
+                        const uint32_t so = (uint32_t)(solid[k] >> sh), sl = (uint32_t)(slip[k] >> sh);
+                        const uint32_t fl = ~(so | sl), e = (uint32_t)(ew >> sh);
+#pragma unroll
+                        for (int d = 0; d < D; ++d) {
+                            uint32_t o = (fl & c[d]) | (so & qh[Dirs<MODEL>::inv(d)]);
+                            if (GM == GEOM_FULL) {
+                                const uint32_t sx = nsrow ? qh[Dirs<MODEL>::mirx(d)] : qh[d];
+                                o |= sl & ((e & qh[Dirs<MODEL>::miry(d)]) | (~e & sx));
+                            }
+                            c[d] = o;
+                        }
+                    }
 #pragma unroll
                     for (int d = 0; d < D; ++d) {
-                        uint32_t o = (fl & c[d]) | (so & qh[Dirs<MODEL>::inv(d)]);
-                        if (GM == GEOM_FULL) {
-                            const uint32_t sx = nsrow ? qh[Dirs<MODEL>::mirx(d)] : qh[d];
-                            o |= sl & ((e & qh[Dirs<MODEL>::miry(d)]) | (~e & sx));
-                        }
-                        c[d] = o;
+                        if (hf == 0) s[k][d] = c[d];
+                        else s[k][d] |= (uint64_t)c[d] << 32;
                     }
                 }
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    if (hf == 0) s[k][d] = c[d];
-                    else s[k][d] |= (uint64_t)c[d] << 32;
-                }
             }
-        }
 
-        if (j + 1 < R.nsteps) {
-            force(flip_next);
-            publish((unsigned)j + 1);
-        } else if (active && !ctl[4 + cur]) {
-            uint64_t *dp = a.dst + row0 + w0;
+            if (j + 1 < R.nsteps) {
+                force(flip_next);
+                publish((unsigned)j + 1);
+            } else if (active && !ctl[4 + cur]) {
+                uint64_t *dp = a.dst + row0 + w0;
 #pragma unroll
-            for (int d = 0; d < D; ++d)
-                *reinterpret_cast<ulonglong2 *>(dp + d * ps) = make_ulonglong2(s[0][d], s[1][d]);
+                for (int d = 0; d < D; ++d)
+                    *reinterpret_cast<ulonglong2 *>(dp + d * ps) = make_ulonglong2(s[0][d], s[1][d]);
+            }
         }
         __syncthreads();
         if (ctl[4 + cur]) return;  // a wait of this step gave up (block-uniform)
