@@ -468,8 +468,12 @@ bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out)
     if (g.W % 64 != 0 || (g.nw & 1) || g.H < 1) return false;
     const int np = g.nw / 2;
     const int wpr = (np + 31) / 32;
-    const int nblk = std::min(sm_count(), g.H);
-    const int rpb = (g.H + nblk - 1) / nblk;
+    // the fewest bands of the smallest height the SMs allow: every band has
+    // rpb or rpb - 1 rows, and the SMs left over stay free for other streams'
+    // kernels (e.g. the layout conversions of an upload or a download, which
+    // then overlap the steps)
+    const int rpb = (g.H + std::min(sm_count(), g.H) - 1) / std::min(sm_count(), g.H);
+    const int nblk = (g.H + rpb - 1) / rpb;
     if (rpb * wpr > RES_MAX_WARPS) return false;
     const size_t smem = resident_smem_bytes(model, g, rpb);
     if (smem > RES_MAX_SMEM) return false;
