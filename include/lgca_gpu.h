@@ -181,6 +181,19 @@ int lgca_set_block_warps(lgca_handle h, int warps);
  * ignored there and has no counterpart. */
 int lgca_collide_and_propagate(lgca_handle h, int nsteps);
 
+/* One job on the handle's stream, without waiting: the state from cells_in
+ * (host, dim_x*dim_y bytes as lgca_upload_state; NULL keeps the current
+ * state), nsteps steps, and the result to cells_out (host, as
+ * lgca_download_state_async; NULL: no download); cells_out is valid after
+ * lgca_sync.  The same as those three calls in that order, but where the
+ * resident kernel runs the steps, the byte-per-cell conversions happen
+ * inside its launch (no separate conversion kernels between jobs).  Host
+ * buffers should be pinned for the copies to overlap other work.
+ * Reference counterpart: copy_data_to_device, collide_and_propagate (x
+ * nsteps) and copy_data_from_device + copy_data_to_output_buffer
+ * (src/lattice.cpp:422-441, src/omp_lattice.cpp:100-249). */
+int lgca_run_job_async(lgca_handle h, const uint8_t *cells_in, int nsteps, uint8_t *cells_out);
+
 /* Random-cell body force with the reference's semantics: candidate cells
  * are drawn (FSEQ stream, call counter of the handle) until `forcing`
  * particles were reverted or 2*num_cells draws were made; bf_dir is 'x', 'y'

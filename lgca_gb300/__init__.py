@@ -74,6 +74,7 @@ def lib() -> C.CDLL:
             "lgca_set_temporal_depth": (C.c_int, [vp, C.c_int]),
             "lgca_set_kernel_variant": (C.c_int, [vp, C.c_int]),
             "lgca_step_plan": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+            "lgca_run_job_async": (C.c_int, [vp, vp, C.c_int, vp]),
             "lgca_set_block_warps": (C.c_int, [vp, C.c_int]),
             "lgca_collide_and_propagate": (C.c_int, [vp, C.c_int]),
             "lgca_apply_body_force": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(u64)]),
@@ -233,6 +234,18 @@ class GpuLattice:
         s = np.empty(self.shape, np.uint8) if out is None else out
         _check(self._h, lib().lgca_download_state(self._h, _ptr(s)))
         return s
+
+    def run_job_async(self, cells_in: np.ndarray | None, nsteps: int,
+                      cells_out: np.ndarray | None) -> None:
+        """Upload cells_in (or keep the state), advance nsteps steps and queue
+        the result into cells_out (pinned for overlap; valid after sync()),
+        in one call: where the resident kernel runs the steps, the layout
+        conversions happen inside its launch."""
+        for c in (cells_in, cells_out):
+            assert c is None or (c.shape == self.shape and c.dtype == np.uint8 and
+                                 c.flags.c_contiguous)
+        _check(self._h, lib().lgca_run_job_async(self._h, _ptr(cells_in), int(nsteps),
+                                                 _ptr(cells_out)))
 
     def download_async(self, out: np.ndarray) -> None:
         """Queue a download into `out` (pinned for overlap); valid after sync()."""

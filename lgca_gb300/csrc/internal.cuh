@@ -192,9 +192,13 @@ struct ResidentShape {
 static constexpr size_t RES_MAX_SMEM = 200 * 1024;
 static constexpr int RESIDENT_MIN_STEPS = 8;  // fewest steps of a call the automatic choice gives it
 bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out);
+// aos_in / aos_out (device, H x W bytes, bit d = channel d; either may be
+// null): the launch's input is read from aos_in instead of a.src, and its
+// result is written to aos_out as well as to a.dst.
 cudaError_t launch_resident(int model, int geom_mode, const StepArgs &a, const ResidentShape &sh,
                             uint64_t *halo, int *err, uint64_t seed, uint64_t t0,
-                            int nsteps, const PersistWait &w, cudaStream_t stream);
+                            int nsteps, const PersistWait &w, const uint8_t *aos_in,
+                            uint8_t *aos_out, cudaStream_t stream);
 
 // Kernel families selectable per handle.
 enum : int {

@@ -615,6 +615,47 @@ int pass_depth(const lgca_lattice *h, int left)
         --k;
     return k;
 }
+// Step arguments of the handle (buffers and keys set by the caller).
+StepArgs step_args(const lgca_lattice *h)
+{
+    StepArgs a;
+    a.solid = h->solid;
+    a.slip = h->slip;
+    a.chir = h->frozen ? h->chir : nullptr;
+    a.g = h->g;
+    a.chunks = (h->g.nw + 31) / 32;
+    a.force_thr = h->force_thr;
+    a.fx = h->force_x;
+    a.wpt = (h->variant == VARIANT_PLAIN) ? 1 : h->wpt;
+    a.bw = h->bw;
+    return a;
+}
+// nsteps steps on the resident kernel (shape rs); the input comes from the
+// byte-per-cell device buffer aos_in when it is not null, and the result
+// also goes to aos_out when that is not null.
+int run_resident(lgca_lattice *h, int nsteps, const ResidentShape &rs, const uint8_t *aos_in,
+                 uint8_t *aos_out)
+{
+    if (const int fst = error_flag(h)) return fst;
+    const size_t halo_bytes = rs.halo_words * sizeof(uint64_t);
+    if (!h->res) {
+        int st = dalloc(h, &h->res, halo_bytes, false, "resident halo");
+        if (st) return st;
+    }
+    // items carry the step they belong to: none may survive from an earlier call
+    CK(h, cudaMemsetAsync(h->res, 0, halo_bytes, h->stream));
+    StepArgs a = step_args(h);
+    a.src = h->buf[h->cur];
+    a.dst = h->buf[h->cur ^ 1];
+    const PersistWait w{h->wait_ns, h->withhold};
+    CK(h, launch_resident(h->model, geom_mode(h), a, rs, static_cast<uint64_t *>(h->res), h->sync,
+                          h->seed, h->t, nsteps, w, aos_in, aos_out, h->stream));
+    CK(h, cudaMemcpyAsync(h->sync_err_host, h->sync, sizeof(int), cudaMemcpyDeviceToHost,
+                          h->stream));
+    h->cur ^= 1;
+    h->t += (uint64_t)nsteps;
+    return LGCA_OK;
+}
 }  // namespace
 
 extern "C" {
@@ -643,16 +684,7 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     CHECK_HANDLE(h);
     if (nsteps < 0) return fail(h, LGCA_ERR_INVALID, "nsteps < 0");
     DeviceGuard dg(h->device);
-    StepArgs a;
-    a.solid = h->solid;
-    a.slip = h->slip;
-    a.chir = h->frozen ? h->chir : nullptr;
-    a.g = h->g;
-    a.chunks = (h->g.nw + 31) / 32;
-    a.force_thr = h->force_thr;
-    a.fx = h->force_x;
-    a.wpt = (h->variant == VARIANT_PLAIN) ? 1 : h->wpt;
-    a.bw = h->bw;
+    StepArgs a = step_args(h);
     const int gm = geom_mode(h);
     ResidentShape rs;
     const int family = step_family(h, nsteps, &rs);
@@ -670,26 +702,7 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
         h->t += (uint64_t)nsteps;
         return LGCA_OK;
     }
-    if (family == VARIANT_RESIDENT) {
-        if (const int fst = error_flag(h)) return fst;
-        const size_t halo_bytes = rs.halo_words * sizeof(uint64_t);
-        if (!h->res) {
-            int st = dalloc(h, &h->res, halo_bytes, false, "resident halo");
-            if (st) return st;
-        }
-        // items carry the step they belong to: none may survive from an earlier call
-        CK(h, cudaMemsetAsync(h->res, 0, halo_bytes, h->stream));
-        a.src = h->buf[h->cur];
-        a.dst = h->buf[h->cur ^ 1];
-        const PersistWait w{h->wait_ns, h->withhold};
-        CK(h, launch_resident(h->model, gm, a, rs, static_cast<uint64_t *>(h->res), h->sync,
-                              h->seed, h->t, nsteps, w, h->stream));
-        CK(h, cudaMemcpyAsync(h->sync_err_host, h->sync, sizeof(int), cudaMemcpyDeviceToHost,
-                              h->stream));
-        h->cur ^= 1;
-        h->t += (uint64_t)nsteps;
-        return LGCA_OK;
-    }
+    if (family == VARIANT_RESIDENT) return run_resident(h, nsteps, rs, nullptr, nullptr);
     int done = 0;
     while (done < nsteps) {
         // largest supported depth that fits, else one step per pass
@@ -721,6 +734,34 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
         h->t += 1;
         done += 1;
     }
+    return LGCA_OK;
+}
+
+int lgca_run_job_async(lgca_handle h, const uint8_t *cells_in, int nsteps, uint8_t *cells_out)
+{
+    CHECK_HANDLE(h);
+    if (nsteps < 0) return fail(h, LGCA_ERR_INVALID, "nsteps < 0");
+    DeviceGuard dg(h->device);
+    ResidentShape rs;
+    if (step_family(h, nsteps, &rs) == VARIANT_RESIDENT && (cells_in || cells_out)) {
+        // one launch converts the input, steps and converts the result: the
+        // byte-per-cell buffer is read and rewritten row by row by the warp
+        // that owns the row, so input and output share the scratch buffer
+        const size_t n = (size_t)h->g.W * h->g.H;
+        int st = scratch_reserve(h, n + 64);
+        if (st) return st;
+        uint8_t *aos = static_cast<uint8_t *>(h->scratch);
+        if (cells_in) CK(h, cudaMemcpyAsync(aos, cells_in, n, cudaMemcpyHostToDevice, h->stream));
+        st = run_resident(h, nsteps, rs, cells_in ? aos : nullptr, cells_out ? aos : nullptr);
+        if (st) return st;
+        if (cells_out) CK(h, cudaMemcpyAsync(cells_out, aos, n, cudaMemcpyDeviceToHost, h->stream));
+        return LGCA_OK;
+    }
+    if (cells_in) {
+        if (const int st = lgca_upload_state(h, cells_in)) return st;
+    }
+    if (const int st = lgca_collide_and_propagate(h, nsteps)) return st;
+    if (cells_out) return lgca_download_state_async(h, cells_out);
     return LGCA_OK;
 }
 

@@ -57,7 +57,29 @@ struct ResidentArgs {
     int nblk, wpr, rpb;  // blocks, warps per row, most rows in a band
     uint64_t wait_ns;
     int withhold;  // block that never writes its halo slots (test hook), -1 none
+    // optional byte-per-cell state (the reference's layout: H rows of W
+    // bytes, bit d = channel d): the launch reads its input from aos_in
+    // instead of a.src, and writes its result to aos_out as well as to a.dst
+    const uint8_t *aos_in;
+    uint8_t *aos_out;
 };
+
+// Byte-per-cell <-> bit-plane conversion of 8 cells (the 8 bytes of x, cell
+// i in byte i).  gather8: bit i of the result = bit d of byte i (the
+// masked bits sit 8 apart, and one multiply moves bit 8i to bit 56 + i;
+// every partial product lands on its own bit, so nothing carries into the
+// top byte).  spread8: byte i of the result = bit i of b (b copied into
+// every byte, byte i masked to bit i, then a byte-wise "is non-zero" by
+// adding 0x7f, which cannot carry out of a byte).
+LGCA_HDI uint64_t res_gather8(uint64_t x, int d)
+{
+    return (((x >> d) & 0x0101010101010101ull) * 0x0102040810204080ull) >> 56;
+}
+LGCA_HDI uint64_t res_spread8(uint64_t b)
+{
+    const uint64_t x = (b * 0x0101010101010101ull) & 0x8040201008040201ull;
+    return ((x + 0x7f7f7f7f7f7f7f7full) >> 7) & 0x0101010101010101ull;
+}
 
 static constexpr int RES_HALO_SLOTS = 3;
 
@@ -152,13 +174,43 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
     // the row's state at the launch's first step
     uint64_t s[2][7] = {};
     uint64_t solid[2] = {0, 0}, slip[2] = {0, 0};
+    // input in the byte-per-cell layout: each lane converts its pair's 128
+    // cells (8 x 16 bytes) into planes written to a.dst, which this launch
+    // otherwise touches only with its result, and then loads them back as
+    // planes like any other input (the conversion's registers stay out of
+    // the steps' register allocation)
+    const uint64_t *in = a.src;
+    if (R.aos_in) {
+        if (active) {
+            const uint4 *cells =
+                reinterpret_cast<const uint4 *>(R.aos_in + (size_t)y * (size_t)g.W + (size_t)128 * t);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                uint64_t wd[7] = {};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {  // cells 64k + 16q .. 64k + 16q + 15
+                    const uint4 v = __ldcg(cells + 4 * k + q);
+                    const uint64_t lo = ((uint64_t)v.y << 32) | v.x, hi = ((uint64_t)v.w << 32) | v.z;
+#pragma unroll
+                    for (int d = 0; d < D; ++d)
+                        wd[d] |= (res_gather8(lo, d) | (res_gather8(hi, d) << 8)) << (16 * q);
+                }
+#pragma unroll
+                for (int d = 0; d < D; ++d) a.dst[d * ps + row0 + w0 + k] = wd[d];
+            }
+        }
+        asm volatile("" ::: "memory");
+        in = a.dst;
+    }
     if (active) {
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-            const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(a.src + d * ps + row0 + w0));
+            const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(in + d * ps + row0 + w0));
             s[0][d] = v.x;
             s[1][d] = v.y;
         }
+    }
+    if (active) {
         if (GM >= GEOM_NOSLIP) {
             const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(a.solid + row0 + w0));
             solid[0] = v.x;
@@ -442,15 +494,35 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
             if (j + 1 < R.nsteps) {
                 force(flip_next);
                 publish((unsigned)j + 1);
-            } else if (active && !ctl[4 + cur]) {
-                uint64_t *dp = a.dst + row0 + w0;
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    *reinterpret_cast<ulonglong2 *>(dp + d * ps) = make_ulonglong2(s[0][d], s[1][d]);
             }
         }
         __syncthreads();
         if (ctl[4 + cur]) return;  // a wait of this step gave up (block-uniform)
+    }
+
+    // the result of the last step: the planes, and the byte-per-cell layout
+    // when asked for (after the loop, so that nothing of it stays live there)
+    if (active) {
+        uint64_t *dp = a.dst + row0 + w0;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            *reinterpret_cast<ulonglong2 *>(dp + d * ps) = make_ulonglong2(s[0][d], s[1][d]);
+        if (R.aos_out) {
+            uint8_t *row = R.aos_out + (size_t)y * (size_t)g.W + (size_t)128 * t;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int k = q >> 2, sh = (q & 3) * 16;
+                uint64_t lo = 0, hi = 0;
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    const uint64_t bits = s[k][d] >> sh;
+                    lo |= res_spread8(bits & 0xffull) << d;
+                    hi |= res_spread8((bits >> 8) & 0xffull) << d;
+                }
+                reinterpret_cast<uint4 *>(row)[q] =
+                    make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+            }
+        }
     }
 }
 
@@ -517,7 +589,8 @@ static cudaError_t res_model(int gm, const StepArgs &a, const ResidentShape &sh,
 
 cudaError_t launch_resident(int model, int gm, const StepArgs &a, const ResidentShape &sh,
                             uint64_t *halo, int *err, uint64_t seed, uint64_t t0,
-                            int nsteps, const PersistWait &w, cudaStream_t st)
+                            int nsteps, const PersistWait &w, const uint8_t *aos_in,
+                            uint8_t *aos_out, cudaStream_t st)
 {
     if (w.wait_ns == 0 || nsteps < 1) return cudaErrorInvalidValue;
     ResidentArgs R;
@@ -531,6 +604,8 @@ cudaError_t launch_resident(int model, int gm, const StepArgs &a, const Resident
     R.rpb = sh.rpb;
     R.wait_ns = w.wait_ns;
     R.withhold = w.withhold;
+    R.aos_in = aos_in;
+    R.aos_out = aos_out;
     switch (model) {
     case M_HPP: return res_model<M_HPP>(gm, a, sh, R, st);
     case M_FHP_I: return res_model<M_FHP_I>(gm, a, sh, R, st);

@@ -9,11 +9,14 @@
 // result with the oracle.
 //
 //   resident_emu IN OUT
-//   IN:  int32 model, W, H, steps, force_x, nblk, chunk, withhold;
+//   IN:  int32 model, W, H, steps, force_x, nblk, chunk, withhold, aos;
 //        uint64 seed, t0, force_thr, wait_ns; H*W uint8 cells (bit d = channel d);
 //        H*W uint8 cell types (0 fluid, 1 no-slip, 2 slip)
 //   OUT: int32 err; H*W uint8 cells after `steps` steps, run as launches of
-//        `chunk` steps each
+//        `chunk` steps each (converted from the planes); then, with aos & 2,
+//        the H*W bytes the last launch wrote in the byte-per-cell layout.
+//   aos & 1: the first launch reads its input in the byte-per-cell layout;
+//   aos & 2: every launch also writes its result in that layout.
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -177,11 +180,11 @@ int main(int argc, char **argv)
     }
     FILE *f = std::fopen(argv[1], "rb");
     if (!f) return 2;
-    int32_t hdr[8];
+    int32_t hdr[9];
     uint64_t u[4];
     if (std::fread(hdr, sizeof(hdr), 1, f) != 1 || std::fread(u, sizeof(u), 1, f) != 1) return 2;
     const int model = hdr[0], W = hdr[1], H = hdr[2], steps = hdr[3], fx = hdr[4], nblk = hdr[5],
-              chunk = hdr[6], withhold = hdr[7];
+              chunk = hdr[6], withhold = hdr[7], aos = hdr[8];
     const uint64_t seed = u[0], t0 = u[1], thr = u[2], wait_ns = u[3];
     std::vector<uint8_t> cells((size_t)W * H), types((size_t)W * H);
     if (std::fread(cells.data(), 1, cells.size(), f) != cells.size() ||
@@ -229,6 +232,7 @@ int main(int argc, char **argv)
     a.force_thr = fx >= 0 ? thr : 0;
     a.fx = fx;
     a.wpt = 2;
+    std::vector<uint8_t> aos_in(cells), aos_out((size_t)W * H, 0xff);
     int cur = 0;
     for (int done = 0; done < steps; done += chunk) {
         const int n = std::min(chunk, steps - done);
@@ -246,6 +250,8 @@ int main(int argc, char **argv)
         R.rpb = rpb;
         R.wait_ns = wait_ns;
         R.withhold = withhold;
+        R.aos_in = (done == 0 && (aos & 1)) ? aos_in.data() : nullptr;
+        R.aos_out = (aos & 2) ? aos_out.data() : nullptr;
         if (model == 0) launch_gm<M_HPP>(gm, a, R);
         else if (model == 1) launch_gm<M_FHP_I>(gm, a, R);
         else launch_gm<M_FHP_II>(gm, a, R);
@@ -264,6 +270,7 @@ int main(int argc, char **argv)
     const int32_t e32 = err;
     std::fwrite(&e32, sizeof(e32), 1, o);
     std::fwrite(cells.data(), 1, cells.size(), o);
+    if (aos & 2) std::fwrite(aos_out.data(), 1, aos_out.size(), o);
     std::fclose(o);
     return 0;
 }

@@ -388,3 +388,37 @@ def test_step_plan_names_the_kernels_a_call_runs(gpu, oracle):
         assert L.step_plan(100) == (1, 100)
     with gpu.GpuLattice(3, 32768, 4096, seed=2) as L:  # too many rows per SM
         assert L.step_plan(100) == (1, 100)
+
+
+@pytest.mark.parametrize("model", [0, 1, 3])
+def test_run_job_equals_upload_steps_download(gpu, oracle, model):
+    """lgca_run_job_async (state in, steps, state out in one call; the
+    resident kernel converts the byte-per-cell layout inside its launch) gives
+    the oracle's bits, on lattices the resident kernel holds and on others,
+    with and without input and output buffers, twice in a row on one handle."""
+    import torch
+    rng = np.random.default_rng(model + 40)
+    for W, H, geom in [(4096, 40, "karman"), (8192, 300, "pipe"), (4160, 40, "periodic"),
+                       (2048, 2048, "disc")]:
+        types = GEOMS[geom](W, H)
+        seed = int(rng.integers(1 << 40))
+        st = oracle.init_bernoulli(model, W, H, types, seed=seed, p_move=0.35, p_rest=0.3)
+        kw = dict(types=types, seed=seed, force_x=W - 1, force_p=0.5)
+        want1 = oracle.run(model, st, 12, **kw)
+        want2 = oracle.run(model, want1, 9, t0=12, **kw)
+        pin = lambda: torch.empty((H, W), dtype=torch.uint8, pin_memory=True).numpy()
+        src, out1, out2 = pin(), pin(), pin()
+        src[:] = st | np.uint8((0xff << oracle.NUM_DIR[model]) & 0xff)  # bits above the channels ignored
+        with gpu.GpuLattice(model, W, H, seed) as L:
+            L.set_cell_types(types)
+            L.set_forcing_column(W - 1, 0.5)
+            L.run_job_async(src, 12, out1)
+            L.run_job_async(None, 9, out2)
+            L.sync()
+            assert np.array_equal(out1, want1), (W, H, geom)
+            assert np.array_equal(out2, want2), (W, H, geom)
+            assert np.array_equal(L.download(), want2)
+            assert L.step_count == 21
+            L.set_step(0)
+            L.run_job_async(src, 12, None)
+            assert np.array_equal(L.download(), want1)

@@ -324,19 +324,22 @@ def resident_emu(tmp_path_factory):
 
 
 def run_resident(exe, tmp, model, cells, types, steps, seed, t0, force_x, force_thr, nblk,
-                 chunk, withhold=-1, wait_ns=10_000_000_000):
+                 chunk, withhold=-1, wait_ns=10_000_000_000, aos=0):
     H, W = cells.shape
     inp, out = tmp / "rin.bin", tmp / "rout.bin"
     with open(inp, "wb") as f:
-        f.write(struct.pack("<8i4Q", model, W, H, steps, force_x, nblk, chunk, withhold, seed, t0,
-                            force_thr, wait_ns))
+        f.write(struct.pack("<9i4Q", model, W, H, steps, force_x, nblk, chunk, withhold, aos, seed,
+                            t0, force_thr, wait_ns))
         f.write(np.ascontiguousarray(cells, np.uint8).tobytes())
         f.write(np.ascontiguousarray(types, np.uint8).tobytes())
     r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True, env=ENV, timeout=600)
     assert r.returncode == 0, (r.returncode, r.stderr[-800:])
     raw = out.read_bytes()
     err = struct.unpack("<i", raw[:4])[0]
-    return err, np.frombuffer(raw[4:], np.uint8).reshape(H, W)
+    got = np.frombuffer(raw[4:4 + H * W], np.uint8).reshape(H, W)
+    if aos & 2:
+        return err, got, np.frombuffer(raw[4 + H * W:], np.uint8).reshape(H, W)
+    return err, got
 
 
 # (W, H, blocks): one and two warps per row, a row of a single word pair,
@@ -369,6 +372,14 @@ def test_emulated_resident_kernel_equals_oracle(resident_emu, tmp_path, oracle, 
                                         6, 13, 9, fx, thr, nblk, chunk)
                 assert err == 0
                 assert np.array_equal(got, want), (model, geom, W, H, nblk, fx, chunk)
+            # input read and result written in the byte-per-cell layout by the
+            # launch itself (garbage in the bits above the model's channels)
+            noisy = st | np.uint8((0xff << oracle.NUM_DIR[model]) & 0xff)
+            err, got, aos_out = run_resident(resident_emu, tmp_path, model, noisy,
+                                             types.astype(np.uint8), 6, 13, 9, fx, thr, nblk, 4,
+                                             aos=3)
+            assert err == 0
+            assert np.array_equal(got, want) and np.array_equal(aos_out, want), (model, W, H)
 
 
 def test_emulated_resident_kernel_stays_in_bounds(tmp_path, oracle):
