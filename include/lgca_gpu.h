@@ -144,9 +144,10 @@ int lgca_set_chirality(lgca_handle h, const uint8_t *field);
 int lgca_set_temporal_depth(lgca_handle h, int depth);
 
 /* Kernel family for the steps: 0 = automatic (default: the resident form 6
- * for calls of 8 or more steps on lattices it holds with rows of at least
- * 2048 sites, else one step per pass, or the register wavefront when a
- * temporal depth above 1 is set), 1 = one step per
+ * for calls of 16 or more steps on lattices it holds with rows of at least
+ * 2048 sites and at least 1024 rows x ceil(dim_x / 4096), else one step per
+ * pass, or the register wavefront when a temporal depth above 1 is set),
+ * 1 = one step per
  * pass only, 2 = register wavefront (several steps per pass), 3 = shared-
  * memory tiles (several steps per pass), 4 = persistent (all steps of a call
  * in one cooperative launch; each block owns a band of rows and waits, with a

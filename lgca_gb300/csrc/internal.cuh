@@ -190,7 +190,10 @@ struct ResidentShape {
     size_t halo_words;
 };
 static constexpr size_t RES_MAX_SMEM = 200 * 1024;
-static constexpr int RESIDENT_MIN_STEPS = 8;  // fewest steps of a call the automatic choice gives it
+// the automatic choice gives the resident form calls of at least this many
+// steps on lattices of at least this many warp rows (rows x warps per row)
+static constexpr int RESIDENT_MIN_STEPS = 16;
+static constexpr long long RESIDENT_MIN_WARPS = 1024;
 bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out);
 // aos_in / aos_out (device, H x W bytes, bit d = channel d; either may be
 // null): the launch's input is read from aos_in instead of a.src, and its

@@ -591,14 +591,17 @@ namespace {
 int step_family(const lgca_lattice *h, int nsteps, ResidentShape *rs)
 {
     if (h->variant == VARIANT_PERSIST && nsteps > 1) return VARIANT_PERSIST;
-    // the resident form: asked for, or chosen for calls of several steps on
-    // lattices it holds with at least half of every warp's lanes busy
+    // the resident form: asked for, or chosen for calls of enough steps to
+    // repay its launch on lattices it holds with at least half of every
+    // warp's lanes busy and enough warps to fill the SMs (measured on GB300:
+    // below about 1024 warp rows, or 16 steps per call, chained one-step
+    // launches are as fast or faster)
     ResidentShape tmp;
-    if (nsteps > 0 &&
-        (h->variant == VARIANT_RESIDENT ||
-         (h->variant == VARIANT_AUTO && h->depth == 1 && nsteps >= RESIDENT_MIN_STEPS &&
-          h->g.nw / 2 >= 16)) &&
-        resident_shape(h->model, h->g, rs ? *rs : tmp))
+    ResidentShape &shape = rs ? *rs : tmp;
+    if (nsteps <= 0 || !resident_shape(h->model, h->g, shape)) return VARIANT_PLAIN;
+    if (h->variant == VARIANT_RESIDENT) return VARIANT_RESIDENT;
+    if (h->variant == VARIANT_AUTO && h->depth == 1 && nsteps >= RESIDENT_MIN_STEPS &&
+        h->g.nw / 2 >= 16 && (long long)h->g.H * shape.wpr >= RESIDENT_MIN_WARPS)
         return VARIANT_RESIDENT;
     return VARIANT_PLAIN;
 }

@@ -370,13 +370,13 @@ def test_roofline_sweep_kernels_at_1024(gpu, oracle, model, p):
 
 def test_step_plan_names_the_kernels_a_call_runs(gpu, oracle):
     """lgca_step_plan reports the kernel family and launches of a call; the
-    automatic choice takes the resident form for calls of 8 steps or more on
-    lattices it holds, and the call gives the same bits whichever it takes."""
+    automatic choice takes the resident form for calls of 16 steps or more on
+    lattices it holds that fill the SMs."""
     W, H = 8192, 2048
     with gpu.GpuLattice(3, W, H, seed=2) as L:
         assert L.step_plan(100) == (6, 1)
-        assert L.step_plan(8) == (6, 1)
-        assert L.step_plan(7) == (1, 7)
+        assert L.step_plan(16) == (6, 1)
+        assert L.step_plan(15) == (1, 15)
         L.set_temporal_depth(4)
         assert L.step_plan(10)[0] == 1  # passes of up to 4 steps on the wavefront
         L.set_temporal_depth(1)
@@ -386,6 +386,10 @@ def test_step_plan_names_the_kernels_a_call_runs(gpu, oracle):
         assert L.step_plan(10) == (1, 10)
     with gpu.GpuLattice(3, 4160, 64, seed=2) as L:  # odd word count: not held
         assert L.step_plan(100) == (1, 100)
+    with gpu.GpuLattice(3, 4096, 256, seed=2) as L:  # held, but too few warps to pay
+        assert L.step_plan(100) == (1, 100)
+        L.set_kernel_variant(6)
+        assert L.step_plan(100) == (6, 1)
     with gpu.GpuLattice(3, 32768, 4096, seed=2) as L:  # too many rows per SM
         assert L.step_plan(100) == (1, 100)
 
@@ -409,16 +413,20 @@ def test_run_job_equals_upload_steps_download(gpu, oracle, model):
         pin = lambda: torch.empty((H, W), dtype=torch.uint8, pin_memory=True).numpy()
         src, out1, out2 = pin(), pin(), pin()
         src[:] = st | np.uint8((0xff << oracle.NUM_DIR[model]) & 0xff)  # bits above the channels ignored
-        with gpu.GpuLattice(model, W, H, seed) as L:
-            L.set_cell_types(types)
-            L.set_forcing_column(W - 1, 0.5)
-            L.run_job_async(src, 12, out1)
-            L.run_job_async(None, 9, out2)
-            L.sync()
-            assert np.array_equal(out1, want1), (W, H, geom)
-            assert np.array_equal(out2, want2), (W, H, geom)
-            assert np.array_equal(L.download(), want2)
-            assert L.step_count == 21
-            L.set_step(0)
-            L.run_job_async(src, 12, None)
-            assert np.array_equal(L.download(), want1)
+        for variant in (0, 6):  # automatic (separate calls here), resident (conversions in the launch)
+            out1[:] = 0
+            out2[:] = 0
+            with gpu.GpuLattice(model, W, H, seed) as L:
+                L.set_cell_types(types)
+                L.set_forcing_column(W - 1, 0.5)
+                L.set_kernel_variant(variant)
+                L.run_job_async(src, 12, out1)
+                L.run_job_async(None, 9, out2)
+                L.sync()
+                assert np.array_equal(out1, want1), (W, H, geom, variant)
+                assert np.array_equal(out2, want2), (W, H, geom, variant)
+                assert np.array_equal(L.download(), want2)
+                assert L.step_count == 21
+                L.set_step(0)
+                L.run_job_async(src, 12, None)
+                assert np.array_equal(L.download(), want1)
