@@ -270,7 +270,11 @@ def served_leg(rate, duration):
             "x_fcfs_measured": r.get("throughput_speedup_vs_fcfs_measured"),
             "sample_verified": r.get("sample_verified"),
             "sample_bit_exact": r.get("sample_bit_exact"),
-            "evictions": r["evictions"], "batch_calls": r["batch_calls"]}
+            "evictions": r["evictions"], "batch_calls": r["batch_calls"],
+            "limited_by": "the batch step kernel (k_batch_persist), at 0.90 of the measured HBM "
+                          "bandwidth on a 1 G-site mix (profiles/batch_512_mixed.md); FCFS runs "
+                          "each job alone with the fastest single-lattice path, the resident "
+                          "kernel for jobs of 1024+ warp rows"}
 
 
 def run_ours(args):
