@@ -3,8 +3,10 @@
 Workload: fully periodic lattices, no obstacles; models HPP, FHP-I, FHP-II,
 FHP-III; sizes 4096x4096, 16384x8192 and 32768x16384; Bernoulli occupation
 p in {0.1, 0.5} on every channel, seed 3; steps per HBM pass k in {1, 2, 4,
-8} -- k = 1 with the one-step kernel, k > 1 with the register wavefront
-(variant 2; FHP up to k = 4) and with shared-memory tiles (variant 3).
+8} -- k = 1 with the one-step kernel (variant 5) and, where the lattice fits
+it, the resident kernel (variant 6: every step of the run on chip, no HBM
+traffic between steps), k > 1 with the register wavefront (variant 2; FHP
+up to k = 4) and with shared-memory tiles (variant 3).
 Each case runs `steps` steps (default 2000) timed with CUDA events on the
 lattice's stream after a warm-up.
 
@@ -66,17 +68,20 @@ def sweep(sizes=SIZES, models=(0, 1, 2, 3), probs=PROBS, depths=DEPTHS, steps: i
             for p in probs:
                 L.init_random(p, p)
                 for depth in depths:
-                    for variant in ((0,) if depth == 1 else (2, 3)):
+                    for variant in ((5, 6) if depth == 1 else (2, 3)):
                         if variant == 2 and depth == 8 and model != 0:
                             continue  # the FHP wavefront holds at most 4 time levels
                         L.set_kernel_variant(variant)
                         L.set_temporal_depth(depth)
+                        if variant == 6 and L.step_plan(steps)[0] != 6:
+                            continue  # the lattice does not fit the resident kernel
                         n = max(depth, steps // depth * depth)
                         t = time_case(L, torch, n, depth)
                         bytes_site = 2 * NUM_DIR[model] / 8 / depth
                         gbs = W * H * bytes_site / t / 1e9
                         rows.append({"W": W, "H": H, "model": model, "p": p, "depth": depth,
-                                     "kernel": {0: "one-step", 2: "wavefront", 3: "tiles"}[variant],
+                                     "kernel": {5: "one-step", 6: "resident", 2: "wavefront",
+                                                3: "tiles"}[variant],
                                      "ms_per_step": t * 1e3, "gsite_updates_s": W * H / t / 1e9,
                                      "gbs": gbs, "frac": gbs / peak, "peak_gbs": peak,
                                      "peak_kind": kind})
