@@ -4,7 +4,8 @@ Two tables, both chosen by timing candidates on the GPU:
 
 * single lattice, per (model, size class): kernel family and steps per pass
   over global memory -- one step per pass with one or two words per lane,
-  register wavefront or shared-memory tiles with 2, 4 or 8 steps per pass;
+  register wavefront or shared-memory tiles with 2, 4 or 8 steps per pass,
+  or the resident kernel (every step of a call on chip) where it fits;
 * batch members, per (model family, size class): the batched one-step
   kernel with one or two words per lane, or the batched register wavefront
   with 2, 4 or 8 steps per pass (8 for HPP only).
@@ -25,9 +26,11 @@ import lgca_gb300 as gpu
 
 # (variant, depth, warps per block): 5 = one step per pass, two words per
 # lane; 1 = one word per lane; 2 = register wavefront; 3 = shared-memory
-# tiles.  Warps per block applies to the one-step kernels (0 = per launch).
+# tiles; 6 = resident (one step per pass where the lattice does not fit it).
+# Warps per block applies to the one-step kernels (0 = per launch).
 SINGLE_CANDIDATES = [(5, 1, 4), (5, 1, 8), (5, 1, 2), (1, 1, 4), (1, 1, 2),
-                     (2, 2, 0), (2, 4, 0), (2, 8, 0), (3, 2, 0), (3, 4, 0), (3, 8, 0)]
+                     (2, 2, 0), (2, 4, 0), (2, 8, 0), (3, 2, 0), (3, 4, 0), (3, 8, 0),
+                     (6, 1, 0)]
 # (kernel variant, steps per pass) of a batch member: one step per launch
 # with two or one words per lane, or passes of 2, 4, 8 steps on the wavefront
 BATCH_CANDIDATES = [(5, 1), (1, 1), (2, 2), (2, 4), (2, 8)]
