@@ -635,7 +635,11 @@ StepArgs step_args(const lgca_lattice *h)
 }
 // nsteps steps on the resident kernel (shape rs); the input comes from the
 // byte-per-cell device buffer aos_in when it is not null, and the result
-// also goes to aos_out when that is not null.
+// also goes to aos_out when that is not null.  RESIDENT_UNAVAILABLE when
+// the device cannot hold the launch's blocks at once right now (e.g. a
+// share of the SMs under MPS): nothing was stepped, and the caller takes
+// one step per pass instead.
+constexpr int RESIDENT_UNAVAILABLE = -1;
 int run_resident(lgca_lattice *h, int nsteps, const ResidentShape &rs, const uint8_t *aos_in,
                  uint8_t *aos_out)
 {
@@ -651,8 +655,14 @@ int run_resident(lgca_lattice *h, int nsteps, const ResidentShape &rs, const uin
     a.src = h->buf[h->cur];
     a.dst = h->buf[h->cur ^ 1];
     const PersistWait w{h->wait_ns, h->withhold};
-    CK(h, launch_resident(h->model, geom_mode(h), a, rs, static_cast<uint64_t *>(h->res), h->sync,
-                          h->seed, h->t, nsteps, w, aos_in, aos_out, h->stream));
+    const cudaError_t e = launch_resident(h->model, geom_mode(h), a, rs,
+                                          static_cast<uint64_t *>(h->res), h->sync, h->seed, h->t,
+                                          nsteps, w, aos_in, aos_out, h->stream);
+    if (e == cudaErrorCooperativeLaunchTooLarge) {
+        cudaGetLastError();  // (not sticky: the context stays usable)
+        return RESIDENT_UNAVAILABLE;
+    }
+    CK(h, e);
     CK(h, cudaMemcpyAsync(h->sync_err_host, h->sync, sizeof(int), cudaMemcpyDeviceToHost,
                           h->stream));
     h->cur ^= 1;
@@ -705,7 +715,10 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
         h->t += (uint64_t)nsteps;
         return LGCA_OK;
     }
-    if (family == VARIANT_RESIDENT) return run_resident(h, nsteps, rs, nullptr, nullptr);
+    if (family == VARIANT_RESIDENT) {
+        const int st = run_resident(h, nsteps, rs, nullptr, nullptr);
+        if (st != RESIDENT_UNAVAILABLE) return st;
+    }
     int done = 0;
     while (done < nsteps) {
         // largest supported depth that fits, else one step per pass
@@ -756,6 +769,12 @@ int lgca_run_job_async(lgca_handle h, const uint8_t *cells_in, int nsteps, uint8
         uint8_t *aos = static_cast<uint8_t *>(h->scratch);
         if (cells_in) CK(h, cudaMemcpyAsync(aos, cells_in, n, cudaMemcpyHostToDevice, h->stream));
         st = run_resident(h, nsteps, rs, cells_in ? aos : nullptr, cells_out ? aos : nullptr);
+        if (st == RESIDENT_UNAVAILABLE) {  // the copied input converted here, then the plain path
+            if (cells_in)
+                CK(h, launch_aos_to_planes(h->D, h->g, aos, h->buf[h->cur], h->stream));
+            if ((st = lgca_collide_and_propagate(h, nsteps))) return st;
+            return cells_out ? lgca_download_state_async(h, cells_out) : LGCA_OK;
+        }
         if (st) return st;
         if (cells_out) CK(h, cudaMemcpyAsync(cells_out, aos, n, cudaMemcpyDeviceToHost, h->stream));
         return LGCA_OK;
