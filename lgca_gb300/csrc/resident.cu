@@ -36,6 +36,13 @@
 // memory, so that every lane that pulls the forced words sees them; the
 // state written back to global memory after the last step carries no flips.
 //
+// Input and output may also be in the reference's byte-per-cell layout
+// (lgca_run_job_async): each lane converts its own 128 cells in the launch's
+// first and last moments, so no conversion kernel runs between jobs.
+//
+// The launcher takes the fewest bands of the smallest height the SMs allow,
+// which leaves a few SMs free for other streams' kernels.
+//
 // Synchronisation per step: one block barrier, plus the edge warps' waits.
 // Every wait is bounded (wait_ns, measured with %globaltimer): past it, or
 // when another block has given up, a warp records the error in *err, the
@@ -226,13 +233,15 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
     const bool walls = GM != GEOM_NONE &&
                        __any_sync(FULL, (solid[0] | solid[1] | slip[0] | slip[1]) != 0ull);
 
-    // forcing flips of one step on the registers (the owner of the column)
-    // (the draw of a step: does the forcing column flip in this row)
+    // the forcing draw of a step: does the forcing column flip in this row
+    // (the owner of the column's word only)
     auto force_draw = [&](uint64_t fkey) -> bool {
         if (!fowner) return false;
         const uint64_t u = lgca_rng_draw(fkey, lgca_rng_index((uint32_t)y, (uint32_t)a.fx)) >> 32;
         return u < a.force_thr;
     };
+    // that flip applied to the registers: a fluid cell with channel 0 empty
+    // and the west-moving channel occupied reverses it
     auto force = [&](bool flip) {
         if (!flip) return;
         const uint64_t bit = 1ull << (a.fx & 63);
