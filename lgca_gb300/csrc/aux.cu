@@ -282,12 +282,24 @@ static cudaError_t block_sums_model(const PlaneGeom &g, const uint64_t *planes, 
                                     int32_t *Jx2, int32_t *Jy, cudaStream_t s)
 {
     const int Wb = (g.W + B - 1) / B, Hb = (g.H + B - 1) / B;
-    const unsigned seg_grid = grid_for((long long)Hb * g.nw, 128);
+    auto seg_grid = [&](long long warps) { return grid_for(warps * 32, 128); };
     switch (B) {
-    case 8: k_block_sums_seg<MODEL, 8><<<seg_grid, 128, 0, s>>>(g, planes, Wb, Hb, N, Jx2, Jy); break;
-    case 16: k_block_sums_seg<MODEL, 16><<<seg_grid, 128, 0, s>>>(g, planes, Wb, Hb, N, Jx2, Jy); break;
-    case 32: k_block_sums_seg<MODEL, 32><<<seg_grid, 128, 0, s>>>(g, planes, Wb, Hb, N, Jx2, Jy); break;
-    case 64: k_block_sums_seg<MODEL, 64><<<seg_grid, 128, 0, s>>>(g, planes, Wb, Hb, N, Jx2, Jy); break;
+    case 8:
+        k_block_sums_seg<MODEL, 8><<<seg_grid(seg_block_sums_warps<8>(g.nw, Hb)), 128, 0, s>>>(
+            g, planes, Wb, Hb, N, Jx2, Jy);
+        break;
+    case 16:
+        k_block_sums_seg<MODEL, 16><<<seg_grid(seg_block_sums_warps<16>(g.nw, Hb)), 128, 0, s>>>(
+            g, planes, Wb, Hb, N, Jx2, Jy);
+        break;
+    case 32:
+        k_block_sums_seg<MODEL, 32><<<seg_grid(seg_block_sums_warps<32>(g.nw, Hb)), 128, 0, s>>>(
+            g, planes, Wb, Hb, N, Jx2, Jy);
+        break;
+    case 64:
+        k_block_sums_seg<MODEL, 64><<<seg_grid(seg_block_sums_warps<64>(g.nw, Hb)), 128, 0, s>>>(
+            g, planes, Wb, Hb, N, Jx2, Jy);
+        break;
     default:
         if (B % 64 == 0 && B <= 2048 && ((B / 64) & (B / 64 - 1)) == 0) {
             const int K = B / 64, chunks = (g.nw + 31) / 32;

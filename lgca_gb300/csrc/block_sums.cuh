@@ -34,32 +34,59 @@ __device__ __forceinline__ void accum_counts(const uint64_t *v, uint64_t m, int 
     }
 }
 
-// B divides 64: one thread per (block row, word); S = 64/B blocks per word.
+// B divides 64 (B >= 8): S = 64/B blocks per word.  A warp takes 32/QG
+// consecutive words of one block row; the QG consecutive lanes of a word
+// split the block's B rows into groups of 8, and their sums are added by
+// shuffles.  Launch: seg_block_sums_warps(...) warps.
+template <int B>
+__host__ __device__ __forceinline__ long long seg_block_sums_warps(int nw, int Hb)
+{
+    constexpr int WPW = 32 / (B / 8);  // words per warp
+    return (long long)Hb * ((nw + WPW - 1) / WPW);
+}
 template <int MODEL, int B>
 __global__ void k_block_sums_seg(PlaneGeom g, const uint64_t *__restrict__ planes, int Wb, int Hb,
                                  int32_t *__restrict__ N, int32_t *__restrict__ Jx2,
                                  int32_t *__restrict__ Jy)
 {
+    static_assert(B >= 8 && 64 % B == 0, "B divides 64");
     constexpr int D = ModelTraits<MODEL>::D;
-    constexpr int S = 64 / B;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)Hb * g.nw) return;
-    const int by = (int)(idx / g.nw), w = (int)(idx - (long long)by * g.nw);
+    constexpr int S = 64 / B, QG = B / 8, WPW = 32 / QG;
+    const int wchunks = (g.nw + WPW - 1) / WPW;
+    const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (wid >= (long long)Hb * wchunks) return;  // whole warp
+    const int lane = threadIdx.x & 31;
+    const int by = (int)(wid / wchunks), wc = (int)(wid - (long long)by * wchunks);
+    const int q = lane % QG, w = wc * WPW + lane / QG;
     int n[S], jx[S], jy[S];
 #pragma unroll
     for (int s = 0; s < S; ++s) n[s] = jx[s] = jy[s] = 0;
-    const int y1 = min(g.H, (by + 1) * B);
-    for (int y = by * B; y < y1; ++y) {
-        uint64_t v[7];
-        const size_t o = (size_t)y * g.pitch + w;
+    if (w < g.nw) {
+#pragma unroll 4
+        for (int i = 0; i < 8; ++i) {
+            const int y = by * B + q * 8 + i;
+            if (y >= g.H) break;
+            uint64_t v[7];
+            const size_t o = (size_t)y * g.pitch + w;
 #pragma unroll
-        for (int d = 0; d < D; ++d) v[d] = __ldg(planes + (size_t)d * g.ps + o);
+            for (int d = 0; d < D; ++d) v[d] = __ldg(planes + (size_t)d * g.ps + o);
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-            const uint64_t m = (B == 64) ? ~0ull : (((1ull << B) - 1ull) << (s * B));
-            accum_counts<MODEL>(v, m, n[s], jx[s], jy[s]);
+            for (int s = 0; s < S; ++s) {
+                const uint64_t m = (B == 64) ? ~0ull : (((1ull << B) - 1ull) << (s * B));
+                accum_counts<MODEL>(v, m, n[s], jx[s], jy[s]);
+            }
         }
     }
+#pragma unroll
+    for (int off = 1; off < QG; off <<= 1) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            n[s] += __shfl_xor_sync(FULL, n[s], off);
+            jx[s] += __shfl_xor_sync(FULL, jx[s], off);
+            jy[s] += __shfl_xor_sync(FULL, jy[s], off);
+        }
+    }
+    if (q != 0 || w >= g.nw) return;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
         const int bx = w * S + s;

@@ -80,12 +80,24 @@ static void block_sums(const PlaneGeom &g, const uint64_t *planes, int B, int32_
                        int32_t *Jx2, int32_t *Jy)
 {
     const int Wb = (g.W + B - 1) / B, Hb = (g.H + B - 1) / B;
-    const unsigned seg_grid = grid_of((long long)Hb * g.nw, 128);
+    auto seg_grid = [&](long long warps) { return grid_of(warps * 32, 128); };
     switch (B) {
-    case 8: run_grid(seg_grid, [&] { k_block_sums_seg<MODEL, 8>(g, planes, Wb, Hb, N, Jx2, Jy); }); break;
-    case 16: run_grid(seg_grid, [&] { k_block_sums_seg<MODEL, 16>(g, planes, Wb, Hb, N, Jx2, Jy); }); break;
-    case 32: run_grid(seg_grid, [&] { k_block_sums_seg<MODEL, 32>(g, planes, Wb, Hb, N, Jx2, Jy); }); break;
-    case 64: run_grid(seg_grid, [&] { k_block_sums_seg<MODEL, 64>(g, planes, Wb, Hb, N, Jx2, Jy); }); break;
+    case 8:
+        run_grid(seg_grid(seg_block_sums_warps<8>(g.nw, Hb)),
+                 [&] { k_block_sums_seg<MODEL, 8>(g, planes, Wb, Hb, N, Jx2, Jy); });
+        break;
+    case 16:
+        run_grid(seg_grid(seg_block_sums_warps<16>(g.nw, Hb)),
+                 [&] { k_block_sums_seg<MODEL, 16>(g, planes, Wb, Hb, N, Jx2, Jy); });
+        break;
+    case 32:
+        run_grid(seg_grid(seg_block_sums_warps<32>(g.nw, Hb)),
+                 [&] { k_block_sums_seg<MODEL, 32>(g, planes, Wb, Hb, N, Jx2, Jy); });
+        break;
+    case 64:
+        run_grid(seg_grid(seg_block_sums_warps<64>(g.nw, Hb)),
+                 [&] { k_block_sums_seg<MODEL, 64>(g, planes, Wb, Hb, N, Jx2, Jy); });
+        break;
     default:
         if (B % 64 == 0 && B <= 2048 && ((B / 64) & (B / 64 - 1)) == 0) {
             const int K = B / 64, chunks = (g.nw + 31) / 32;
