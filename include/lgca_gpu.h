@@ -182,18 +182,29 @@ int lgca_set_block_warps(lgca_handle h, int warps);
  * ignored there and has no counterpart. */
 int lgca_collide_and_propagate(lgca_handle h, int nsteps);
 
+/* nsteps steps, then the B x B block sums of the result into the device
+ * arrays N, Jx2, Jy (as lgca_block_sums_device).  Where the resident kernel
+ * runs the steps and B is 8, 16, 32 or 64, the sums are computed inside its
+ * launch.  No reference counterpart beyond the two calls it stands for
+ * (src/omp_lattice.cpp:100-249 and the block sums). */
+int lgca_collide_and_propagate_sums(lgca_handle h, int nsteps, int B, int32_t *N, int32_t *Jx2,
+                                    int32_t *Jy);
+
 /* One job on the handle's stream, without waiting: the state from cells_in
  * (host, dim_x*dim_y bytes as lgca_upload_state; NULL keeps the current
- * state), nsteps steps, and the result to cells_out (host, as
- * lgca_download_state_async; NULL: no download); cells_out is valid after
- * lgca_sync.  The same as those three calls in that order, but where the
- * resident kernel runs the steps, the byte-per-cell conversions happen
- * inside its launch (no separate conversion kernels between jobs).  Host
+ * state), nsteps steps, the result to cells_out (host, as
+ * lgca_download_state_async; NULL: no download) and, for B > 0, the B x B
+ * block sums of the result to the host arrays N, Jx2, Jy (as
+ * lgca_block_sums_async).  Outputs are valid after lgca_sync.  The same as
+ * those calls in that order, but where the resident kernel runs the steps,
+ * the byte-per-cell conversions (and the block sums for B = 8, 16, 32, 64)
+ * happen inside its launch, so no other kernel runs between jobs.  Host
  * buffers should be pinned for the copies to overlap other work.
  * Reference counterpart: copy_data_to_device, collide_and_propagate (x
  * nsteps) and copy_data_from_device + copy_data_to_output_buffer
  * (src/lattice.cpp:422-441, src/omp_lattice.cpp:100-249). */
-int lgca_run_job_async(lgca_handle h, const uint8_t *cells_in, int nsteps, uint8_t *cells_out);
+int lgca_run_job_async(lgca_handle h, const uint8_t *cells_in, int nsteps, uint8_t *cells_out,
+                       int B, int32_t *N, int32_t *Jx2, int32_t *Jy);
 
 /* Random-cell body force with the reference's semantics: candidate cells
  * are drawn (FSEQ stream, call counter of the handle) until `forcing`

@@ -74,7 +74,8 @@ def lib() -> C.CDLL:
             "lgca_set_temporal_depth": (C.c_int, [vp, C.c_int]),
             "lgca_set_kernel_variant": (C.c_int, [vp, C.c_int]),
             "lgca_step_plan": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
-            "lgca_run_job_async": (C.c_int, [vp, vp, C.c_int, vp]),
+            "lgca_run_job_async": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]),
+            "lgca_collide_and_propagate_sums": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp]),
             "lgca_set_block_warps": (C.c_int, [vp, C.c_int]),
             "lgca_collide_and_propagate": (C.c_int, [vp, C.c_int]),
             "lgca_apply_body_force": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(u64)]),
@@ -236,16 +237,33 @@ class GpuLattice:
         return s
 
     def run_job_async(self, cells_in: np.ndarray | None, nsteps: int,
-                      cells_out: np.ndarray | None) -> None:
+                      cells_out: np.ndarray | None, B: int = 0, sums: np.ndarray | None = None) -> None:
         """Upload cells_in (or keep the state), advance nsteps steps and queue
-        the result into cells_out (pinned for overlap; valid after sync()),
-        in one call: where the resident kernel runs the steps, the layout
-        conversions happen inside its launch."""
+        the result into cells_out and, for B > 0, its B x B block sums into
+        sums (int32, shape (3, ceil(H/B), ceil(W/B)): N, Jx2, Jy), all pinned
+        for overlap and valid after sync(), in one call: where the resident
+        kernel runs the steps, the layout conversions and the sums happen
+        inside its launch."""
         for c in (cells_in, cells_out):
             assert c is None or (c.shape == self.shape and c.dtype == np.uint8 and
                                  c.flags.c_contiguous)
+        n = jx = jy = None
+        if B > 0:
+            H, W = self.shape
+            assert sums is not None and sums.dtype == np.int32 and sums.flags.c_contiguous
+            assert sums.shape == (3, -(-H // B), -(-W // B))
+            n, jx, jy = sums[0], sums[1], sums[2]
         _check(self._h, lib().lgca_run_job_async(self._h, _ptr(cells_in), int(nsteps),
-                                                 _ptr(cells_out)))
+                                                 _ptr(cells_out), int(B), _ptr(n), _ptr(jx),
+                                                 _ptr(jy)))
+
+    def collide_and_propagate_sums(self, nsteps: int, B: int, N_ptr: int, Jx2_ptr: int,
+                                   Jy_ptr: int) -> None:
+        """nsteps steps, then the B x B block sums of the result into device
+        buffers (fused into the resident kernel's launch where it runs)."""
+        _check(self._h, lib().lgca_collide_and_propagate_sums(self._h, int(nsteps), int(B),
+                                                              _ptr(N_ptr), _ptr(Jx2_ptr),
+                                                              _ptr(Jy_ptr)))
 
     def download_async(self, out: np.ndarray) -> None:
         """Queue a download into `out` (pinned for overlap); valid after sync()."""

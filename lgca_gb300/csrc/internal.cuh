@@ -197,11 +197,19 @@ static constexpr long long RESIDENT_MIN_WARPS = 1024;
 bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out);
 // aos_in / aos_out (device, H x W bytes, bit d = channel d; either may be
 // null): the launch's input is read from aos_in instead of a.src, and its
-// result is written to aos_out as well as to a.dst.
+// result is written to aos_out as well as to a.dst.  sums (or null): the
+// B x B block sums of the result, fused into the launch, added into the
+// device arrays N, Jx2, Jy (ceil(H/B) x ceil(W/B), zero before the launch);
+// B in 8, 16, 32, 64 and resident_sums_fit true.
+struct ResidentSums {
+    int B;
+    int32_t *N, *Jx2, *Jy;
+};
+bool resident_sums_fit(int model, const PlaneGeom &g, const ResidentShape &sh, int B);
 cudaError_t launch_resident(int model, int geom_mode, const StepArgs &a, const ResidentShape &sh,
                             uint64_t *halo, int *err, uint64_t seed, uint64_t t0,
                             int nsteps, const PersistWait &w, const uint8_t *aos_in,
-                            uint8_t *aos_out, cudaStream_t stream);
+                            uint8_t *aos_out, const ResidentSums *sums, cudaStream_t stream);
 
 // Kernel families selectable per handle.
 enum : int {

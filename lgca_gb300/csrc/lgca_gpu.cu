@@ -641,7 +641,7 @@ StepArgs step_args(const lgca_lattice *h)
 // one step per pass instead.
 constexpr int RESIDENT_UNAVAILABLE = -1;
 int run_resident(lgca_lattice *h, int nsteps, const ResidentShape &rs, const uint8_t *aos_in,
-                 uint8_t *aos_out)
+                 uint8_t *aos_out, const ResidentSums *sums = nullptr)
 {
     if (const int fst = error_flag(h)) return fst;
     const size_t halo_bytes = rs.halo_words * sizeof(uint64_t);
@@ -657,7 +657,7 @@ int run_resident(lgca_lattice *h, int nsteps, const ResidentShape &rs, const uin
     const PersistWait w{h->wait_ns, h->withhold};
     const cudaError_t e = launch_resident(h->model, geom_mode(h), a, rs,
                                           static_cast<uint64_t *>(h->res), h->sync, h->seed, h->t,
-                                          nsteps, w, aos_in, aos_out, h->stream);
+                                          nsteps, w, aos_in, aos_out, sums, h->stream);
     if (e == cudaErrorCooperativeLaunchTooLarge) {
         cudaGetLastError();  // (not sticky: the context stays usable)
         return RESIDENT_UNAVAILABLE;
@@ -753,38 +753,81 @@ int lgca_collide_and_propagate(lgca_handle h, int nsteps)
     return LGCA_OK;
 }
 
-int lgca_run_job_async(lgca_handle h, const uint8_t *cells_in, int nsteps, uint8_t *cells_out)
+int lgca_collide_and_propagate_sums(lgca_handle h, int nsteps, int B, int32_t *N, int32_t *Jx2,
+                                    int32_t *Jy)
 {
     CHECK_HANDLE(h);
     if (nsteps < 0) return fail(h, LGCA_ERR_INVALID, "nsteps < 0");
+    if (B < 1 || !N || !Jx2 || !Jy) return fail(h, LGCA_ERR_INVALID, "invalid block-sum arguments");
     DeviceGuard dg(h->device);
     ResidentShape rs;
-    if (step_family(h, nsteps, &rs) == VARIANT_RESIDENT && (cells_in || cells_out)) {
-        // one launch converts the input, steps and converts the result: the
-        // byte-per-cell buffer is read and rewritten row by row by the warp
-        // that owns the row, so input and output share the scratch buffer
-        const size_t n = (size_t)h->g.W * h->g.H;
-        int st = scratch_reserve(h, n + 64);
+    if (step_family(h, nsteps, &rs) == VARIANT_RESIDENT && resident_sums_fit(h->model, h->g, rs, B)) {
+        // the sums fused into the step launch: its blocks add into zeroed arrays
+        const size_t nb = (size_t)((h->g.W + B - 1) / B) * ((h->g.H + B - 1) / B);
+        for (int32_t *p : {N, Jx2, Jy}) CK(h, cudaMemsetAsync(p, 0, nb * sizeof(int32_t), h->stream));
+        const ResidentSums sums{B, N, Jx2, Jy};
+        const int st = run_resident(h, nsteps, rs, nullptr, nullptr, &sums);
+        if (st != RESIDENT_UNAVAILABLE) return st;
+    }
+    if (const int st = lgca_collide_and_propagate(h, nsteps)) return st;
+    return lgca_block_sums_device(h, B, N, Jx2, Jy);
+}
+
+int lgca_run_job_async(lgca_handle h, const uint8_t *cells_in, int nsteps, uint8_t *cells_out,
+                       int B, int32_t *N, int32_t *Jx2, int32_t *Jy)
+{
+    CHECK_HANDLE(h);
+    if (nsteps < 0) return fail(h, LGCA_ERR_INVALID, "nsteps < 0");
+    if (B < 0 || (B > 0 && (!N || !Jx2 || !Jy)))
+        return fail(h, LGCA_ERR_INVALID, "invalid block-sum arguments");
+    DeviceGuard dg(h->device);
+    ResidentShape rs;
+    if (step_family(h, nsteps, &rs) == VARIANT_RESIDENT && (cells_in || cells_out || B > 0)) {
+        // one launch converts the input, steps, converts the result and (for
+        // B in 8, 16, 32, 64) adds up the block sums: the byte-per-cell
+        // buffer is read and rewritten row by row by the warp that owns the
+        // row, so input and output share it; the sums follow it in scratch
+        const size_t n = (size_t)h->g.W * h->g.H, aos_bytes = (n + 255) & ~(size_t)255;
+        const size_t nb = B > 0 ? (size_t)((h->g.W + B - 1) / B) * ((h->g.H + B - 1) / B) : 0;
+        int st = scratch_reserve(h, aos_bytes + 3 * nb * sizeof(int32_t) + 64);
         if (st) return st;
         uint8_t *aos = static_cast<uint8_t *>(h->scratch);
+        int32_t *d = reinterpret_cast<int32_t *>(aos + aos_bytes);
+        const bool fused = B > 0 && resident_sums_fit(h->model, h->g, rs, B);
+        if (fused) CK(h, cudaMemsetAsync(d, 0, 3 * nb * sizeof(int32_t), h->stream));
         if (cells_in) CK(h, cudaMemcpyAsync(aos, cells_in, n, cudaMemcpyHostToDevice, h->stream));
-        st = run_resident(h, nsteps, rs, cells_in ? aos : nullptr, cells_out ? aos : nullptr);
+        const ResidentSums sums{B, d, d + nb, d + 2 * nb};
+        st = run_resident(h, nsteps, rs, cells_in ? aos : nullptr, cells_out ? aos : nullptr,
+                          fused ? &sums : nullptr);
         if (st == RESIDENT_UNAVAILABLE) {  // the copied input converted here, then the plain path
             if (cells_in)
                 CK(h, launch_aos_to_planes(h->D, h->g, aos, h->buf[h->cur], h->stream));
             if ((st = lgca_collide_and_propagate(h, nsteps))) return st;
-            return cells_out ? lgca_download_state_async(h, cells_out) : LGCA_OK;
+            if (cells_out && (st = lgca_download_state_async(h, cells_out))) return st;
+            return B > 0 ? lgca_block_sums_async(h, B, N, Jx2, Jy) : LGCA_OK;
         }
         if (st) return st;
         if (cells_out) CK(h, cudaMemcpyAsync(cells_out, aos, n, cudaMemcpyDeviceToHost, h->stream));
+        if (B > 0) {
+            if (!fused)
+                CK(h, launch_block_sums(h->model, h->g, h->buf[h->cur], B, d, d + nb, d + 2 * nb,
+                                        h->stream));
+            CK(h, cudaMemcpyAsync(N, d, nb * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+            CK(h, cudaMemcpyAsync(Jx2, d + nb, nb * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                  h->stream));
+            CK(h, cudaMemcpyAsync(Jy, d + 2 * nb, nb * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                  h->stream));
+        }
         return LGCA_OK;
     }
     if (cells_in) {
         if (const int st = lgca_upload_state(h, cells_in)) return st;
     }
     if (const int st = lgca_collide_and_propagate(h, nsteps)) return st;
-    if (cells_out) return lgca_download_state_async(h, cells_out);
-    return LGCA_OK;
+    if (cells_out) {
+        if (const int st = lgca_download_state_async(h, cells_out)) return st;
+    }
+    return B > 0 ? lgca_block_sums_async(h, B, N, Jx2, Jy) : LGCA_OK;
 }
 
 int lgca_apply_body_force(lgca_handle h, int forcing, int bf_dir, uint64_t *reverted)

@@ -69,6 +69,11 @@ struct ResidentArgs {
     // instead of a.src, and writes its result to aos_out as well as to a.dst
     const uint8_t *aos_in;
     uint8_t *aos_out;
+    // optional B x B block sums of the result (B = sums_B in 8, 16, 32, 64;
+    // 0: none) added into N, Jx2, Jy (Wb = ceil(W / B) columns), which must
+    // be zero before the launch
+    int sums_B, sums_Wb;
+    int32_t *sums_N, *sums_Jx2, *sums_Jy;
 };
 
 // Byte-per-cell <-> bit-plane conversion of 8 cells (the 8 bytes of x, cell
@@ -89,6 +94,29 @@ LGCA_HDI uint64_t res_spread8(uint64_t b)
 }
 
 static constexpr int RES_HALO_SLOTS = 3;
+
+// Particle count and momentum of the cells in mask m of the words v (the
+// block-sum weights: FHP Jx2 = 2n0 + n1 - n2 - 2n3 - n4 + n5 in units of
+// 1/2, Jy = n1 + n2 - n4 - n5 in units of sin 60; HPP Jx2 = 2(n0 - n2),
+// Jy = n1 - n3; src/lgca_models.h:51-52, :246).
+template <int MODEL>
+__device__ __forceinline__ void res_counts(const uint64_t *v, uint64_t m, int &n, int &jx2, int &jy)
+{
+    constexpr int D = ModelTraits<MODEL>::D;
+    int c[7];
+#pragma unroll
+    for (int d = 0; d < D; ++d) c[d] = __popcll(v[d] & m);
+    n = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) n += c[d];
+    if (MODEL == M_HPP) {
+        jx2 = 2 * (c[0] - c[2]);
+        jy = c[1] - c[3];
+    } else {
+        jx2 = 2 * c[0] + c[1] - c[2] - 2 * c[3] - c[4] + c[5];
+        jy = c[1] + c[2] - c[4] - c[5];
+    }
+}
 
 #ifndef LGCA_HOST_EMULATION
 // the block's shared memory: 8 control words, then two buffers of
@@ -533,6 +561,46 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
             }
         }
     }
+
+    // block sums of the result, fused: each lane counts its words' blocks,
+    // the block adds its rows' counts in shared memory (the step buffers are
+    // free now), then adds them once per block row and column to the output
+    // (a block row can span several bands)
+    if (R.sums_B) {
+        const int B = R.sums_B, Wb = R.sums_Wb, S = 64 / B;
+        // the band's rows again from the block index (nothing kept live for this)
+        const int ey0 = (int)((long long)g.H * blockIdx.x / R.nblk);
+        const int ey1 = (int)((long long)g.H * (blockIdx.x + 1) / R.nblk);
+        const int by0 = ey0 / B, nbr = (ey1 - 1) / B - by0 + 1;
+        int *acc = reinterpret_cast<int *>(rows);
+        const int nacc = nbr * Wb * 3, nthr = blockDim.x * blockDim.y;
+        const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+        __syncthreads();  // every warp is done with the step buffers
+        for (int i = tid; i < nacc; i += nthr) acc[i] = 0;
+        __syncthreads();
+        if (active) {
+            int *ra = acc + (size_t)(y / B - by0) * Wb * 3;
+            for (int k = 0; k < 2; ++k) {
+                for (int sb = 0; sb < S; ++sb) {
+                    const uint64_t m = (B == 64) ? ~0ull : (((1ull << B) - 1ull) << (sb * B));
+                    int n, jx2, jy;
+                    res_counts<MODEL>(s[k], m, n, jx2, jy);
+                    int *e = ra + (size_t)((w0 + k) * S + sb) * 3;
+                    atomicAdd(e, n);
+                    atomicAdd(e + 1, jx2);
+                    atomicAdd(e + 2, jy);
+                }
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < nbr * Wb; i += nthr) {
+            const int br = i / Wb, bx = i - br * Wb;
+            const size_t o = (size_t)(by0 + br) * Wb + bx;
+            atomicAdd(R.sums_N + o, acc[i * 3]);
+            atomicAdd(R.sums_Jx2 + o, acc[i * 3 + 1]);
+            atomicAdd(R.sums_Jy + o, acc[i * 3 + 2]);
+        }
+    }
 }
 
 #ifndef LGCA_HOST_EMULATION
@@ -542,6 +610,14 @@ size_t resident_smem_bytes(int model, const PlaneGeom &g, int rpb)
 {
     const int SP = model == M_HPP ? 4 : 6;
     return (8 + 2 * (size_t)rpb * SP * g.nw) * sizeof(uint64_t);
+}
+
+bool resident_sums_fit(int model, const PlaneGeom &g, const ResidentShape &sh, int B)
+{
+    if (!(B == 8 || B == 16 || B == 32 || B == 64)) return false;
+    const size_t Wb = (size_t)(g.W + B - 1) / B;
+    const size_t nbr = (size_t)(sh.rpb + B - 2) / B + 1;  // block rows a band can touch
+    return nbr * Wb * 3 * sizeof(int) <= resident_smem_bytes(model, g, sh.rpb) - 8 * sizeof(uint64_t);
 }
 
 bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out)
@@ -599,7 +675,7 @@ static cudaError_t res_model(int gm, const StepArgs &a, const ResidentShape &sh,
 cudaError_t launch_resident(int model, int gm, const StepArgs &a, const ResidentShape &sh,
                             uint64_t *halo, int *err, uint64_t seed, uint64_t t0,
                             int nsteps, const PersistWait &w, const uint8_t *aos_in,
-                            uint8_t *aos_out, cudaStream_t st)
+                            uint8_t *aos_out, const ResidentSums *sums, cudaStream_t st)
 {
     if (w.wait_ns == 0 || nsteps < 1) return cudaErrorInvalidValue;
     ResidentArgs R;
@@ -615,6 +691,11 @@ cudaError_t launch_resident(int model, int gm, const StepArgs &a, const Resident
     R.withhold = w.withhold;
     R.aos_in = aos_in;
     R.aos_out = aos_out;
+    R.sums_B = sums ? sums->B : 0;
+    R.sums_Wb = sums ? (a.g.W + sums->B - 1) / sums->B : 0;
+    R.sums_N = sums ? sums->N : nullptr;
+    R.sums_Jx2 = sums ? sums->Jx2 : nullptr;
+    R.sums_Jy = sums ? sums->Jy : nullptr;
     switch (model) {
     case M_HPP: return res_model<M_HPP>(gm, a, sh, R, st);
     case M_FHP_I: return res_model<M_FHP_I>(gm, a, sh, R, st);

@@ -35,7 +35,9 @@ def main(argv=None):
     ap.add_argument("--force-x", type=int, default=-1)
     ap.add_argument("--force-p", type=float, default=0.0)
     ap.add_argument("--p", type=float, default=0.5)
-    ap.add_argument("--block", type=int, default=0, help="also compute BxB block sums per step")
+    ap.add_argument("--block", type=int, default=0,
+                    help="also compute the BxB block sums of each call's result (into device "
+                         "buffers, fused into the step launch where the resident kernel runs)")
     ap.add_argument("--batch", type=int, default=0,
                     help="run the first N jobs of the batched workload as one batch instead")
     ap.add_argument("--launches", action="store_true",
@@ -78,11 +80,18 @@ def main(argv=None):
     L.collide_and_propagate(args.warmup)
     L.sync()
     per_call = args.chunk or (1 if args.depth == 1 else args.depth)
+    sums = None
+    if args.block:
+        import torch
+        B = args.block
+        sums = torch.empty((3, -(-args.H // B), -(-args.W // B)), dtype=torch.int32, device="cuda")
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        L.collide_and_propagate(per_call)
-        if args.block:
-            L.block_sums(args.block)
+        if sums is not None:
+            L.collide_and_propagate_sums(per_call, args.block, sums[0].data_ptr(),
+                                         sums[1].data_ptr(), sums[2].data_ptr())
+        else:
+            L.collide_and_propagate(per_call)
     L.sync()
     dt = time.perf_counter() - t0
     n = args.steps * per_call

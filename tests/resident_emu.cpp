@@ -9,7 +9,7 @@
 // result with the oracle.
 //
 //   resident_emu IN OUT
-//   IN:  int32 model, W, H, steps, force_x, nblk, chunk, withhold, aos;
+//   IN:  int32 model, W, H, steps, force_x, nblk, chunk, withhold, aos, B;
 //        uint64 seed, t0, force_thr, wait_ns; H*W uint8 cells (bit d = channel d);
 //        H*W uint8 cell types (0 fluid, 1 no-slip, 2 slip)
 //   OUT: int32 err; H*W uint8 cells after `steps` steps, run as launches of
@@ -17,6 +17,8 @@
 //        the H*W bytes the last launch wrote in the byte-per-cell layout.
 //   aos & 1: the first launch reads its input in the byte-per-cell layout;
 //   aos & 2: every launch also writes its result in that layout.
+//   B > 0: the last launch also adds up the B x B block sums of its result,
+//   written last as int32 N, Jx2, Jy (each ceil(H/B) x ceil(W/B)).
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -92,6 +94,8 @@ inline void __syncthreads() { emu::block_bar->arrive_and_wait(); }
 inline void __threadfence() { std::atomic_thread_fence(std::memory_order_seq_cst); }
 inline void __nanosleep(unsigned) { std::this_thread::yield(); }
 inline int atomicExch(int *p, int v) { return __atomic_exchange_n(p, v, __ATOMIC_SEQ_CST); }
+inline int atomicAdd(int *p, int v) { return __atomic_fetch_add(p, v, __ATOMIC_RELAXED); }
+inline int __popcll(unsigned long long x) { return __builtin_popcountll(x); }
 template <class T> inline T __ldcg(const T *p) { return *p; }
 template <class T> inline T __ldg(const T *p) { return *p; }
 thread_local uint3 threadIdx;
@@ -180,11 +184,11 @@ int main(int argc, char **argv)
     }
     FILE *f = std::fopen(argv[1], "rb");
     if (!f) return 2;
-    int32_t hdr[9];
+    int32_t hdr[10];
     uint64_t u[4];
     if (std::fread(hdr, sizeof(hdr), 1, f) != 1 || std::fread(u, sizeof(u), 1, f) != 1) return 2;
     const int model = hdr[0], W = hdr[1], H = hdr[2], steps = hdr[3], fx = hdr[4], nblk = hdr[5],
-              chunk = hdr[6], withhold = hdr[7], aos = hdr[8];
+              chunk = hdr[6], withhold = hdr[7], aos = hdr[8], sumsB = hdr[9];
     const uint64_t seed = u[0], t0 = u[1], thr = u[2], wait_ns = u[3];
     std::vector<uint8_t> cells((size_t)W * H), types((size_t)W * H);
     if (std::fread(cells.data(), 1, cells.size(), f) != cells.size() ||
@@ -233,6 +237,8 @@ int main(int argc, char **argv)
     a.fx = fx;
     a.wpt = 2;
     std::vector<uint8_t> aos_in(cells), aos_out((size_t)W * H, 0xff);
+    const int Wb = sumsB > 0 ? (W + sumsB - 1) / sumsB : 0, Hb = sumsB > 0 ? (H + sumsB - 1) / sumsB : 0;
+    std::vector<int32_t> sums((size_t)3 * Wb * Hb, 0);
     int cur = 0;
     for (int done = 0; done < steps; done += chunk) {
         const int n = std::min(chunk, steps - done);
@@ -252,6 +258,12 @@ int main(int argc, char **argv)
         R.withhold = withhold;
         R.aos_in = (done == 0 && (aos & 1)) ? aos_in.data() : nullptr;
         R.aos_out = (aos & 2) ? aos_out.data() : nullptr;
+        const bool last = done + n >= steps;
+        R.sums_B = last ? sumsB : 0;
+        R.sums_Wb = Wb;
+        R.sums_N = sums.data();
+        R.sums_Jx2 = sums.data() + (size_t)Wb * Hb;
+        R.sums_Jy = sums.data() + (size_t)2 * Wb * Hb;
         if (model == 0) launch_gm<M_HPP>(gm, a, R);
         else if (model == 1) launch_gm<M_FHP_I>(gm, a, R);
         else launch_gm<M_FHP_II>(gm, a, R);
@@ -271,6 +283,7 @@ int main(int argc, char **argv)
     std::fwrite(&e32, sizeof(e32), 1, o);
     std::fwrite(cells.data(), 1, cells.size(), o);
     if (aos & 2) std::fwrite(aos_out.data(), 1, aos_out.size(), o);
+    if (sumsB > 0) std::fwrite(sums.data(), sizeof(int32_t), sums.size(), o);
     std::fclose(o);
     return 0;
 }

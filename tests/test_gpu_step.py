@@ -412,6 +412,9 @@ def test_run_job_equals_upload_steps_download(gpu, oracle, model):
         want2 = oracle.run(model, want1, 9, t0=12, **kw)
         pin = lambda: torch.empty((H, W), dtype=torch.uint8, pin_memory=True).numpy()
         src, out1, out2 = pin(), pin(), pin()
+        B = 32
+        sums = torch.empty((3, -(-H // B), -(-W // B)), dtype=torch.int32, pin_memory=True).numpy()
+        want_sums = oracle.block_sums(model, want2, B)
         src[:] = st | np.uint8((0xff << oracle.NUM_DIR[model]) & 0xff)  # bits above the channels ignored
         for variant in (0, 6):  # automatic (separate calls here), resident (conversions in the launch)
             out1[:] = 0
@@ -421,12 +424,50 @@ def test_run_job_equals_upload_steps_download(gpu, oracle, model):
                 L.set_forcing_column(W - 1, 0.5)
                 L.set_kernel_variant(variant)
                 L.run_job_async(src, 12, out1)
-                L.run_job_async(None, 9, out2)
+                sums[:] = -1
+                L.run_job_async(None, 9, out2, B, sums)
                 L.sync()
                 assert np.array_equal(out1, want1), (W, H, geom, variant)
                 assert np.array_equal(out2, want2), (W, H, geom, variant)
+                for i in range(3):
+                    assert np.array_equal(sums[i], want_sums[i]), (W, H, geom, variant, i)
                 assert np.array_equal(L.download(), want2)
                 assert L.step_count == 21
                 L.set_step(0)
                 L.run_job_async(src, 12, None)
                 assert np.array_equal(L.download(), want1)
+
+
+@pytest.mark.parametrize("model", [0, 1, 3])
+def test_steps_with_fused_block_sums(gpu, oracle, model):
+    """lgca_collide_and_propagate_sums: the steps and the B x B block sums of
+    their result equal the oracle's, with the sums inside the resident
+    kernel's launch (B = 8, 16, 32, 64) or from the block-sum kernel (other
+    B, other kernels), and repeated calls do not accumulate."""
+    import torch
+    rng = np.random.default_rng(model + 70)
+    for W, H, variant in [(4096, 64, 6), (8192, 300, 6), (2048, 2048, 0), (4160, 40, 0)]:
+        types = GEOMS["karman"](W, H)
+        seed = int(rng.integers(1 << 40))
+        st = oracle.init_bernoulli(model, W, H, types, seed=seed, p_move=0.35, p_rest=0.3)
+        kw = dict(types=types, seed=seed, force_x=W // 3, force_p=0.5)
+        want1 = oracle.run(model, st, 20, **kw)
+        want2 = oracle.run(model, want1, 20, t0=20, **kw)
+        with gpu.GpuLattice(model, W, H, seed) as L:
+            L.set_cell_types(types)
+            L.upload(st)
+            L.set_forcing_column(W // 3, 0.5)
+            L.set_kernel_variant(variant)
+            for B in (8, 16, 32, 64, 48):
+                L.upload(st)
+                L.set_step(0)
+                sums = torch.full((3, -(-H // B), -(-W // B)), -1, dtype=torch.int32, device="cuda")
+                L.collide_and_propagate_sums(20, B, sums[0].data_ptr(), sums[1].data_ptr(),
+                                             sums[2].data_ptr())
+                L.collide_and_propagate_sums(20, B, sums[0].data_ptr(), sums[1].data_ptr(),
+                                             sums[2].data_ptr())
+                L.sync()
+                assert np.array_equal(L.download(), want2), (W, H, B)
+                got = sums.cpu().numpy()
+                for i, w in enumerate(oracle.block_sums(model, want2, B)):
+                    assert np.array_equal(got[i], w), (W, H, variant, B, i)

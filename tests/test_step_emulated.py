@@ -324,12 +324,12 @@ def resident_emu(tmp_path_factory):
 
 
 def run_resident(exe, tmp, model, cells, types, steps, seed, t0, force_x, force_thr, nblk,
-                 chunk, withhold=-1, wait_ns=10_000_000_000, aos=0):
+                 chunk, withhold=-1, wait_ns=10_000_000_000, aos=0, B=0):
     H, W = cells.shape
     inp, out = tmp / "rin.bin", tmp / "rout.bin"
     with open(inp, "wb") as f:
-        f.write(struct.pack("<9i4Q", model, W, H, steps, force_x, nblk, chunk, withhold, aos, seed,
-                            t0, force_thr, wait_ns))
+        f.write(struct.pack("<10i4Q", model, W, H, steps, force_x, nblk, chunk, withhold, aos, B,
+                            seed, t0, force_thr, wait_ns))
         f.write(np.ascontiguousarray(cells, np.uint8).tobytes())
         f.write(np.ascontiguousarray(types, np.uint8).tobytes())
     r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True, env=ENV, timeout=600)
@@ -337,9 +337,14 @@ def run_resident(exe, tmp, model, cells, types, steps, seed, t0, force_x, force_
     raw = out.read_bytes()
     err = struct.unpack("<i", raw[:4])[0]
     got = np.frombuffer(raw[4:4 + H * W], np.uint8).reshape(H, W)
+    rest = raw[4 + H * W:]
+    extra = []
     if aos & 2:
-        return err, got, np.frombuffer(raw[4 + H * W:], np.uint8).reshape(H, W)
-    return err, got
+        extra.append(np.frombuffer(rest[:H * W], np.uint8).reshape(H, W))
+        rest = rest[H * W:]
+    if B > 0:
+        extra.append(np.frombuffer(rest, np.int32).reshape(3, -(-H // B), -(-W // B)))
+    return (err, got, *extra)
 
 
 # (W, H, blocks): one and two warps per row, a row of a single word pair,
@@ -375,11 +380,15 @@ def test_emulated_resident_kernel_equals_oracle(resident_emu, tmp_path, oracle, 
             # input read and result written in the byte-per-cell layout by the
             # launch itself (garbage in the bits above the model's channels)
             noisy = st | np.uint8((0xff << oracle.NUM_DIR[model]) & 0xff)
-            err, got, aos_out = run_resident(resident_emu, tmp_path, model, noisy,
-                                             types.astype(np.uint8), 6, 13, 9, fx, thr, nblk, 4,
-                                             aos=3)
+            B = (8, 16, 32, 64)[nblk % 4]
+            err, got, aos_out, sums = run_resident(resident_emu, tmp_path, model, noisy,
+                                                   types.astype(np.uint8), 6, 13, 9, fx, thr, nblk,
+                                                   4, aos=3, B=B)
             assert err == 0
             assert np.array_equal(got, want) and np.array_equal(aos_out, want), (model, W, H)
+            # B x B block sums of the result, fused into the last launch
+            for i, w in enumerate(oracle.block_sums(model, want, B)):
+                assert np.array_equal(sums[i], w), (model, W, H, nblk, B, i)
 
 
 def test_emulated_resident_kernel_stays_in_bounds(tmp_path, oracle):
