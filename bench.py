@@ -406,7 +406,15 @@ def run_ours(args):
     aos_out = [torch.empty((H_K, W_K), dtype=torch.uint8, pin_memory=True).numpy() for _ in lats]
     hs = [torch.empty((3, Hb, Wb), dtype=torch.int32, pin_memory=True).numpy() for _ in lats]
     e2e_steps = max(2, min(args.steps, 50))
-    first = [None, None]
+    # warm-up jobs (first-call allocations, pinned flags) outside the timed
+    # region; their outputs are what every timed job must reproduce
+    for X, out, h in zip(lats, aos_out, hs):
+        X.set_step(0)
+        X.run_job_async(aos_in, STEPS_PER_CHUNK, out, BLOCK, h)
+    for X in lats:
+        X.sync()
+    expect = (aos_out[0].copy(), hs[0].copy())
+    e2e_same = np.array_equal(aos_out[1], expect[0]) and np.array_equal(hs[1], expect[1])
     barrier()
     t_e2e = time.perf_counter()
     for i in range(e2e_steps):
@@ -414,18 +422,14 @@ def run_ours(args):
         X = lats[k]
         X.set_step(0)
         X.run_job_async(aos_in, STEPS_PER_CHUNK, aos_out[k], BLOCK, hs[k])
-        if i >= 1:  # collect the other lattice's job
+        if i >= 1:  # the other lattice's job is complete before that lattice takes the next
             lats[k ^ 1].sync()
-            if first[k ^ 1] is None:
-                first[k ^ 1] = (aos_out[k ^ 1].copy(), hs[k ^ 1].copy())
     lats[(e2e_steps - 1) & 1].sync()
     barrier()
     t_e2e = time.perf_counter() - t_e2e
-    last = (e2e_steps - 1) & 1
-    if first[last] is None:
-        first[last] = (aos_out[last].copy(), hs[last].copy())
-    e2e_same = all(np.array_equal(first[0][j], first[1][j]) and
-                   np.array_equal(first[0][j], (aos_out, hs)[j][last]) for j in range(2))
+    # the last job of each lattice reproduced the warm-up output
+    e2e_same = e2e_same and all(np.array_equal(aos_out[k], expect[0]) and
+                                np.array_equal(hs[k], expect[1]) for k in range(2))
     L2.close()
     if ws > 1:
         tt = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
