@@ -606,7 +606,7 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
 #ifndef LGCA_HOST_EMULATION
 // ------------------------------------------------------------------ launcher
 
-size_t resident_smem_bytes(int model, const PlaneGeom &g, int rpb)
+static size_t resident_smem_bytes(int model, const PlaneGeom &g, int rpb)
 {
     const int SP = model == M_HPP ? 4 : 6;
     return (8 + 2 * (size_t)rpb * SP * g.nw) * sizeof(uint64_t);
