@@ -182,8 +182,7 @@ cudaError_t launch_persistent(int model, int geom_mode, const StepArgs &a, uint6
 // Resident form (resident.cu): nsteps steps in one cooperative launch with
 // the state held on chip between steps; for lattices of whole word pairs per
 // row whose one-row-per-warp tasks fit on the GPU at once.  The result is in
-// `a.dst`.  `halo` holds halo_words words, zero before the launch; *err as
-// for launch_persistent.
+// `a.dst`.  `halo` holds halo_words words; *err as for launch_persistent.
 struct ResidentShape {
     int nblk, wpr, rpb;  // blocks (bands), warps per row, most rows in a band
     size_t smem;         // dynamic shared memory per block
@@ -206,10 +205,15 @@ struct ResidentSums {
     int32_t *N, *Jx2, *Jy;
 };
 bool resident_sums_fit(int model, const PlaneGeom &g, const ResidentShape &sh, int B);
+// epoch (1..255) tags the launch's halo items: the slots must hold no item
+// of that epoch (zero them, then use each epoch once); nsteps is at most
+// RESIDENT_MAX_STEPS.
+static constexpr int RESIDENT_MAX_STEPS = (1 << 24) - 2;
 cudaError_t launch_resident(int model, int geom_mode, const StepArgs &a, const ResidentShape &sh,
                             uint64_t *halo, int *err, uint64_t seed, uint64_t t0,
                             int nsteps, const PersistWait &w, const uint8_t *aos_in,
-                            uint8_t *aos_out, const ResidentSums *sums, cudaStream_t stream);
+                            uint8_t *aos_out, const ResidentSums *sums, unsigned epoch,
+                            cudaStream_t stream);
 
 // Kernel families selectable per handle.
 enum : int {

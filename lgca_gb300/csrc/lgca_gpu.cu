@@ -42,7 +42,9 @@ struct lgca_lattice {
     // between calls), per-call state, the table's clean mark and the count
     void *bf = nullptr;
     // resident form: the band edges' halo slots (resident_shape of the lattice)
+    // and the epoch of the last launch's items (0: the slots need zeroing)
     void *res = nullptr;
+    unsigned res_epoch = 0;
     // persistent kernel: sync[0] = error flag (sticky: set when a bounded
     // neighbour wait gave up, cleared only by lgca_clear_error), then one step
     // flag per block; sync_err_host is its pinned copy, refreshed after each
@@ -598,7 +600,8 @@ int step_family(const lgca_lattice *h, int nsteps, ResidentShape *rs)
     // launches are as fast or faster)
     ResidentShape tmp;
     ResidentShape &shape = rs ? *rs : tmp;
-    if (nsteps <= 0 || !resident_shape(h->model, h->g, shape)) return VARIANT_PLAIN;
+    if (nsteps <= 0 || nsteps > RESIDENT_MAX_STEPS || !resident_shape(h->model, h->g, shape))
+        return VARIANT_PLAIN;
     if (h->variant == VARIANT_RESIDENT) return VARIANT_RESIDENT;
     if (h->variant == VARIANT_AUTO && h->depth == 1 && nsteps >= RESIDENT_MIN_STEPS &&
         h->g.nw / 2 >= 16 && (long long)h->g.H * shape.wpr >= RESIDENT_MIN_WARPS)
@@ -649,15 +652,22 @@ int run_resident(lgca_lattice *h, int nsteps, const ResidentShape &rs, const uin
         int st = dalloc(h, &h->res, halo_bytes, false, "resident halo");
         if (st) return st;
     }
-    // items carry the step they belong to: none may survive from an earlier call
-    CK(h, cudaMemsetAsync(h->res, 0, halo_bytes, h->stream));
+    // items carry their launch's epoch and step: each launch takes the next
+    // epoch, and the slots are zeroed once every 255 launches
+    if (h->res_epoch == 0 || h->res_epoch >= 255) {
+        CK(h, cudaMemsetAsync(h->res, 0, halo_bytes, h->stream));
+        h->res_epoch = 1;
+    } else {
+        ++h->res_epoch;
+    }
     StepArgs a = step_args(h);
     a.src = h->buf[h->cur];
     a.dst = h->buf[h->cur ^ 1];
     const PersistWait w{h->wait_ns, h->withhold};
     const cudaError_t e = launch_resident(h->model, geom_mode(h), a, rs,
                                           static_cast<uint64_t *>(h->res), h->sync, h->seed, h->t,
-                                          nsteps, w, aos_in, aos_out, sums, h->stream);
+                                          nsteps, w, aos_in, aos_out, sums, h->res_epoch,
+                                          h->stream);
     if (e == cudaErrorCooperativeLaunchTooLarge) {
         cudaGetLastError();  // (not sticky: the context stays usable)
         return RESIDENT_UNAVAILABLE;

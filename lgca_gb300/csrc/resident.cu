@@ -57,7 +57,11 @@ namespace lgca_gpu {
 static constexpr int RES_MAX_WARPS = 28;  // warps per block (<= 72 registers per thread)
 
 struct ResidentArgs {
-    uint64_t *halo;  // [3 steps][nblk][2 sides][2 channels][nw][2] items, zero before the launch
+    // [3 steps][nblk][2 sides][2 channels][nw][2] items; items of time t
+    // carry the tag (epoch << 24) | (t + 1), and no item in the slots may
+    // carry a tag of this launch's epoch when it starts
+    uint64_t *halo;
+    unsigned epoch;  // 1 .. 255
     int *err;
     uint64_t seed, t0;
     int nsteps;
@@ -290,7 +294,7 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
         for (int d = 0; d < SP; ++d)
             *reinterpret_cast<ulonglong2 *>(dr + (size_t)d * nw + w0) = make_ulonglong2(s[0][d], s[1][d]);
         if (b == R.withhold) return;
-        const uint64_t tag = (uint64_t)(tm + 1) << 32;
+        const uint64_t tag = (uint64_t)((R.epoch << 24) | (tm + 1)) << 32;
         auto put = [&](uint64_t *slot, int k, uint64_t v0, uint64_t v1) {
             uint64_t *p = slot + ((size_t)k * nw + w0) * 2;
             st_items(p, tag | (v0 & 0xffffffffull), tag | (v0 >> 32));
@@ -313,7 +317,7 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
     // the step; false when the wait gave up (every lane returns alike)
     auto halo_get = [&](const uint64_t *slot, unsigned tm, int ek, int ew, bool need_edge,
                         uint64_t (&v)[2][2], uint64_t &edge) -> bool {
-        const uint64_t tag = (uint64_t)(tm + 1);
+        const uint64_t tag = (uint64_t)((R.epoch << 24) | (tm + 1));
         uint64_t t_start = 0;
         for (int spin = 0;; ++spin) {
             bool ok = true;
@@ -675,11 +679,14 @@ static cudaError_t res_model(int gm, const StepArgs &a, const ResidentShape &sh,
 cudaError_t launch_resident(int model, int gm, const StepArgs &a, const ResidentShape &sh,
                             uint64_t *halo, int *err, uint64_t seed, uint64_t t0,
                             int nsteps, const PersistWait &w, const uint8_t *aos_in,
-                            uint8_t *aos_out, const ResidentSums *sums, cudaStream_t st)
+                            uint8_t *aos_out, const ResidentSums *sums, unsigned epoch,
+                            cudaStream_t st)
 {
-    if (w.wait_ns == 0 || nsteps < 1) return cudaErrorInvalidValue;
+    if (w.wait_ns == 0 || nsteps < 1 || nsteps > RESIDENT_MAX_STEPS || epoch < 1 || epoch > 255)
+        return cudaErrorInvalidValue;
     ResidentArgs R;
     R.halo = halo;
+    R.epoch = epoch;
     R.err = err;
     R.seed = seed;
     R.t0 = t0;

@@ -242,11 +242,11 @@ int main(int argc, char **argv)
     int cur = 0;
     for (int done = 0; done < steps; done += chunk) {
         const int n = std::min(chunk, steps - done);
-        std::fill(halo.begin(), halo.end(), 0ull);
         a.src = buf[cur].data();
         a.dst = buf[cur ^ 1].data();
         ResidentArgs R{};
         R.halo = halo.data();
+        R.epoch = 1 + (unsigned)(done / chunk) % 255;  // a new epoch per launch (slots zeroed once)
         R.err = &err;
         R.seed = seed;
         R.t0 = t0 + (uint64_t)done;
