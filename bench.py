@@ -203,6 +203,7 @@ def gate_measurement(gpu, torch, hbm_peak):
     W, H = 32768, 16384
     with gpu.GpuLattice(MODEL, W, H, seed=3) as L:
         L.init_random(0.5, 0.5)
+        L.set_kernel_variant(5)  # one step per pass (the automatic choice blocks 2 steps here)
         s = torch.cuda.ExternalStream(L.stream_ptr())
         L.collide_and_propagate(3)
         n = 30

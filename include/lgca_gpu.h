@@ -145,8 +145,10 @@ int lgca_set_temporal_depth(lgca_handle h, int depth);
 
 /* Kernel family for the steps: 0 = automatic (default: the resident form 6
  * for calls of 16 or more steps on lattices it holds with rows of at least
- * 2048 sites and at least 1024 rows x ceil(dim_x / 4096), else one step per
- * pass, or the register wavefront when a temporal depth above 1 is set),
+ * 2048 sites and at least 1024 rows x ceil(dim_x / 4096); the register
+ * wavefront at 4 steps per pass for HPP lattices of 64 Mi sites or more and
+ * at 4 (FHP-I) or 2 (FHP-II/III) for FHP lattices of 256 Mi sites or more;
+ * else one step per pass; a temporal depth above 1 selects the wavefront),
  * 1 = one step per
  * pass only, 2 = register wavefront (several steps per pass), 3 = shared-
  * memory tiles (several steps per pass), 4 = persistent (all steps of a call

@@ -612,6 +612,18 @@ int step_family(const lgca_lattice *h, int nsteps, ResidentShape *rs)
 int pass_depth(const lgca_lattice *h, int left)
 {
     int k = std::min(h->depth, left);
+    if (h->variant == VARIANT_AUTO && h->depth == 1) {
+        // lattices far beyond L2, where one step per pass is bound by HBM,
+        // take passes of several steps on the register wavefront (measured
+        // on GB300: HPP from 64 Mi sites, 4 steps per pass, 1.45-2.4x;
+        // FHP-I and FHP-II/III from 256 Mi sites, 4 and 2 steps, 1.34x and
+        // 1.14x; smaller lattices run as fast or faster one step per pass)
+        const long long sites = (long long)h->g.W * h->g.H;
+        const int kauto = h->model == M_HPP     ? (sites >= (64LL << 20) ? 4 : 1)
+                          : h->model == M_FHP_I ? (sites >= (256LL << 20) ? 4 : 1)
+                                                : (sites >= (256LL << 20) ? 2 : 1);
+        k = std::min(kauto, left);
+    }
     const bool tile = h->variant == VARIANT_TILE;
     if (h->variant == VARIANT_PLAIN || h->variant == VARIANT_PLAIN2 ||
         h->variant == VARIANT_RESIDENT)

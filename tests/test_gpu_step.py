@@ -371,7 +371,8 @@ def test_roofline_sweep_kernels_at_1024(gpu, oracle, model, p):
 def test_step_plan_names_the_kernels_a_call_runs(gpu, oracle):
     """lgca_step_plan reports the kernel family and launches of a call; the
     automatic choice takes the resident form for calls of 16 steps or more on
-    lattices it holds that fill the SMs."""
+    lattices it holds that fill the SMs, and passes of several steps on
+    lattices far beyond L2."""
     W, H = 8192, 2048
     with gpu.GpuLattice(3, W, H, seed=2) as L:
         assert L.step_plan(100) == (6, 1)
@@ -390,6 +391,19 @@ def test_step_plan_names_the_kernels_a_call_runs(gpu, oracle):
         assert L.step_plan(100) == (1, 100)
         L.set_kernel_variant(6)
         assert L.step_plan(100) == (6, 1)
+    # far beyond L2: HPP from 64 Mi sites takes 4 steps per pass on the wavefront,
+    # with the same bits as one step per pass
+    W, H = 8192, 8192
+    with gpu.GpuLattice(0, W, H, seed=4) as L, gpu.GpuLattice(0, W, H, seed=4) as R:
+        assert L.step_plan(10) == (1, 4)  # 4 + 4 + 2 steps
+        for X in (L, R):
+            X.init_random(0.3)
+            X.set_forcing_column(100, 0.2)
+        R.set_kernel_variant(5)
+        assert R.step_plan(10) == (1, 10)
+        L.collide_and_propagate(10)
+        R.collide_and_propagate(10)
+        assert np.array_equal(L.download(), R.download())
     with gpu.GpuLattice(3, 32768, 4096, seed=2) as L:  # too many rows per SM
         assert L.step_plan(100) == (1, 100)
 
