@@ -395,7 +395,7 @@ def test_step_plan_names_the_kernels_a_call_runs(gpu, oracle):
     # with the same bits as one step per pass
     W, H = 8192, 8192
     with gpu.GpuLattice(0, W, H, seed=4) as L, gpu.GpuLattice(0, W, H, seed=4) as R:
-        assert L.step_plan(10) == (1, 4)  # 4 + 4 + 2 steps
+        assert L.step_plan(10) == (1, 3)  # passes of 4, 4 and 2 steps
         for X in (L, R):
             X.init_random(0.3)
             X.set_forcing_column(100, 0.2)
