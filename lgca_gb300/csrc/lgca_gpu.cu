@@ -602,6 +602,13 @@ int step_family(const lgca_lattice *h, int nsteps, ResidentShape *rs)
     ResidentShape &shape = rs ? *rs : tmp;
     if (nsteps <= 0 || nsteps > RESIDENT_MAX_STEPS || !resident_shape(h->model, h->g, shape))
         return VARIANT_PLAIN;
+    // not into CUDA graphs: a resident call always leaves its result in the
+    // other buffer and tags its halo items with the call's epoch, so a
+    // replayed capture would neither chain (as an even number of one-step
+    // launches does) nor start from clean halo slots
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(h->stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+        return VARIANT_PLAIN;
     if (h->variant == VARIANT_RESIDENT) return VARIANT_RESIDENT;
     if (h->variant == VARIANT_AUTO && h->depth == 1 && nsteps >= RESIDENT_MIN_STEPS &&
         h->g.nw / 2 >= 16 && (long long)h->g.H * shape.wpr >= RESIDENT_MIN_WARPS)

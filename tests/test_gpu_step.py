@@ -326,18 +326,26 @@ def test_steps_captured_in_a_cuda_graph(gpu, oracle, model):
     and buffers: with an even number of steps per call, every replay repeats
     steps t .. t+k-1 on the current state."""
     torch = pytest.importorskip("torch")
-    W, H, k = 640, 64, 4
+    _captured_replays(gpu, oracle, model, torch, 640, 64, 4, variant=0)
+    # a lattice and call the resident kernel would take: under capture the
+    # engine steps one step per pass, so the replays chain the same way
+    _captured_replays(gpu, oracle, model, torch, 4096, 40, 20, variant=6)
+
+
+def _captured_replays(gpu, oracle, model, torch, W, H, k, variant):
     types = G.pipe(W, H)
     st = oracle.init_bernoulli(model, W, H, types, seed=5, p_move=0.3, p_rest=0.3)
     L = gpu.GpuLattice(model, W, H, seed=5)
     L.set_cell_types(types)
     L.upload(st)
     L.set_forcing_column(10, 0.3)
+    L.set_kernel_variant(variant)
     L.sync()
     s = torch.cuda.Stream()
     L.set_stream(s.cuda_stream)
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g, stream=s):
+        assert L.step_plan(k)[0] == 1
         L.collide_and_propagate(k)
     for _ in range(3):
         g.replay()
