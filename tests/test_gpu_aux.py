@@ -350,3 +350,22 @@ def test_checkpoint_load_rejects_invalid_settings(gpu):
         assert np.array_equal(L.download(), want)
         L.restore(bytes(blob))
         assert np.array_equal(L.download(), want)
+
+
+def test_job_and_fused_sum_calls_reject_bad_arguments(gpu):
+    """The one-call job, the steps-with-sums call and the step plan refuse
+    invalid arguments with a status, before queueing anything."""
+    import ctypes as C
+    lib = gpu.lib()
+    with gpu.GpuLattice(3, 4096, 64, seed=1) as L:
+        L.init_random(0.3)
+        want = L.download()
+        h = L._h
+        assert lib.lgca_run_job_async(h, None, -1, None, 0, None, None, None) != 0
+        assert lib.lgca_run_job_async(h, None, 4, None, -2, None, None, None) != 0
+        assert lib.lgca_run_job_async(h, None, 4, None, 32, None, None, None) != 0  # sums NULL
+        assert lib.lgca_collide_and_propagate_sums(h, 4, 0, None, None, None) != 0
+        assert lib.lgca_collide_and_propagate_sums(h, -1, 32, None, None, None) != 0
+        fam, n = C.c_int(), C.c_int()
+        assert lib.lgca_step_plan(h, -3, C.byref(fam), C.byref(n)) != 0
+        assert np.array_equal(L.download(), want) and L.step_count == 0
