@@ -187,6 +187,7 @@ struct ResidentShape {
     int nblk, wpr, rpb;  // blocks (bands), warps per row, most rows in a band
     size_t smem;         // dynamic shared memory per block
     size_t halo_words;
+    bool rowsync;        // row barriers instead of a block barrier per step
 };
 static constexpr size_t RES_MAX_SMEM = 200 * 1024;
 // the automatic choice gives the resident form calls of at least this many

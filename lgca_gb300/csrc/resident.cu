@@ -26,9 +26,10 @@
 // reader that sees the step it wants has the data, with no fence and no
 // separate flag between writer and reader.  Interior rows never wait for
 // another block.  A writer overwrites a slot three steps later, by which
-// time every reader of the old contents has passed a block barrier that the
-// writer waited behind (it read the readers' own edge row of the step in
-// between).
+// time every reader of the old contents has moved on: the writer has read
+// the step in between from one of the readers' warps, which had waited for
+// all warps of its row to publish that step (through the block barrier, or
+// its row's barrier below).
 //
 // Forcing belongs to the start of a step (it flips source words before the
 // pull).  Here the owner of the forcing column applies the flips of step j+1
@@ -43,11 +44,23 @@
 // The launcher takes the fewest bands of the smallest height the SMs allow,
 // which leaves a few SMs free for other streams' kernels.
 //
-// Synchronisation per step: one block barrier, plus the edge warps' waits.
-// Every wait is bounded (wait_ns, measured with %globaltimer): past it, or
-// when another block has given up, a warp records the error in *err, the
-// block finishes the step without further waits and returns after the
-// barrier.  *err is sticky: a launch that finds it set does nothing.
+// Synchronisation per step, one of two kinds (template parameter RS):
+//  - a block barrier;
+//  - row barriers (RS): each band row has two mbarriers in shared memory, by
+//    step parity, on which all lanes of the row's warps arrive once they
+//    have written a step's channels; before a step a warp waits for that
+//    step on its own row's and its band neighbour rows' barriers.  A warp is
+//    then at most one step ahead of the rows it pulls from, and a buffer is
+//    rewritten only after its readers have published the step that followed
+//    their reads.  Warps drift apart within those bounds, so warps with more
+//    work (walls, the obstacle, the forcing column, band edges) do not hold
+//    up the whole block every step.  Measured on GB300 it pays for
+//    FHP-II/III on blocks of 24 warps or more, which the launcher gives it.
+// The band's edge warps also wait for their halo items.  Every wait is
+// bounded (wait_ns, measured with %globaltimer): past it, or when another
+// warp or block has given up, a warp records the error in *err, finishes the
+// step without further waits, and the block returns after its next barrier.
+// *err is sticky: a launch that finds it set does nothing.
 #include "step_body.cuh"
 
 #include <algorithm>
@@ -98,6 +111,16 @@ LGCA_HDI uint64_t res_spread8(uint64_t b)
 }
 
 static constexpr int RES_HALO_SLOTS = 3;
+static constexpr int RES_KEYS = 16;  // steps of random keys a warp draws at once
+static constexpr int RES_ROWSYNC_WARPS = 24;  // FHP-II/III blocks from this many warps use row barriers
+
+// Shared memory of a block, in words: 8 control words, two row-barrier
+// words per band row, a key ring of 2 x RES_KEYS words per warp, then the
+// two step buffers of rpb x SP x nw words.
+LGCA_HDI size_t res_smem_words(int SP, int nw, int rpb, int wpr)
+{
+    return 8 + 2 * (size_t)rpb + 2 * RES_KEYS * (size_t)rpb * wpr + 2 * (size_t)rpb * SP * nw;
+}
 
 // Particle count and momentum of the cells in mask m of the words v (the
 // block-sum weights: FHP Jx2 = 2n0 + n1 - n2 - 2n3 - n4 + n5 in units of
@@ -141,6 +164,31 @@ __device__ __forceinline__ void st_items(uint64_t *p, uint64_t a, uint64_t b)
 {
     asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b) : "memory");
 }
+// mbarrier in shared memory: init with the arrivals of a phase, arrive
+// (release), and test whether the phase of the given parity has completed
+// (acquire)
+__device__ __forceinline__ void res_bar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(bar)),
+                 "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void res_bar_arrive(uint64_t *bar)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool res_bar_done(const uint64_t *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"((unsigned)__cvta_generic_to_shared(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
 __device__ __forceinline__ uint64_t res_timer_ns()
 {
     uint64_t t;
@@ -159,7 +207,7 @@ struct ResPlanes {
     static constexpr int WEST = HPP ? 2 : 3;   // the forcing's west-moving channel
 };
 
-template <int MODEL, int GM>
+template <int MODEL, int GM, bool RS>
 __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
     k_resident(const __grid_constant__ StepArgs a, const __grid_constant__ ResidentArgs R)
 {
@@ -167,14 +215,22 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
     constexpr int D = ModelTraits<MODEL>::D;
     constexpr int SP = P::SP, NV = P::NV, A0 = P::A0, B0 = P::B0, WEST = P::WEST;
     uint64_t *const sm = res_smem();
-    // control words: chirality keys [0..1] and forcing keys [2..3], and the
-    // stop flags [4..5], by step parity.  A stop flag is written before the
-    // barrier that ends its step and read by every warp right after it; the
-    // slot is not written again until every warp has passed the next
-    // barrier, so all warps of the block read the same value and return
-    // together.  The checks before the first step use slot 1.
+    // control words: the stop flags [4..5].  With a block barrier per step
+    // they go by step parity: a stop flag is written before the barrier that
+    // ends its step and read by every warp right after it; the slot is not
+    // written again until every warp has passed the next barrier, so all
+    // warps of the block read the same value and return together.  With row
+    // barriers, [4] is read once after the step loop.  The check before the
+    // first step uses slot 1.
     volatile uint64_t *const ctl = sm;
-    uint64_t *const rows = sm + 8;
+    uint64_t *const bars = sm + 8;  // row barriers [band row][step parity] (RS)
+    // each warp's random keys: the chirality keys of RES_KEYS steps, then the
+    // forcing keys of the steps after them, drawn by its lanes at once
+    // (lane i < RES_KEYS: chirality of step j + i; lane RES_KEYS + i:
+    // forcing of step j + i + 1), so that no warp draws keys alone on the
+    // path to the step barrier
+    uint64_t *const keyring = bars + 2 * R.rpb;
+    uint64_t *const rows = keyring + (size_t)2 * RES_KEYS * R.rpb * R.wpr;
     const PlaneGeom &g = a.g;
     const int nw = g.nw, np = nw >> 1;
     const size_t ps = g.ps;
@@ -206,9 +262,10 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
     if (warp == 0 && lane == 0) {
         ctl[4] = 0;
         ctl[5] = (uint64_t)(*(volatile int *)R.err);
-        ctl[0] = lgca_rng_key(R.seed, LGCA_STREAM_CHIR, R.t0);
-        ctl[3] = lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0 + 1);
+        if (RS)
+            for (int i = 0; i < 2 * R.rpb; ++i) res_bar_init(bars + i, 32u * (unsigned)R.wpr);
     }
+    if (RS) __syncthreads();  // the barriers are set up before anyone arrives
 
     // the row's state at the launch's first step
     uint64_t s[2][7] = {};
@@ -311,6 +368,33 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
             for (int k = 0; k < NV; ++k) put(hs, k, s[0][A0 + k], s[1][A0 + k]);
         }
     };
+    // publish; with row barriers every lane of the row's warps then arrives
+    // on the row's barrier of that step's parity
+    auto publish_arrive = [&](unsigned tm) {
+        publish(tm);
+        if (RS && rowok) res_bar_arrive(bars + 2 * r + (tm & 1));
+    };
+    // (row barriers) wait until this row and the band rows above and below
+    // have published step j; false when the wait gave up (every lane returns
+    // alike)
+    auto rows_ready = [&](int j) -> bool {
+        const unsigned par = (unsigned)(j >> 1) & 1u;
+        const uint64_t *bj = bars + (j & 1);
+        uint64_t t_start = 0;
+        for (int spin = 0;; ++spin) {
+            bool ok = res_bar_done(bj + 2 * r, par);
+            if (!top) ok = ok && res_bar_done(bj + 2 * (r - 1), par);
+            if (!bot) ok = ok && res_bar_done(bj + 2 * (r + 1), par);
+            if (__all_sync(FULL, ok)) return true;
+            if (spin == 0) t_start = res_timer_ns();
+            const bool give_up =
+                spin > 0 && (*(volatile int *)R.err || res_timer_ns() - t_start > R.wait_ns);
+            if (__any_sync(FULL, give_up)) {
+                if (lane == 0) atomicExch(R.err, 1);
+                return false;
+            }
+        }
+    };
     // an edge warp's words of time `tm` from a neighbour's halo slot: the
     // pair of each of its NV channels and, when `ek` >= 0, word `ew` of
     // channel slot ek (lanes with need_edge).  Polls until every item carries
@@ -351,20 +435,29 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
     };
 
     force(force_draw(lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0)));
-    publish(0u);
+    publish_arrive(0u);
     __syncthreads();
     if (ctl[5]) return;  // an earlier launch gave up: do not step a partial state (block-uniform)
 
     const bool nsrow = (y == 0) || (y == g.H - 1);
-    bool waiting = true;  // false once this warp gave up a wait
+    bool gave_up = false;  // this warp gave up a wait: it finishes the step without further waits
+    uint64_t *const kr = keyring + (size_t)2 * RES_KEYS * warp;
     for (int j = 0; j < R.nsteps; ++j) {
         const int cur = j & 1;
-        const uint64_t ck = ctl[cur], fk = ctl[2 + (cur ^ 1)];
-        if (warp == 0 && lane == 0) {  // keys of the next steps, read after the barrier
-            ctl[cur ^ 1] = lgca_rng_key(R.seed, LGCA_STREAM_CHIR, R.t0 + (uint64_t)j + 1);
-            ctl[2 + cur] = lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0 + (uint64_t)j + 2);
+        // (warp-uniform) with row barriers, warps past the band's last row
+        // have nothing to wait for, and a warp that gave up stops here
+        if (RS && (gave_up || !rowok)) break;
+        if (j % RES_KEYS == 0) {
+            __syncwarp();  // the ring's last keys have been read
+            const int i = lane % RES_KEYS;
+            kr[lane] = lane < RES_KEYS ? lgca_rng_key(R.seed, LGCA_STREAM_CHIR, R.t0 + (uint64_t)(j + i))
+                                       : lgca_rng_key(R.seed, LGCA_STREAM_FORCE, R.t0 + (uint64_t)(j + i) + 1);
+            __syncwarp();
         }
-        if (rowok) {  // (warp-uniform: warps past the band's last row only meet the barrier)
+        // chirality key of step j, forcing key of step j + 1
+        const uint64_t ck = kr[j % RES_KEYS], fk = kr[RES_KEYS + j % RES_KEYS];
+        if (RS && !rows_ready(j)) gave_up = true;
+        if (rowok) {  // (warp-uniform: warps past the band's last row only meet the block barrier)
             // the forcing draw of the next step, made now, off the step's end
             const bool flip_next = force_draw(fk);
             // chirality of word k of the pair, drawn (or, frozen, read) where it is used
@@ -402,11 +495,9 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
                 uint64_t v[2][2] = {{0, 0}, {0, 0}}, e = 0;
                 // FHP: the edge word is channel 1 west (even rows) or channel 2 east (odd rows)
                 const int ek = MODEL == M_HPP ? -1 : (even ? 0 : 1);
-                if (waiting && !halo_get(halo_slot((unsigned)j, bl, 1), (unsigned)j, ek,
-                                         even ? widx : eidx, even ? need_w : need_e, v, e)) {
-                    waiting = false;
-                    if (lane == 0) ctl[4 + cur] = 1;
-                }
+                if (!gave_up && !halo_get(halo_slot((unsigned)j, bl, 1), (unsigned)j, ek,
+                                          even ? widx : eidx, even ? need_w : need_e, v, e))
+                    gave_up = true;
 #pragma unroll
                 for (int k = 0; k < NV; ++k) {
                     n[0][A0 + k] = v[0][k];
@@ -434,11 +525,9 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
                 uint64_t v[2][2] = {{0, 0}, {0, 0}}, e = 0;
                 // FHP: the edge word is channel 5 west (even rows) or channel 4 east (odd rows)
                 const int ek = MODEL == M_HPP ? -1 : (even ? 1 : 0);
-                if (waiting && !halo_get(halo_slot((unsigned)j, br, 0), (unsigned)j, ek,
-                                         even ? widx : eidx, even ? need_w : need_e, v, e)) {
-                    waiting = false;
-                    if (lane == 0) ctl[4 + cur] = 1;
-                }
+                if (!gave_up && !halo_get(halo_slot((unsigned)j, br, 0), (unsigned)j, ek,
+                                          even ? widx : eidx, even ? need_w : need_e, v, e))
+                    gave_up = true;
 #pragma unroll
                 for (int k = 0; k < NV; ++k) {
                     n[0][B0 + k] = v[0][k];
@@ -534,11 +623,19 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
 
             if (j + 1 < R.nsteps) {
                 force(flip_next);
-                publish((unsigned)j + 1);
+                publish_arrive((unsigned)j + 1);
             }
         }
+        if (!RS) {
+            if (gave_up && lane == 0) ctl[4 + cur] = 1;
+            __syncthreads();
+            if (ctl[4 + cur]) return;  // a wait of this step gave up (block-uniform)
+        }
+    }
+    if (RS) {
+        if (gave_up && lane == 0) ctl[4] = 1;
         __syncthreads();
-        if (ctl[4 + cur]) return;  // a wait of this step gave up (block-uniform)
+        if (ctl[4]) return;  // a wait gave up (block-uniform)
     }
 
     // the result of the last step: the planes, and the byte-per-cell layout
@@ -610,10 +707,9 @@ __global__ void __launch_bounds__(32 * RES_MAX_WARPS, 1)
 #ifndef LGCA_HOST_EMULATION
 // ------------------------------------------------------------------ launcher
 
-static size_t resident_smem_bytes(int model, const PlaneGeom &g, int rpb)
+static size_t resident_smem_bytes(int model, const PlaneGeom &g, int rpb, int wpr)
 {
-    const int SP = model == M_HPP ? 4 : 6;
-    return (8 + 2 * (size_t)rpb * SP * g.nw) * sizeof(uint64_t);
+    return res_smem_words(model == M_HPP ? 4 : 6, g.nw, rpb, wpr) * sizeof(uint64_t);
 }
 
 bool resident_sums_fit(int model, const PlaneGeom &g, const ResidentShape &sh, int B)
@@ -621,7 +717,9 @@ bool resident_sums_fit(int model, const PlaneGeom &g, const ResidentShape &sh, i
     if (!(B == 8 || B == 16 || B == 32 || B == 64)) return false;
     const size_t Wb = (size_t)(g.W + B - 1) / B;
     const size_t nbr = (size_t)(sh.rpb + B - 2) / B + 1;  // block rows a band can touch
-    return nbr * Wb * 3 * sizeof(int) <= resident_smem_bytes(model, g, sh.rpb) - 8 * sizeof(uint64_t);
+    // the accumulators take the step buffers' place
+    const size_t bufs = 2 * (size_t)sh.rpb * (model == M_HPP ? 4 : 6) * g.nw * sizeof(uint64_t);
+    return nbr * Wb * 3 * sizeof(int) <= bufs;
 }
 
 bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out)
@@ -636,21 +734,22 @@ bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out)
     const int rpb = (g.H + std::min(sm_count(), g.H) - 1) / std::min(sm_count(), g.H);
     const int nblk = (g.H + rpb - 1) / rpb;
     if (rpb * wpr > RES_MAX_WARPS) return false;
-    const size_t smem = resident_smem_bytes(model, g, rpb);
+    const size_t smem = resident_smem_bytes(model, g, rpb, wpr);
     if (smem > RES_MAX_SMEM) return false;
     out.nblk = nblk;
     out.wpr = wpr;
     out.rpb = rpb;
     out.smem = smem;
+    out.rowsync = model >= M_FHP_II && rpb * wpr >= RES_ROWSYNC_WARPS;
     out.halo_words = (size_t)RES_HALO_SLOTS * nblk * 2 * 2 * g.nw * 2;
     return true;
 }
 
-template <int MODEL, int GM>
+template <int MODEL, int GM, bool RS>
 static cudaError_t res_launch(const StepArgs &a, const ResidentShape &sh, const ResidentArgs &R,
                               cudaStream_t st)
 {
-    auto kern = k_resident<MODEL, GM>;
+    auto kern = k_resident<MODEL, GM, RS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -665,14 +764,14 @@ static cudaError_t res_launch(const StepArgs &a, const ResidentShape &sh, const 
                                       sh.smem, st);
 }
 
-template <int MODEL>
+template <int MODEL, bool RS>
 static cudaError_t res_model(int gm, const StepArgs &a, const ResidentShape &sh,
                              const ResidentArgs &R, cudaStream_t st)
 {
     switch (gm) {
-    case GEOM_NONE: return res_launch<MODEL, GEOM_NONE>(a, sh, R, st);
-    case GEOM_NOSLIP: return res_launch<MODEL, GEOM_NOSLIP>(a, sh, R, st);
-    default: return res_launch<MODEL, GEOM_FULL>(a, sh, R, st);
+    case GEOM_NONE: return res_launch<MODEL, GEOM_NONE, RS>(a, sh, R, st);
+    case GEOM_NOSLIP: return res_launch<MODEL, GEOM_NOSLIP, RS>(a, sh, R, st);
+    default: return res_launch<MODEL, GEOM_FULL, RS>(a, sh, R, st);
     }
 }
 
@@ -703,10 +802,15 @@ cudaError_t launch_resident(int model, int gm, const StepArgs &a, const Resident
     R.sums_N = sums ? sums->N : nullptr;
     R.sums_Jx2 = sums ? sums->Jx2 : nullptr;
     R.sums_Jy = sums ? sums->Jy : nullptr;
+    // row barriers for FHP-II/III blocks of many warps (measured on GB300:
+    // 1-3.5 % faster there; slower for HPP and FHP-I, and on blocks of 14
+    // warps)
     switch (model) {
-    case M_HPP: return res_model<M_HPP>(gm, a, sh, R, st);
-    case M_FHP_I: return res_model<M_FHP_I>(gm, a, sh, R, st);
-    default: return res_model<M_FHP_II>(gm, a, sh, R, st);  // FHP-II and FHP-III share one rule set
+    case M_HPP: return res_model<M_HPP, false>(gm, a, sh, R, st);
+    case M_FHP_I: return res_model<M_FHP_I, false>(gm, a, sh, R, st);
+    default:  // FHP-II and FHP-III share one rule set
+        return sh.rowsync ? res_model<M_FHP_II, true>(gm, a, sh, R, st)
+                          : res_model<M_FHP_II, false>(gm, a, sh, R, st);
     }
 }
 #endif

@@ -9,7 +9,7 @@
 // result with the oracle.
 //
 //   resident_emu IN OUT
-//   IN:  int32 model, W, H, steps, force_x, nblk, chunk, withhold, aos, B;
+//   IN:  int32 model, W, H, steps, force_x, nblk, chunk, withhold, aos, B, rowsync;
 //        uint64 seed, t0, force_thr, wait_ns; H*W uint8 cells (bit d = channel d);
 //        H*W uint8 cell types (0 fluid, 1 no-slip, 2 slip)
 //   OUT: int32 err; H*W uint8 cells after `steps` steps, run as launches of
@@ -19,6 +19,7 @@
 //   aos & 2: every launch also writes its result in that layout.
 //   B > 0: the last launch also adds up the B x B block sums of its result,
 //   written last as int32 N, Jx2, Jy (each ceil(H/B) x ceil(W/B)).
+//   rowsync 1: the kernel's row-barrier form; 0: its block-barrier form.
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -124,6 +125,24 @@ inline void st_items(uint64_t *p, uint64_t a, uint64_t b)
     __atomic_store_n(p, a, __ATOMIC_RELAXED);
     __atomic_store_n(p + 1, b, __ATOMIC_RELAXED);
 }
+// an mbarrier as one word: completed phases << 48 | arrivals per phase << 24
+// | arrivals still missing in the current phase
+inline void res_bar_init(uint64_t *bar, unsigned count)
+{
+    __atomic_store_n(bar, ((uint64_t)count << 24) | count, __ATOMIC_RELEASE);
+}
+inline void res_bar_arrive(uint64_t *bar)
+{
+    uint64_t w = __atomic_load_n(bar, __ATOMIC_RELAXED), nw;
+    do {
+        const uint64_t pend = w & 0xffffff, cnt = (w >> 24) & 0xffffff, ph = w >> 48;
+        nw = pend == 1 ? ((ph + 1) << 48) | (cnt << 24) | cnt : w - 1;
+    } while (!__atomic_compare_exchange_n(bar, &w, nw, true, __ATOMIC_ACQ_REL, __ATOMIC_RELAXED));
+}
+inline bool res_bar_done(const uint64_t *bar, unsigned parity)
+{
+    return ((__atomic_load_n(bar, __ATOMIC_ACQUIRE) >> 48) & 1) != parity;
+}
 inline uint64_t res_timer_ns()
 {
     return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
@@ -136,12 +155,12 @@ inline uint64_t res_timer_ns()
 using namespace lgca_gpu;
 
 // one cooperative launch of the kernel: every block's threads at once
-template <int MODEL, int GM>
+template <int MODEL, int GM, bool RS>
 static void launch(const StepArgs &a, const ResidentArgs &R)
 {
     constexpr int SP = ResPlanes<MODEL>::SP;
     const int warps = R.rpb * R.wpr;
-    const size_t smem_words = 8 + 2 * (size_t)R.rpb * SP * a.g.nw;
+    const size_t smem_words = res_smem_words(SP, a.g.nw, R.rpb, R.wpr);
     std::vector<std::vector<uint64_t>> sm(R.nblk, std::vector<uint64_t>(smem_words, 0));
     std::vector<std::unique_ptr<emu::Warp[]>> wp;
     std::vector<std::unique_ptr<std::barrier<>>> bb;
@@ -161,19 +180,25 @@ static void launch(const StepArgs &a, const ResidentArgs &R)
                 emu::warp = &wp[b][i >> 5];
                 emu::block_bar = bb[b].get();
                 emu::smem = sm[b].data();
-                k_resident<MODEL, GM>(a, R);
+                k_resident<MODEL, GM, RS>(a, R);
                 // a block's threads that returned early leave the barrier
                 // alone: the kernel returns block-uniformly
             });
     for (auto &x : th) x.join();
 }
 
-template <int MODEL>
+template <int MODEL, bool RS>
 static void launch_gm(int gm, const StepArgs &a, const ResidentArgs &R)
 {
-    if (gm == GEOM_NONE) launch<MODEL, GEOM_NONE>(a, R);
-    else if (gm == GEOM_NOSLIP) launch<MODEL, GEOM_NOSLIP>(a, R);
-    else launch<MODEL, GEOM_FULL>(a, R);
+    if (gm == GEOM_NONE) launch<MODEL, GEOM_NONE, RS>(a, R);
+    else if (gm == GEOM_NOSLIP) launch<MODEL, GEOM_NOSLIP, RS>(a, R);
+    else launch<MODEL, GEOM_FULL, RS>(a, R);
+}
+template <int MODEL>
+static void launch_sync(bool rs, int gm, const StepArgs &a, const ResidentArgs &R)
+{
+    if (rs) launch_gm<MODEL, true>(gm, a, R);
+    else launch_gm<MODEL, false>(gm, a, R);
 }
 
 int main(int argc, char **argv)
@@ -184,11 +209,11 @@ int main(int argc, char **argv)
     }
     FILE *f = std::fopen(argv[1], "rb");
     if (!f) return 2;
-    int32_t hdr[10];
+    int32_t hdr[11];
     uint64_t u[4];
     if (std::fread(hdr, sizeof(hdr), 1, f) != 1 || std::fread(u, sizeof(u), 1, f) != 1) return 2;
     const int model = hdr[0], W = hdr[1], H = hdr[2], steps = hdr[3], fx = hdr[4], nblk = hdr[5],
-              chunk = hdr[6], withhold = hdr[7], aos = hdr[8], sumsB = hdr[9];
+              chunk = hdr[6], withhold = hdr[7], aos = hdr[8], sumsB = hdr[9], rowsync = hdr[10];
     const uint64_t seed = u[0], t0 = u[1], thr = u[2], wait_ns = u[3];
     std::vector<uint8_t> cells((size_t)W * H), types((size_t)W * H);
     if (std::fread(cells.data(), 1, cells.size(), f) != cells.size() ||
@@ -264,9 +289,9 @@ int main(int argc, char **argv)
         R.sums_N = sums.data();
         R.sums_Jx2 = sums.data() + (size_t)Wb * Hb;
         R.sums_Jy = sums.data() + (size_t)2 * Wb * Hb;
-        if (model == 0) launch_gm<M_HPP>(gm, a, R);
-        else if (model == 1) launch_gm<M_FHP_I>(gm, a, R);
-        else launch_gm<M_FHP_II>(gm, a, R);
+        if (model == 0) launch_sync<M_HPP>(rowsync != 0, gm, a, R);
+        else if (model == 1) launch_sync<M_FHP_I>(rowsync != 0, gm, a, R);
+        else launch_sync<M_FHP_II>(rowsync != 0, gm, a, R);
         cur ^= 1;
     }
     const std::vector<uint64_t> &res = buf[cur];

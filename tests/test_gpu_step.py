@@ -260,6 +260,24 @@ def test_resident_kernel_vs_oracle(gpu, oracle, model, geom):
                 assert np.array_equal(got, want), (W, H, fx, chunks)
 
 
+@pytest.mark.parametrize("model,geom", [(2, "pipe"), (3, "disc"), (3, "periodic")])
+def test_resident_row_barrier_form_vs_oracle(gpu, oracle, model, geom):
+    """FHP-II/III lattices whose bands take 24 or more warps run the resident
+    kernel with row barriers instead of a block barrier per step: one warp
+    per row (4096 x 3648, bands of 24 rows) and two (8192 x 2100, bands of
+    14 rows), over 40 steps in one call and in calls of 17 and 23."""
+    rng = np.random.default_rng(model * 5 + len(geom))
+    for W, H in [(4096, 3648), (8192, 2100)]:
+        types = GEOMS[geom](W, H)
+        seed = int(rng.integers(1 << 40))
+        st = oracle.init_bernoulli(model, W, H, types, seed=seed, p_move=0.3, p_rest=0.3)
+        kw = dict(types=types, seed=seed, force_x=int(rng.integers(W)), force_p=0.2, t0=7)
+        want = oracle.run(model, st, 40, **kw)
+        for chunks in (None, [17, 23]):
+            got = run_gpu(gpu, model, st, 40, variant=6, chunks=chunks, **kw)
+            assert np.array_equal(got, want), (W, H, chunks)
+
+
 @pytest.mark.parametrize("model", [1, 3])
 def test_resident_kernel_frozen_chirality(gpu, oracle, model):
     rng = np.random.default_rng(7)

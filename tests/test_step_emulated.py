@@ -324,12 +324,12 @@ def resident_emu(tmp_path_factory):
 
 
 def run_resident(exe, tmp, model, cells, types, steps, seed, t0, force_x, force_thr, nblk,
-                 chunk, withhold=-1, wait_ns=10_000_000_000, aos=0, B=0):
+                 chunk, withhold=-1, wait_ns=10_000_000_000, aos=0, B=0, rowsync=0):
     H, W = cells.shape
     inp, out = tmp / "rin.bin", tmp / "rout.bin"
     with open(inp, "wb") as f:
-        f.write(struct.pack("<10i4Q", model, W, H, steps, force_x, nblk, chunk, withhold, aos, B,
-                            seed, t0, force_thr, wait_ns))
+        f.write(struct.pack("<11i4Q", model, W, H, steps, force_x, nblk, chunk, withhold, aos, B,
+                            rowsync, seed, t0, force_thr, wait_ns))
         f.write(np.ascontiguousarray(cells, np.uint8).tobytes())
         f.write(np.ascontiguousarray(types, np.uint8).tobytes())
     r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True, env=ENV, timeout=600)
@@ -354,14 +354,16 @@ RESIDENT = [(4096, 12, 3), (8192, 8, 2), (128, 6, 6), (1024, 10, 1), (2048, 14, 
             (4096, 6, 6)]
 
 
-@pytest.mark.parametrize("model", [0, 1, 3])
+@pytest.mark.parametrize("model,rowsync", [(0, 0), (1, 0), (3, 0), (3, 1)])
 @pytest.mark.parametrize("geom", list(GEOMS))
-def test_emulated_resident_kernel_equals_oracle(resident_emu, tmp_path, oracle, model, geom):
+def test_emulated_resident_kernel_equals_oracle(resident_emu, tmp_path, oracle, model, geom,
+                                                rowsync):
     """The resident kernel k_resident (state on chip across steps, band edges
     exchanged through halo slots and step counters) on its whole grid: every
     model and geometry mode, forcing at the x seam and inside a row, steps
     run as one launch and split over several (forcing at the launch
-    boundary, results written back unforced)."""
+    boundary, results written back unforced); FHP-III also in the
+    row-barrier form."""
     rng = np.random.default_rng(model * 7 + len(geom))
     for W, H, nblk in RESIDENT:
         if model != 0 and H % 2:
@@ -374,7 +376,7 @@ def test_emulated_resident_kernel_equals_oracle(resident_emu, tmp_path, oracle, 
             want = oracle.run(model, st, 6, types=types, seed=13, t0=9, force_x=fx, force_p=p)
             for chunk in (6, 4):
                 err, got = run_resident(resident_emu, tmp_path, model, st, types.astype(np.uint8),
-                                        6, 13, 9, fx, thr, nblk, chunk)
+                                        6, 13, 9, fx, thr, nblk, chunk, rowsync=rowsync)
                 assert err == 0
                 assert np.array_equal(got, want), (model, geom, W, H, nblk, fx, chunk)
             # input read and result written in the byte-per-cell layout by the
@@ -383,7 +385,7 @@ def test_emulated_resident_kernel_equals_oracle(resident_emu, tmp_path, oracle, 
             B = (8, 16, 32, 64)[nblk % 4]
             err, got, aos_out, sums = run_resident(resident_emu, tmp_path, model, noisy,
                                                    types.astype(np.uint8), 6, 13, 9, fx, thr, nblk,
-                                                   4, aos=3, B=B)
+                                                   4, aos=3, B=B, rowsync=rowsync)
             assert err == 0
             assert np.array_equal(got, want) and np.array_equal(aos_out, want), (model, W, H)
             # B x B block sums of the result, fused into the last launch
@@ -391,11 +393,31 @@ def test_emulated_resident_kernel_equals_oracle(resident_emu, tmp_path, oracle, 
                 assert np.array_equal(sums[i], w), (model, W, H, nblk, B, i)
 
 
+@pytest.mark.parametrize("model,geom,rowsync", [(3, "disc", 0), (3, "disc", 1), (1, "periodic", 0),
+                                               (0, "pipe", 0)])
+def test_emulated_resident_long_calls_equal_oracle(resident_emu, tmp_path, oracle, model, geom,
+                                                   rowsync):
+    """Calls of more steps than a warp draws random keys for at once (16),
+    so that every warp's key ring refills mid-call and the row barriers go
+    through many phases: one launch of 37 steps, and 40 steps as launches of
+    17."""
+    for W, H, nblk in [(2048, 14, 4), (8192, 8, 2)]:
+        types = GEOMS[geom](W, H)
+        st = oracle.init_bernoulli(model, W, H, types, seed=5, p_move=0.35, p_rest=0.3)
+        thr = oracle.prob_threshold(0.3)
+        for steps, chunk in ((37, 37), (40, 17)):
+            want = oracle.run(model, st, steps, types=types, seed=13, t0=3, force_x=W // 3,
+                              force_p=0.3)
+            err, got = run_resident(resident_emu, tmp_path, model, st, types.astype(np.uint8),
+                                    steps, 13, 3, W // 3, thr, nblk, chunk, rowsync=rowsync)
+            assert err == 0 and np.array_equal(got, want), (model, geom, W, H, steps, chunk)
+
+
 def test_emulated_resident_kernel_stays_in_bounds(tmp_path, oracle):
     """k_resident's shared-memory, halo and state accesses stay in bounds:
     the emulator built with the address and undefined-behaviour sanitizers."""
     exe = _build_resident(tmp_path / "resident_emu_asan", sanitize=True)
-    for model in (0, 3):
+    for model, rowsync in ((0, 0), (3, 0), (3, 1)):
         for W, H, nblk in [(4096, 6, 3), (8192, 4, 2), (128, 4, 4)]:
             types = GEOMS["slip"](W, H)
             st = oracle.init_bernoulli(model, W, H, types, seed=5, p_move=0.35, p_rest=0.3)
@@ -403,16 +425,18 @@ def test_emulated_resident_kernel_stays_in_bounds(tmp_path, oracle):
             want = oracle.run(model, st, 3, types=types, seed=13, t0=9, force_x=W - 1,
                               force_p=0.4)
             err, got = run_resident(exe, tmp_path, model, st, types.astype(np.uint8), 3, 13, 9,
-                                    W - 1, thr, nblk, 3)
-            assert err == 0 and np.array_equal(got, want), (model, W, H, nblk)
+                                    W - 1, thr, nblk, 3, rowsync=rowsync)
+            assert err == 0 and np.array_equal(got, want), (model, W, H, nblk, rowsync)
 
 
-def test_emulated_resident_wait_gives_up(resident_emu, tmp_path, oracle):
-    """A block that never raises its step counters makes its neighbours'
-    bounded waits run out: every block returns, the error flag is set."""
+@pytest.mark.parametrize("rowsync", [0, 1])
+def test_emulated_resident_wait_gives_up(resident_emu, tmp_path, oracle, rowsync):
+    """A block that never writes its halo items makes its neighbours' bounded
+    waits run out: every block returns, the error flag is set (with row
+    barriers, also the waits of the rows behind the band edges)."""
     W, H = 4096, 12
     types = GEOMS["periodic"](W, H)
     st = oracle.init_bernoulli(3, W, H, types, seed=5, p_move=0.35, p_rest=0.3)
     err, _ = run_resident(resident_emu, tmp_path, 3, st, types.astype(np.uint8), 5, 13, 0, -1, 0,
-                          3, 5, withhold=1, wait_ns=2_000_000)
+                          3, 5, withhold=1, wait_ns=2_000_000, rowsync=rowsync)
     assert err == 1
