@@ -274,8 +274,8 @@ def served_leg(rate, duration):
             "evictions": r["evictions"], "batch_calls": r["batch_calls"],
             "limited_by": "the batch step kernel (k_batch_persist), at 0.90 of the measured HBM "
                           "bandwidth on a 1 G-site mix (profiles/batch_512_mixed.md); FCFS runs "
-                          "each job alone with the fastest single-lattice path, the resident "
-                          "kernel for jobs of 1024+ warp rows"}
+                          "each job alone with the fastest single-lattice path (the automatic "
+                          "choice, which takes the resident kernel for large jobs)"}
 
 
 def run_ours(args):
@@ -366,14 +366,14 @@ def run_ours(args):
                     "traffic": profiled_traffic(prof), "inst_per_launch": inst,
                     "steps_per_launch": STEPS_PER_CHUNK, "launch_ms": launch_s * 1e3,
                     "alu_pipe_active": profiled_value(prof, "alu_pipe_active"),
-                    "kernel": "k_resident<FHP_II/III, GEOM_NOSLIP>: 100 steps per launch, the "
-                              "lattice on chip between steps",
+                    "kernel": "k_resident<FHP_II/III, GEOM_NOSLIP, row barriers>: 100 steps "
+                              "per launch, the lattice on chip between steps",
                     "hbm_equivalent": {"bytes_per_step": bytes_step,
                                        "achieved": bytes_step / step_s / 1e9, "peak": hbm_peak,
                                        "unit": "GB/s", "peak_kind": peak_kind},
                     "note": "DRAM traffic per launch is the state read once (ncu); the ALU pipe "
-                            "is two-thirds busy while SMs are active and runs logic at half the "
-                            "issue rate, so frac (issue) near 0.6 is the ALU bound; "
+                            "is 78 % busy while SMs are active and runs logic at half the "
+                            "issue rate, so frac (issue) near 0.6 is close to the ALU bound; "
                             "hbm_equivalent is the algorithmic bytes of the same steps over "
                             "time, which never reach HBM; the HBM gate is roofline_gate"}
     else:

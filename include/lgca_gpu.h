@@ -144,8 +144,10 @@ int lgca_set_chirality(lgca_handle h, const uint8_t *field);
 int lgca_set_temporal_depth(lgca_handle h, int depth);
 
 /* Kernel family for the steps: 0 = automatic (default: the resident form 6
- * for calls of 16 or more steps on lattices it holds with rows of at least
- * 2048 sites and at least 1024 rows x ceil(dim_x / 4096); the register
+ * on lattices it holds, for calls of 16 or more steps on lattices of at
+ * least 4 Mi sites with rows of at least 2048 sites, and for calls of 64 or
+ * more steps on lattices of at least 1 Mi sites with rows of at least 4096
+ * sites; the register
  * wavefront at 4 steps per pass for HPP lattices of 64 Mi sites or more and
  * at 4 (FHP-I) or 2 (FHP-II/III) for FHP lattices of 256 Mi sites or more;
  * else one step per pass; a temporal depth above 1 selects the wavefront),

@@ -190,10 +190,14 @@ struct ResidentShape {
     bool rowsync;        // row barriers instead of a block barrier per step
 };
 static constexpr size_t RES_MAX_SMEM = 200 * 1024;
-// the automatic choice gives the resident form calls of at least this many
-// steps on lattices of at least this many warp rows (rows x warps per row)
+// the automatic choice gives the resident form calls of at least
+// RESIDENT_MIN_STEPS steps on lattices of at least RESIDENT_MIN_SITES sites,
+// and calls of at least RESIDENT_LONG_STEPS steps on lattices of at least
+// RESIDENT_LONG_SITES sites whose rows fill whole warps (4096+ sites)
 static constexpr int RESIDENT_MIN_STEPS = 16;
-static constexpr long long RESIDENT_MIN_WARPS = 1024;
+static constexpr long long RESIDENT_MIN_SITES = 4LL << 20;
+static constexpr int RESIDENT_LONG_STEPS = 64;
+static constexpr long long RESIDENT_LONG_SITES = 1LL << 20;
 bool resident_shape(int model, const PlaneGeom &g, ResidentShape &out);
 // aos_in / aos_out (device, H x W bytes, bit d = channel d; either may be
 // null): the launch's input is read from aos_in instead of a.src, and its

@@ -594,10 +594,15 @@ int step_family(const lgca_lattice *h, int nsteps, ResidentShape *rs)
 {
     if (h->variant == VARIANT_PERSIST && nsteps > 1) return VARIANT_PERSIST;
     // the resident form: asked for, or chosen for calls of enough steps to
-    // repay its launch on lattices it holds with at least half of every
-    // warp's lanes busy and enough warps to fill the SMs (measured on GB300:
-    // below about 1024 warp rows, or 16 steps per call, chained one-step
-    // launches are as fast or faster)
+    // repay its launch on lattices it holds that are large enough.  Measured
+    // on GB300 (FHP-III, us per step, chained one-step launches / resident):
+    //   2048 x 1024, 16 steps per call: 2.05 / 2.45; 100 steps: 2.05 / 2.09
+    //   2048 x 2048, 16 steps: 3.96 / 3.06
+    //   4096 x 256, 16 steps: 1.84 / 2.28; 100 steps: 1.86 / 1.77
+    //   4096 x 512, 16 steps: 2.14 / 2.29; 100 steps: 2.06 / 1.77
+    // so: 16+ steps from 4 Mi sites on rows of 2048+ sites (at least half of
+    // every warp's lanes busy); 64+ steps from 1 Mi sites when the rows fill
+    // whole warps (4096+ sites)
     ResidentShape tmp;
     ResidentShape &shape = rs ? *rs : tmp;
     if (nsteps <= 0 || nsteps > RESIDENT_MAX_STEPS || !resident_shape(h->model, h->g, shape))
@@ -610,8 +615,12 @@ int step_family(const lgca_lattice *h, int nsteps, ResidentShape *rs)
     if (cudaStreamIsCapturing(h->stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
         return VARIANT_PLAIN;
     if (h->variant == VARIANT_RESIDENT) return VARIANT_RESIDENT;
-    if (h->variant == VARIANT_AUTO && h->depth == 1 && nsteps >= RESIDENT_MIN_STEPS &&
-        h->g.nw / 2 >= 16 && (long long)h->g.H * shape.wpr >= RESIDENT_MIN_WARPS)
+    // (np = pairs per row: lanes busy in a row's warps)
+    const long long sites = (long long)h->g.W * h->g.H;
+    const int np = h->g.nw / 2;
+    if (h->variant == VARIANT_AUTO && h->depth == 1 &&
+        ((nsteps >= RESIDENT_MIN_STEPS && sites >= RESIDENT_MIN_SITES && np >= 16) ||
+         (nsteps >= RESIDENT_LONG_STEPS && sites >= RESIDENT_LONG_SITES && np >= 32)))
         return VARIANT_RESIDENT;
     return VARIANT_PLAIN;
 }

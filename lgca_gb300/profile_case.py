@@ -30,7 +30,7 @@ def main(argv=None):
                          "4 persistent bands, 5 two words per lane, 6 resident")
     ap.add_argument("--chunk", type=int, default=0,
                     help="steps per call (default: 1, or the depth); the automatic choice takes "
-                         "the resident form for calls of 16 steps or more where it fits")
+                         "the resident form for large enough lattices and calls where it fits")
     ap.add_argument("--geometry", default="periodic", choices=["periodic", "pipe", "karman"])
     ap.add_argument("--force-x", type=int, default=-1)
     ap.add_argument("--force-p", type=float, default=0.0)

@@ -396,9 +396,10 @@ def test_roofline_sweep_kernels_at_1024(gpu, oracle, model, p):
 
 def test_step_plan_names_the_kernels_a_call_runs(gpu, oracle):
     """lgca_step_plan reports the kernel family and launches of a call; the
-    automatic choice takes the resident form for calls of 16 steps or more on
-    lattices it holds that fill the SMs, and passes of several steps on
-    lattices far beyond L2."""
+    automatic choice takes the resident form, where it holds the lattice, for
+    calls of 16 steps or more from 4 Mi sites (rows of 2048+ sites) and of 64
+    or more from 1 Mi sites (rows of 4096+ sites), and passes of several
+    steps on lattices far beyond L2."""
     W, H = 8192, 2048
     with gpu.GpuLattice(3, W, H, seed=2) as L:
         assert L.step_plan(100) == (6, 1)
@@ -413,10 +414,19 @@ def test_step_plan_names_the_kernels_a_call_runs(gpu, oracle):
         assert L.step_plan(10) == (1, 10)
     with gpu.GpuLattice(3, 4160, 64, seed=2) as L:  # odd word count: not held
         assert L.step_plan(100) == (1, 100)
-    with gpu.GpuLattice(3, 4096, 256, seed=2) as L:  # held, but too few warps to pay
-        assert L.step_plan(100) == (1, 100)
-        L.set_kernel_variant(6)
+    with gpu.GpuLattice(3, 4096, 256, seed=2) as L:  # 1 Mi sites: long calls only
         assert L.step_plan(100) == (6, 1)
+        assert L.step_plan(64) == (6, 1)
+        assert L.step_plan(63) == (1, 63)
+        L.set_kernel_variant(6)
+        assert L.step_plan(16) == (6, 1)
+    with gpu.GpuLattice(3, 4096, 128, seed=2) as L:  # held, but too small to pay
+        assert L.step_plan(100) == (1, 100)
+    with gpu.GpuLattice(3, 2048, 1024, seed=2) as L:  # 2 Mi sites, half of every warp idle
+        assert L.step_plan(100) == (1, 100)
+    with gpu.GpuLattice(3, 2048, 2048, seed=2) as L:  # 4 Mi sites
+        assert L.step_plan(16) == (6, 1)
+        assert L.step_plan(15) == (1, 15)
     # far beyond L2: HPP from 64 Mi sites takes 4 steps per pass on the wavefront,
     # with the same bits as one step per pass
     W, H = 8192, 8192
