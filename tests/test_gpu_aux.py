@@ -296,15 +296,17 @@ def test_paint_rejects_bad_arguments(gpu):
         assert not L.get_cell_types().any()
 
 
-@pytest.mark.parametrize("variant", [4, 6])
-def test_persistent_wait_timeout_marks_handle_failed_until_cleared(gpu, oracle, variant):
+@pytest.mark.parametrize("variant,W,H", [(4, 512, 256), (6, 512, 256), (6, 4096, 3648)])
+def test_persistent_wait_timeout_marks_handle_failed_until_cleared(gpu, oracle, variant, W, H):
     """One block of the persistent (4) or resident (6) kernel withholds its
     progress (test hook),
     so its neighbours' bounded waits run out after the 1 ms limit.  Every call
     that waits for the handle then reports LGCA_ERR_TIMEOUT, and persistent
     calls queued behind the failure do not step, until lgca_clear_error; after
-    a state is reloaded the handle steps correctly again."""
-    model, W, H = 3, 512, 256
+    a state is reloaded the handle steps correctly again.  4096 x 3648 runs
+    the resident kernel with row barriers (FHP-III, bands of 24 warps), whose
+    row waits give up once the edge warps' halo waits have."""
+    model = 3
     st = oracle.init_bernoulli(model, W, H, None, seed=4, p_move=0.3, p_rest=0.3)
     with gpu.GpuLattice(model, W, H, seed=4) as L:
         L.upload(st)
