@@ -359,7 +359,7 @@ RESIDENT = [(4096, 12, 3), (8192, 8, 2), (128, 6, 6), (1024, 10, 1), (2048, 14, 
 def test_emulated_resident_kernel_equals_oracle(resident_emu, tmp_path, oracle, model, geom,
                                                 rowsync):
     """The resident kernel k_resident (state on chip across steps, band edges
-    exchanged through halo slots and step counters) on its whole grid: every
+    exchanged as step-tagged halo items) on its whole grid: every
     model and geometry mode, forcing at the x seam and inside a row, steps
     run as one launch and split over several (forcing at the launch
     boundary, results written back unforced); FHP-III also in the
