@@ -255,7 +255,7 @@ def served_leg(rate, duration):
     every streamed field compared."""
     from lgca_gb300 import serve as SV
     r = SV.serve(rate, duration, budget=150e9, drain_limit=10.0, verify=8, fcfs=True,
-                 fcfs_sample=200)
+                 fcfs_sample=1000)
     fm = r.get("fcfs_measured", {})
     return {"rate_jobs_s": rate, "duration_s": duration, "jobs": r["jobs"],
             "completed": r["completed"], "backlog": r["backlog"], "elapsed_s": r["elapsed_s"],

@@ -173,6 +173,13 @@ int lgca_set_kernel_variant(lgca_handle h, int variant);
  * No reference counterpart (introspection of this engine's scheduling). */
 int lgca_step_plan(lgca_handle h, int nsteps, int *family, int *launches);
 
+/* lgca_step_plan for a lattice of model and dim_x x dim_y with a new handle's
+ * settings (automatic kernel choice, one step per pass unless chosen
+ * otherwise) on the current device, without creating it.  Either pointer may
+ * be NULL.  Invalid dimensions as for lgca_create.
+ * No reference counterpart (introspection of this engine's scheduling). */
+int lgca_plan_shape(int model, int dim_x, int dim_y, int nsteps, int *family, int *launches);
+
 /* Launch shape of the one-step kernels: warps per block (1, 2, 4 or 8), or 0
  * to choose per launch the largest block whose grid spreads over the SMs with
  * the least wave-quantisation loss.  A tuning knob: results do not depend on

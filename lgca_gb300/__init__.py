@@ -74,6 +74,8 @@ def lib() -> C.CDLL:
             "lgca_set_temporal_depth": (C.c_int, [vp, C.c_int]),
             "lgca_set_kernel_variant": (C.c_int, [vp, C.c_int]),
             "lgca_step_plan": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+            "lgca_plan_shape": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int)]),
             "lgca_run_job_async": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]),
             "lgca_collide_and_propagate_sums": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp]),
             "lgca_set_block_warps": (C.c_int, [vp, C.c_int]),
@@ -139,6 +141,15 @@ def _check(h, status: int) -> None:
 def trim_memory(device: int = 0, keep_bytes: int = 0) -> None:
     """Return the lattice memory pool's unused blocks beyond keep_bytes."""
     _check(None, lib().lgca_trim_memory(int(device), int(keep_bytes)))
+
+
+def plan_shape(model: int, dim_x: int, dim_y: int, nsteps: int) -> tuple[int, int]:
+    """GpuLattice.step_plan of a new lattice of this model and shape (default
+    settings, current device), without creating it."""
+    fam, n = C.c_int(), C.c_int()
+    _check(None, lib().lgca_plan_shape(int(model), int(dim_x), int(dim_y), int(nsteps),
+                                       C.byref(fam), C.byref(n)))
+    return fam.value, n.value
 
 
 class GpuLattice:
@@ -473,5 +484,6 @@ class GpuBatch:
         self.close()
 
 
-__all__ = ["GpuBatch", "GpuLattice", "LgcaError", "build", "lib", "HPP", "FHP_I", "FHP_II", "FHP_III",
+__all__ = ["GpuBatch", "GpuLattice", "LgcaError", "build", "lib", "plan_shape", "trim_memory",
+           "HPP", "FHP_I", "FHP_II", "FHP_III",
            "FLUID", "SOLID_NO_SLIP", "SOLID_SLIP", "NUM_DIR"]

@@ -71,6 +71,19 @@ namespace {
 
 thread_local std::string g_err;
 
+// The plane layout of a W x H lattice: 64 sites per word, rows padded to an
+// even number of words.
+void set_plane_geom(PlaneGeom &g, int W, int H)
+{
+    g.W = W;
+    g.H = H;
+    g.nw = (W + 63) / 64;
+    g.pitch = (g.nw + 1) & ~1;
+    g.ps = (size_t)H * g.pitch;
+    g.L = (W - 1) & 63;
+    g.lastmask = (g.L == 63) ? ~0ull : ((1ull << (g.L + 1)) - 1ull);
+}
+
 int fail(lgca_lattice *h, int status, const char *fmt, ...)
 {
     char buf[512];
@@ -300,13 +313,7 @@ int lgca_create(int model, int W, int H, uint64_t seed, lgca_handle *out)
     h->D = num_dir(model);
     h->seed = seed;
     PlaneGeom &g = h->g;
-    g.W = W;
-    g.H = H;
-    g.nw = (W + 63) / 64;
-    g.pitch = (g.nw + 1) & ~1;
-    g.ps = (size_t)H * g.pitch;
-    g.L = (W - 1) & 63;
-    g.lastmask = (g.L == 63) ? ~0ull : ((1ull << (g.L + 1)) - 1ull);
+    set_plane_geom(g, W, H);
     cudaGetDevice(&h->device);
 
     cudaError_t e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
@@ -707,14 +714,9 @@ int run_resident(lgca_lattice *h, int nsteps, const ResidentShape &rs, const uin
     h->t += (uint64_t)nsteps;
     return LGCA_OK;
 }
-}  // namespace
-
-extern "C" {
-
-int lgca_step_plan(lgca_handle h, int nsteps, int *family, int *launches)
+// The family and step-kernel launches of a call of nsteps steps on h.
+void plan_counts(const lgca_lattice *h, int nsteps, int *family, int *launches)
 {
-    CHECK_VALID(h);
-    if (nsteps < 0) return fail(h, LGCA_ERR_INVALID, "nsteps < 0");
     const int f = step_family(h, nsteps, nullptr);
     int n = 0;
     if (f == VARIANT_PLAIN) {
@@ -727,6 +729,41 @@ int lgca_step_plan(lgca_handle h, int nsteps, int *family, int *launches)
     }
     if (family) *family = f == VARIANT_PLAIN ? 1 : f;
     if (launches) *launches = n;
+}
+}  // namespace
+
+extern "C" {
+
+int lgca_step_plan(lgca_handle h, int nsteps, int *family, int *launches)
+{
+    CHECK_VALID(h);
+    if (nsteps < 0) return fail(h, LGCA_ERR_INVALID, "nsteps < 0");
+    DeviceGuard dg(h->device);
+    plan_counts(h, nsteps, family, launches);
+    return LGCA_OK;
+}
+
+int lgca_plan_shape(int model, int W, int H, int nsteps, int *family, int *launches)
+{
+    if (model < LGCA_HPP || model > LGCA_FHP_III)
+        return fail(nullptr, LGCA_ERR_INVALID, "unknown model %d", model);
+    if (W < 1 || H < 1) return fail(nullptr, LGCA_ERR_INVALID, "invalid dimensions %d x %d", W, H);
+    if (model != LGCA_HPP && (H % 2) != 0)
+        return fail(nullptr, LGCA_ERR_INVALID,
+                    "FHP lattices need an even number of rows (dim_y = %d)", H);
+    if ((unsigned long long)W * (unsigned long long)H > 0x7fffffffULL)
+        return fail(nullptr, LGCA_ERR_INVALID, "lattice of %d x %d exceeds 2^31-1 cells", W, H);
+    if (nsteps < 0) return fail(nullptr, LGCA_ERR_INVALID, "nsteps < 0");
+    // a handle's default settings on the current device, with no memory
+    lgca_lattice h;
+    h.model = model;
+    h.D = num_dir(model);
+    set_plane_geom(h.g, W, H);
+    if (cudaGetDevice(&h.device) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(nullptr, LGCA_ERR_CUDA, "no CUDA device");
+    }
+    plan_counts(&h, nsteps, family, launches);
     return LGCA_OK;
 }
 

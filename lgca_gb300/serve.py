@@ -436,27 +436,65 @@ def fcfs_baseline(jobs, step_time, out_every: int = 500) -> dict:
 
 
 class StepTimeTable:
-    """Per-step time of the plain single-lattice kernel by (model, W, H),
-    measured once per shape class on the GPU and interpolated by site count,
-    and the per-job costs around the steps.
+    """Per-step time of single-lattice execution by (model, W, H), measured on
+    the GPU, and the per-job costs around the steps.
 
-    Each point is the wall time of `steps` steps of a lattice run alone
-    (launches included), repeated `repeats` times: `stat` "median" uses the
-    median repeat, "best" the fastest (the baseline at its best).  Each point
-    also holds the wall time of setting a job's lattice up (create, pipe
-    walls painted, occupation drawn, waited for) and of one field output
-    (16 x 16 block sums copied to the host), medians of `repeats`."""
+    Grid: widths 256 .. 8192 by powers of two, and the same widths plus 64
+    (8128 for the last), whose odd word counts take the one-step kernel's
+    padded last pair and never the resident kernel; heights 256 .. 4096 by
+    powers of two; two geometry classes, periodic and walls (pipe walls and a
+    forcing column, standing for the pipe and disc jobs, whose solid plane is
+    read alike).  Each point is a lattice of that shape and class run alone
+    with the automatic kernel choice in calls of `steps` steps (500: the
+    calls of the FCFS run between field outputs), `repeats` times, wall clock
+    with launches; it records the kernel family its calls take.  A job's
+    per-step time comes from the points of its model, geometry class,
+    word-count parity and kernel family (the family `plan` gives for its
+    shape, lgca_plan_shape by default): the time per site interpolated in
+    (log W, log H) by inverse squared distance over the nearest four such
+    points, or the point itself when the job's shape is on the grid.  `stat`
+    "median" uses the median repeat of each point, "best" the fastest.
 
-    def __init__(self, samples_per_model=(256, 512, 1024, 2048, 4096, 8192), steps: int = 50,
-                 repeats: int = 5, stat: str = "median"):
+    Set-up (create, pipe walls painted, occupation drawn, waited for) and one
+    field output (16 x 16 block sums copied to the host) are measured on the
+    shapes W x max(256, W / 2) of the power-of-two widths and interpolated by
+    site count."""
+
+    WIDTHS = (256, 512, 1024, 2048, 4096, 8192)
+    HEIGHTS = (256, 512, 1024, 2048, 4096)
+
+    def __init__(self, steps: int = 500, repeats: int = 3, stat: str = "median", plan=None):
         import lgca_gb300 as gpu
         self.stat = stat
-        self.samples = {}  # model -> [(sites, [seconds per step of each repeat])]
+        self.plan = plan
+        # model -> [(W, H, family, geometry class, [seconds per step of each repeat])]
+        self.samples = {}
         self.costs = {}    # model -> [(sites, setup seconds, output seconds)]
+        widths = self.WIDTHS + tuple(min(w + 64, 8128) for w in self.WIDTHS)
         for m in range(4):
-            pts, costs = [], []
-            for s in samples_per_model:
-                W, H = s, max(256, s // 2)
+            pts = []
+            for geo, W, H in ((geo, W, H) for geo in ("periodic", "walls") for W in widths
+                              for H in self.HEIGHTS):
+                L = gpu.GpuLattice(m, W, H, seed=1)
+                if geo == "walls":
+                    L.apply_bc_pipe()
+                    L.set_forcing_column(8, 0.01)
+                L.init_random(0.25, 0.25)
+                fam = L.step_plan(steps)[0]
+                L.collide_and_propagate(steps)
+                L.sync()
+                reps = []
+                for _ in range(repeats):
+                    t0 = time.perf_counter()
+                    L.collide_and_propagate(steps)
+                    L.sync()
+                    reps.append((time.perf_counter() - t0) / steps)
+                pts.append((W, H, fam, geo, reps))
+                L.close()
+            self.samples[m] = pts
+            costs = []
+            for W in self.WIDTHS:
+                H = max(256, W // 2)
                 setup = []
                 for _ in range(repeats):
                     t0 = time.perf_counter()
@@ -468,39 +506,52 @@ class StepTimeTable:
                     L.close()
                 L = gpu.GpuLattice(m, W, H, seed=1)
                 L.init_random(0.25, 0.25)
-                L.set_kernel_variant(0)  # the plain kernel: one step per pass, its fastest form
-                L.collide_and_propagate(10)
-                L.sync()
-                reps = []
-                for _ in range(repeats):
-                    t0 = time.perf_counter()
-                    L.collide_and_propagate(steps)
-                    L.sync()
-                    reps.append((time.perf_counter() - t0) / steps)
+                L.block_sums(16)
                 out = []
                 for _ in range(repeats):
                     t0 = time.perf_counter()
                     L.block_sums(16)
                     out.append(time.perf_counter() - t0)
-                pts.append((W * H, reps))
-                costs.append((W * H, float(np.median(setup)), float(np.median(out))))
                 L.close()
-            self.samples[m] = pts
+                costs.append((W * H, float(np.median(setup)), float(np.median(out))))
             self.costs[m] = costs
 
     def with_stat(self, stat: str) -> "StepTimeTable":
         """The same samples read with another statistic."""
         other = object.__new__(StepTimeTable)
-        other.samples, other.stat = self.samples, stat
-        other.costs = getattr(self, "costs", {})
+        other.__dict__.update(self.__dict__)
+        other.stat = stat
         return other
 
+    def family(self, job: Job) -> int:
+        """The kernel family of the job's calls when run alone."""
+        plan = getattr(self, "plan", None)
+        if plan is None:
+            import lgca_gb300 as gpu
+            plan = gpu.plan_shape
+        key = (job.model, job.W, job.H, min(500, job.steps))
+        cache = self.__dict__.setdefault("_families", {})
+        if key not in cache:
+            cache[key] = plan(*key)[0]
+        return cache[key]
+
     def __call__(self, job: Job) -> float:
-        pts = self.samples[job.model]
         f = np.min if self.stat == "best" else np.median
-        xs = np.log([p[0] for p in pts])
-        ys = np.log([f(p[1]) for p in pts])
-        return float(np.exp(np.interp(math.log(job.sites), xs, ys)))
+        odd = (job.W // 64) % 2
+        geo = "periodic" if job.geometry == "periodic" else "walls"
+        pts = [p for p in self.samples[job.model] if (p[0] // 64) % 2 == odd and p[3] == geo]
+        same = [p for p in pts if p[2] == self.family(job)]
+        pts = same or pts or self.samples[job.model]
+        lw, lh = math.log(job.W), math.log(job.H)
+        near = sorted(((math.log(p[0]) - lw) ** 2 + (math.log(p[1]) - lh) ** 2, i)
+                      for i, p in enumerate(pts))[:4]
+        near = [(d, pts[i]) for d, i in near]
+        per_site = lambda p: float(f(p[4])) / (p[0] * p[1])
+        if near[0][0] < 1e-12:
+            return per_site(near[0][1]) * job.sites
+        wts = [1.0 / d for d, _ in near]
+        log_ps = sum(w * math.log(per_site(p)) for w, (_, p) in zip(wts, near)) / sum(wts)
+        return math.exp(log_ps) * job.sites
 
     def job_overhead(self, job: Job, outputs: int) -> float:
         """Seconds a job spends outside its steps when run alone: set-up and

@@ -444,6 +444,19 @@ def test_step_plan_names_the_kernels_a_call_runs(gpu, oracle):
         assert L.step_plan(100) == (1, 100)
 
 
+def test_plan_shape_equals_a_new_lattices_step_plan(gpu):
+    """lgca_plan_shape gives, without a lattice, what a new lattice of that
+    shape reports; it refuses what lgca_create refuses."""
+    for model, W, H in [(3, 8192, 2048), (3, 2048, 1024), (3, 2048, 2048), (3, 4096, 256),
+                        (1, 4160, 64), (0, 8192, 8192), (0, 16384, 2048), (2, 320, 100)]:
+        with gpu.GpuLattice(model, W, H, seed=1) as L:
+            for n in (1, 15, 16, 63, 64, 100, 500):
+                assert gpu.plan_shape(model, W, H, n) == L.step_plan(n), (model, W, H, n)
+    for args in [(4, 64, 64, 10), (1, 64, 63, 10), (0, 0, 64, 10), (0, 64, 64, -1)]:
+        with pytest.raises(gpu.LgcaError):
+            gpu.plan_shape(*args)
+
+
 @pytest.mark.parametrize("model", [0, 1, 3])
 def test_run_job_equals_upload_steps_download(gpu, oracle, model):
     """lgca_run_job_async (state in, steps, state out in one call; the

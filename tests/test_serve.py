@@ -183,22 +183,46 @@ def test_fcfs_baseline_queueing():
 
 
 def test_step_time_table_statistics():
-    """Median and fastest repeat of each sample, interpolated log-log by site
-    count (the table's samples are set by hand; measuring them needs a GPU)."""
+    """A job's per-step time: the median (or fastest) repeat of the grid
+    points of its model, geometry class, word-count parity and kernel family, as time per
+    site interpolated in (log W, log H) by inverse squared distance (the
+    table's points are set by hand; measuring them needs a GPU)."""
     t = object.__new__(S.StepTimeTable)
     t.stat = "median"
-    t.samples = {m: [(1000, [3e-6, 1e-6, 2e-6]), (100000, [4e-4, 1e-4, 2e-4])] for m in range(4)}
-    job = S.Job(index=0, arrival=0.0, model=2, W=100, H=100, geometry="periodic", p=0.2,
-                steps=10, seed=0)  # 10^4 sites: halfway in log between the samples
-    assert t(job) == pytest.approx((2e-6 * 2e-4) ** 0.5)
-    assert t.with_stat("best")(job) == pytest.approx((1e-6 * 1e-4) ** 0.5)
+    fam = {}
+    t.plan = lambda m, W, H, n: (fam.get((W, H), 1), n)
+    pts = [(256, 256, 1, "periodic", [3e-6, 1e-6, 2e-6]),     # 2e-6 s per step at 65536 sites
+           (1024, 256, 1, "periodic", [8e-6, 16e-6, 32e-6]),  # 16e-6 at 262144
+           (320, 256, 1, "periodic", [1.0, 1.0, 1.0]),        # odd word count: other points
+           (1024, 1024, 6, "periodic", [4e-6, 4e-6, 4e-6]),   # another kernel family
+           (256, 256, 1, "walls", [5.0, 5.0, 5.0])]           # pipe and disc jobs
+    t.samples = {m: pts for m in range(4)}
+    job = lambda W, H: S.Job(index=0, arrival=0.0, model=2, W=W, H=H, geometry="periodic", p=0.2,
+                             steps=10, seed=0)
+    assert t(job(256, 256)) == pytest.approx(2e-6)  # on a point: that point
+    assert t.with_stat("best")(job(256, 256)) == pytest.approx(1e-6)
     assert t.stat == "median"
-    # per-job costs: set-up plus one field copy per output, interpolated alike
-    assert t.job_overhead(job, 3) == 0.0  # no measured costs
+    # halfway in log W between the two family-1 points of even word count:
+    # the per-site times' geometric mean (2e-6/65536 and 16e-6/262144)
+    want = ((2e-6 / 65536) * (16e-6 / 262144)) ** 0.5 * 512 * 256
+    assert t(job(512, 256)) == pytest.approx(want)
+    # the same shape on the resident path reads only family-6 points
+    fam[(512, 256)] = 6
+    t._families = {}
+    assert t(job(512, 256)) == pytest.approx(4e-6 / (1024 * 1024) * 512 * 256)
+    # an odd word count reads only the odd-width points
+    assert t(job(320, 256)) == pytest.approx(1.0)
+    # a job with walls or an obstacle reads the points with walls
+    disc = S.Job(index=1, arrival=0.0, model=2, W=256, H=256, geometry="disc", p=0.2, steps=10,
+                 seed=1)
+    assert t(disc) == pytest.approx(5.0)
+    # per-job costs: set-up plus one field copy per output, interpolated by sites
+    j = job(100, 100)
+    assert t.job_overhead(j, 3) == 0.0  # no measured costs
     t.costs = {m: [(1000, 1e-3, 1e-5), (100000, 1e-1, 1e-3)] for m in range(4)}
-    assert t.job_overhead(job, 3) == pytest.approx(1e-2 + 3 * 1e-4)
-    base = S.fcfs_baseline([job], t)  # 10 steps + set-up + one output
-    assert base["makespan_s"] == pytest.approx(10 * t(job) + 1e-2 + 1e-4)
+    assert t.job_overhead(j, 3) == pytest.approx(1e-2 + 3 * 1e-4)
+    base = S.fcfs_baseline([job(256, 256)], t)  # 10 steps + set-up + one output
+    assert base["makespan_s"] == pytest.approx(10 * 2e-6 + t.job_overhead(job(256, 256), 1))
 
 
 def test_job_stream_shapes():
