@@ -327,9 +327,12 @@ int lgca_create(int model, int W, int H, uint64_t seed, lgca_handle *out)
     int st = LGCA_OK;
     for (int i = 0; i < 2 && st == LGCA_OK; ++i)
         st = dalloc(h, reinterpret_cast<void **>(&h->buf[i]), state_bytes, true, "state buffer");
-    // the buffers are usable from any stream once this returns
-    if (st == LGCA_OK && (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
-        st = cuda_fail(h, e, "cudaStreamSynchronize");
+    // No wait here: the allocations and their zeroing are queued on the
+    // handle's stream like all of its work.  Every call of this library uses
+    // that stream, a batch orders its first call on a new member after the
+    // member's queued work, lgca_set_stream synchronises first, and callers
+    // order on lgca_stream.  (A wait here would stall admissions while a
+    // persistent batch launch holds the SMs.)
     if (st != LGCA_OK) {
         dfree(h, h->buf[0]);
         dfree(h, h->buf[1]);
