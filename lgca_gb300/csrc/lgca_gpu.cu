@@ -842,7 +842,10 @@ int lgca_collide_and_propagate_sums(lgca_handle h, int nsteps, int B, int32_t *N
     if (step_family(h, nsteps, &rs) == VARIANT_RESIDENT && resident_sums_fit(h->model, h->g, rs, B)) {
         // the sums fused into the step launch: its blocks add into zeroed arrays
         const size_t nb = (size_t)((h->g.W + B - 1) / B) * ((h->g.H + B - 1) / B);
-        for (int32_t *p : {N, Jx2, Jy}) CK(h, cudaMemsetAsync(p, 0, nb * sizeof(int32_t), h->stream));
+        if (Jx2 == N + nb && Jy == Jx2 + nb)  // one array of three planes: one memset
+            CK(h, cudaMemsetAsync(N, 0, 3 * nb * sizeof(int32_t), h->stream));
+        else
+            for (int32_t *p : {N, Jx2, Jy}) CK(h, cudaMemsetAsync(p, 0, nb * sizeof(int32_t), h->stream));
         const ResidentSums sums{B, N, Jx2, Jy};
         const int st = run_resident(h, nsteps, rs, nullptr, nullptr, &sums);
         if (st != RESIDENT_UNAVAILABLE) return st;

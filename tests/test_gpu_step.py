@@ -534,3 +534,12 @@ def test_steps_with_fused_block_sums(gpu, oracle, model):
                 got = sums.cpu().numpy()
                 for i, w in enumerate(oracle.block_sums(model, want2, B)):
                     assert np.array_equal(got[i], w), (W, H, variant, B, i)
+                if B == 32:  # three separate arrays (zeroed one by one)
+                    L.upload(want1)
+                    L.set_step(20)
+                    parts = [torch.full((-(-H // B), -(-W // B)), -1, dtype=torch.int32,
+                                        device="cuda") for _ in range(3)]
+                    L.collide_and_propagate_sums(20, B, *(p.data_ptr() for p in parts))
+                    L.sync()
+                    for p, w in zip(parts, oracle.block_sums(model, want2, B)):
+                        assert np.array_equal(p.cpu().numpy(), w), (W, H, variant)
