@@ -54,7 +54,8 @@ const char *lgca_status_string(int status);
 const char *lgca_last_error(lgca_handle h); /* h may be NULL: last global error */
 
 /* Allocate a dim_x x dim_y lattice of `model` on the current CUDA device,
- * all cells FLUID and empty, step counter 0.  FHP models need an even dim_y
+ * all cells FLUID and empty, step counter 0 (the zeroing is queued on the
+ * handle's stream; the call does not wait for it).  FHP models need an even dim_y
  * (src/lattice.cpp:141, src/omp_lattice.cpp:103-111).
  * Replaces: OMP_Lattice<M>::OMP_Lattice + allocate_memory
  *           (src/omp_lattice.cpp:75-88,457-471). */
@@ -314,7 +315,9 @@ int lgca_set_stream(lgca_handle h, void *stream);
 
 /* Device view of the current state: base pointer of plane 0, words between
  * consecutive planes, words between consecutive rows.  Valid until the next
- * call that steps or replaces the state. */
+ * call that steps or replaces the state.  Everything that writes the state,
+ * from lgca_create's zeroing on, is queued on the handle's stream: read it on
+ * that stream (lgca_stream) or after lgca_sync. */
 int lgca_state_device(lgca_handle h, const uint64_t **planes, size_t *plane_stride,
                       int *row_pitch);
 
