@@ -65,3 +65,20 @@ def test_invalid_arguments_rejected_before_touching_a_device():
         with pytest.raises(lgca_gb300.LgcaError) as e:
             lgca_gb300.GpuLattice(*args)
         assert e.value.status == 1
+
+
+def test_plan_shape_rejects_invalid_shapes_before_touching_a_device():
+    """lgca_plan_shape checks its arguments as lgca_create does, before it
+    asks for a device; without a GPU a valid shape fails loudly."""
+    import lgca_gb300
+    lgca_gb300.build()
+    for args in [(7, 64, 64, 10), (1, 64, 63, 10), (0, 0, 8, 10), (3, 70000, 70000, 10),
+                 (0, 64, 64, -1)]:
+        with pytest.raises(lgca_gb300.LgcaError) as e:
+            lgca_gb300.plan_shape(*args)
+        assert e.value.status == 1
+    import torch
+    if not torch.cuda.is_available():
+        with pytest.raises(lgca_gb300.LgcaError) as e:
+            lgca_gb300.plan_shape(3, 8192, 2048, 100)
+        assert e.value.status != 0
